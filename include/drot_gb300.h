@@ -1,0 +1,186 @@
+/*
+ * drot_gb300.h -- C ABI of the GB300 DROT solver (libdrot_gb300.so).
+ *
+ * Douglas-Rachford optimal transport with quadratic (QR) or group-lasso (GL)
+ * regularisation, as solved by WangZesen/Regularized-DROT.  Every entry point
+ * below replaces one interface of that reference (cited per declaration).
+ *
+ * Layout: C, X are column-major n_rows x n_cols float32 matrices (element
+ * (i, j) at j*n_rows + i), i.e. the reference's PyTorch [n_cols, n_rows]
+ * contiguous tensor.  p has n_rows entries, q has n_cols entries.
+ *
+ * Errors are returned as drot_status codes; nothing is printed.  Device entry
+ * points take an explicit cudaStream_t (0 = legacy default stream, as the
+ * reference uses) and a caller-owned workspace whose size the matching
+ * *_workspace_bytes function returns for the current device.
+ */
+#ifndef DROT_GB300_H
+#define DROT_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *drot_stream_t; /* == cudaStream_t */
+
+typedef enum {
+  DROT_OK = 0,
+  DROT_ERR_INVALID_ARG = 1,     /* bad shape, null pointer, bad parameter */
+  DROT_ERR_CUDA = 2,            /* a CUDA runtime call failed */
+  DROT_ERR_BARRIER_TIMEOUT = 3, /* a device-side grid barrier hit its time limit */
+  DROT_ERR_UNSUPPORTED = 4,     /* shape outside what the solver plans for */
+  DROT_ERR_WORKSPACE = 5        /* workspace too small or misaligned */
+} drot_status;
+
+/* Result of one solve, copied back to the host by the blocking entry points. */
+typedef struct {
+  int n_iter;          /* the reference's count: QR = index of the last
+                          iteration + 1 (max_iters + 1 without convergence,
+                          core/drot_qr.hpp:233); GL = iterations run
+                          (core/drot_glr.hpp:354) */
+  int iters_run;       /* iterations actually executed */
+  int converged;       /* 1 if the stop test passed */
+  int status;          /* drot_status of the device run */
+  int objective_valid; /* 0 when no objective-bearing iteration ran */
+  float objective;     /* <C, X> of the last even QR / last GL iteration */
+  double objective_f64;/* same, FP64 accumulation */
+  double residual;     /* absolute marginal residual ||X1-p, X^T1-q||_2 at the
+                          last stop test (-1 if none ran) */
+  double phase_ms[4];  /* device time of the solve split by stage, summed over
+                          iterations: fused X-update, first grid barrier,
+                          dual update, second grid barrier + stop test */
+} drot_result;
+
+/* Text for a drot_status code. */
+const char *drot_status_string(int status);
+
+/* Status of the last host-buffer wrapper call on this thread
+ * (drot_qr_wrapper / drot_gl_wrapper return a pointer, not a status). */
+int drot_last_status(void);
+
+/* ---------------------------------------------------------------------------
+ * Parameter helpers
+ * ------------------------------------------------------------------------- */
+
+/* Columns-per-block heuristic of the reference, kept for callers that size
+ * their own buffers with it: core/drot_qr.hpp:236-239 (_q_get_work_size_update_x)
+ * and core/drot_glr.hpp:357-360 (_gl_get_work_size_update_x). */
+int drot_q_get_work_size_update_x(int n_rows, int n_cols);
+int drot_gl_get_work_size_update_x(int n_rows, int n_cols);
+
+/* Group row boundaries bounds[0..n_groups] that the reference GL kernels use
+ * for NGROUPS contiguous classes (core/kernel_glr.hpp:79-80, 185-186, with
+ * the kernel choice of core/drot_glr.hpp:280). */
+int drot_gl_group_bounds(int n_rows, int n_groups, int *bounds);
+
+/* Initial state.  warm != 0: the reference warm start (X = 0 and constant
+ * phi1, phi2, a, b, alpha from step_size; core/drot_qr.hpp:321-346,
+ * pytorch/src/qr_drot_cuda_kernel.cu:107-133).  warm == 0: the cold start
+ * X = p q^T, a = b = phi = 0, alpha = 0 (core/kernel_qr.hpp:7-40,
+ * core/drot_qr.hpp:308-320).  All pointers are device pointers. */
+int drot_init_state(int n_rows, int n_cols, float step_size, int warm,
+                    const float *p, const float *q, float *x, float *a,
+                    float *b, float *phi1, float *phi2, float *alpha,
+                    drot_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * Device-pointer solve loops (state in/out)
+ * ------------------------------------------------------------------------- */
+
+/* Scratch bytes for drot_qr_solve / drot_gl_solve on the current device. */
+size_t drot_qr_workspace_bytes(int n_rows, int n_cols);
+size_t drot_gl_workspace_bytes(int n_rows, int n_cols, int n_groups);
+
+/* QR solve loop.  Replaces quadratic_regularizer_drot<float>
+ * (core/drot_qr.hpp:159-234): same parameters (step_size, scale = the QR
+ * divisor, max_iters, eps on the absolute residual), same state arrays x, a,
+ * b, phi1, phi2 and alpha (aux[4] there) read on entry and written on exit,
+ * same stop rule (even iterations, residual < eps, X unfolded on
+ * convergence).  The reference's partial-sum buffers are replaced by
+ * `workspace`.  With result != NULL the call waits for the stream and fills
+ * *result; with result == NULL it returns after enqueueing the work and the
+ * result can be read later with drot_read_result(workspace, ...). */
+int drot_qr_solve(const float *c, const float *p, const float *q, int n_rows,
+                  int n_cols, float step_size, float scale, int max_iters,
+                  float eps, float *x, float *a, float *b, float *phi1,
+                  float *phi2, float *alpha, void *workspace,
+                  size_t workspace_bytes, drot_result *result,
+                  drot_stream_t stream);
+
+/* GL solve loop.  Replaces group_lasso_regularizer_drot<float>
+ * (core/drot_glr.hpp:242-355): groups are the n_groups contiguous row blocks
+ * of drot_gl_group_bounds, lambda is the threshold used by the shrink
+ * max(1 - lambda/(||Y_g|| + 1e-9), 0), the stop test runs every iteration
+ * with residual <= eps. */
+int drot_gl_solve(const float *c, const float *p, const float *q, int n_rows,
+                  int n_cols, int n_groups, float step_size, float lambda,
+                  int max_iters, float eps, float *x, float *a, float *b,
+                  float *phi1, float *phi2, float *alpha, void *workspace,
+                  size_t workspace_bytes, drot_result *result,
+                  drot_stream_t stream);
+
+/* Copy the result block of the last solve that used `workspace` to the host
+ * (waits for `stream`). */
+int drot_read_result(const void *workspace, drot_result *result,
+                     drot_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * PyTorch-operator equivalents (device pointers, state kept in the workspace)
+ * ------------------------------------------------------------------------- */
+
+/* reg_drot.quadratic_drot (pytorch/src/drot_cuda.cpp:26-40,
+ * pytorch/src/qr_drot_cuda_kernel.cu:12-148): step = rho/(n_rows+n_cols),
+ * divisor = 1 + step*r_weight*(n_rows+n_cols), warm start, solve into x. */
+size_t drot_quadratic_drot_workspace_bytes(int n_rows, int n_cols);
+int drot_quadratic_drot(const float *c, const float *p, const float *q,
+                        int n_rows, int n_cols, float rho, float r_weight,
+                        int max_iters, float eps, float *x, void *workspace,
+                        size_t workspace_bytes, drot_result *result,
+                        drot_stream_t stream);
+
+/* reg_drot.group_lasso_drot (pytorch/src/drot_cuda.cpp:42-57,
+ * pytorch/src/glr_drot_cuda_kernel.cu:13-171): lambda =
+ * r_weight*sqrt(n_rows/n_class) with integer division, warm start. */
+size_t drot_group_lasso_drot_workspace_bytes(int n_rows, int n_cols, int n_class);
+int drot_group_lasso_drot(const float *c, const float *p, const float *q,
+                          int n_rows, int n_cols, int n_class, float rho,
+                          float r_weight, int max_iters, float eps, float *x,
+                          void *workspace, size_t workspace_bytes,
+                          drot_result *result, drot_stream_t stream);
+
+/* ---------------------------------------------------------------------------
+ * Host-buffer wrappers
+ * ------------------------------------------------------------------------- */
+
+/* quadratic_regularizer_drot_wrapper<float> (core/drot_qr.hpp:241-393):
+ * host C, p, q in; device buffers allocated, inputs copied, solved, freed.
+ * Returns a malloc'd host copy of X (column-major) when return_x != 0, else
+ * NULL; free it with free() or drot_free_host().  *dur_in_ms is the solve
+ * time, *prep_dur_in_ms the allocation + copy + initialisation time (CUDA
+ * events, as the reference measures them).  On failure returns NULL and
+ * drot_last_status() tells why. */
+float *drot_qr_wrapper(const float *c, const float *p, const float *q,
+                       int n_rows, int n_cols, float step_size,
+                       float r_weight, int max_iters, float eps,
+                       float *dur_in_ms, float *prep_dur_in_ms, int *n_iter,
+                       float *objective, int use_warmup_init, int return_x);
+
+/* group_lasso_regularizer_drot_wrapper<float> (core/drot_glr.hpp:362-527):
+ * as above; lambda = r_weight / sqrt(n_rows / NGROUPS) with integer division
+ * (core/drot_glr.hpp:385). */
+float *drot_gl_wrapper(const float *c, const float *p, const float *q,
+                       int n_rows, int n_cols, int n_groups, float step_size,
+                       float r_weight, int max_iters, float eps,
+                       float *dur_in_ms, float *prep_dur_in_ms, int *n_iter,
+                       float *objective, int use_warmup_init, int return_x);
+
+/* Frees a matrix returned by the wrappers. */
+void drot_free_host(float *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DROT_GB300_H */

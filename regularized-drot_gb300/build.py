@@ -1,0 +1,54 @@
+"""Build recipe of the solver library (libdrot_gb300.so) for sm_103a.
+
+One nvcc invocation compiles csrc/drot_api.cu (which includes the kernels)
+into reg_drot/libdrot_gb300.so, in tree.  Device code is compiled with
+--fmad=false: the kernels spell out every fused multiply-add they need
+(the ones the reference's kernels compile to), so nothing else is contracted.
+Host code is compiled with -ffp-contract=off so the parameter mapping rounds
+the same on x86-64 and aarch64 hosts.
+
+Usage: python regularized-drot_gb300/build.py [--force] [-v]
+"""
+import os
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(REPO, "include")
+OUT = os.path.join(PKG, "reg_drot", "libdrot_gb300.so")
+SOURCES = [os.path.join(CSRC, "drot_api.cu")]
+DEPS = SOURCES + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))] + \
+    [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+
+NVCC_FLAGS = [
+    "-gencode", "arch=compute_103a,code=sm_103a",
+    "-lineinfo", "-O3", "-std=c++17", "--fmad=false",
+    "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+    "-shared",
+]
+
+
+def nvcc():
+    cand = os.environ.get("NVCC") or os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"),
+                                                   "bin", "nvcc")
+    return cand if os.path.exists(cand) else "nvcc"
+
+
+def build(force=False, verbose=False, extra=()):
+    """Compile libdrot_gb300.so if missing or stale; return its path."""
+    newest = max(os.path.getmtime(f) for f in DEPS)
+    if not force and os.path.exists(OUT) and os.path.getmtime(OUT) >= newest:
+        return OUT
+    cmd = [nvcc(), *NVCC_FLAGS, *extra, "-I", INCLUDE, "-I", CSRC, "-o", OUT + ".tmp", *SOURCES]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    subprocess.check_call(cmd)
+    os.replace(OUT + ".tmp", OUT)
+    return OUT
+
+
+if __name__ == "__main__":
+    extra = ["-Xptxas", "-v"] if "-v" in sys.argv else []
+    print(build(force="--force" in sys.argv or bool(extra), verbose=True, extra=extra))

@@ -1,0 +1,737 @@
+// drot_api.cu -- host side of the GB300 DROT solver: launch planning,
+// workspace layout, the cooperative launch, and the extern "C" entry points
+// declared in include/drot_gb300.h.
+//
+// Host arithmetic that mirrors the reference's parameter mapping is compiled
+// with -ffp-contract=off (see build.py) so it rounds like the reference's
+// x86-64 host code on every host architecture.
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "drot_gb300.h"
+#include "drot_kernels.cuh"
+
+namespace drot {
+
+// ---------------------------------------------------------------------------
+// kernel table
+// ---------------------------------------------------------------------------
+
+typedef void (*SolveFn)(const SolveParams);
+
+template <int MODE, bool TMA>
+static SolveFn kernel_kv(int vec, int kv) {
+  if constexpr (TMA) {
+    if (vec != 4) return nullptr;
+    if (kv == 1) return drot_solve_kernel<MODE, 4, 1, true>;
+    if (kv == 2) return drot_solve_kernel<MODE, 4, 2, true>;
+    if (kv == 4) return drot_solve_kernel<MODE, 4, 4, true>;
+    if constexpr (MODE == MODE_GL) {
+      if (kv == 8) return drot_solve_kernel<MODE, 4, 8, true>;
+    }
+  } else {
+    if (vec == 4) {
+      if (kv == 1) return drot_solve_kernel<MODE, 4, 1, false>;
+      if (kv == 2) return drot_solve_kernel<MODE, 4, 2, false>;
+      if (kv == 4) return drot_solve_kernel<MODE, 4, 4, false>;
+      if constexpr (MODE == MODE_GL) {
+        if (kv == 8) return drot_solve_kernel<MODE, 4, 8, false>;
+      }
+    } else {
+      if (kv == 1) return drot_solve_kernel<MODE, 1, 1, false>;
+      if (kv == 2) return drot_solve_kernel<MODE, 1, 2, false>;
+      if (kv == 4) return drot_solve_kernel<MODE, 1, 4, false>;
+      if constexpr (MODE == MODE_GL) {
+        if (kv == 8) return drot_solve_kernel<MODE, 1, 8, false>;
+      }
+    }
+  }
+  return nullptr;
+}
+
+static SolveFn kernel_for(int mode, int vec, int kv, bool tma) {
+  if (mode == MODE_QR) return tma ? kernel_kv<MODE_QR, true>(vec, kv) : kernel_kv<MODE_QR, false>(vec, kv);
+  return tma ? kernel_kv<MODE_GL, true>(vec, kv) : kernel_kv<MODE_GL, false>(vec, kv);
+}
+
+// ---------------------------------------------------------------------------
+// small helper kernels (initial state)
+// ---------------------------------------------------------------------------
+
+__global__ void fill_kernel(float* __restrict__ v, long long n, float val) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    v[i] = val;
+}
+
+// Cold start X = p q^T (init_x, core/kernel_qr.hpp:7-40): x = p_i * q_j.
+__global__ void outer_kernel(float* __restrict__ x, const float* __restrict__ p,
+                             const float* __restrict__ q, int nr, int nc) {
+  const long long n = (long long)nr * nc;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(t / nr);
+    const int i = (int)(t - (long long)j * nr);
+    x[t] = p[i] * q[j];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// planning
+// ---------------------------------------------------------------------------
+
+static const size_t kAlign = 256;
+static inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+// Scratch layout (offsets from the workspace base):
+//   [0, 256)     DeviceStats
+//   [256, 512)   barrier counter + abort flag
+//   rowpart      P * nr floats
+//   colpart      nsb * nc floats
+//   cta_sum/obj/res  grid doubles each
+struct Plan {
+  int mode = 0, vec = 4, kv = 4, wt = 1, threads = 256, nbands = 1, P = 1, grid = 1, nsb = 1;
+  int band_h = 0, ns = 1;
+  bool tma = false;
+  size_t smem = 0;
+  std::vector<int> bounds;
+  size_t off_stats = 0, off_ctrl = 256, off_rowpart = 0, off_colpart = 0, off_sum = 0,
+         off_obj = 0, off_res = 0, total = 0;
+};
+
+struct DeviceInfo {
+  int dev = 0, sms = 0, smem_optin = 0;
+  bool ok = false;
+};
+
+static DeviceInfo device_info() {
+  DeviceInfo d;
+  if (cudaGetDevice(&d.dev) != cudaSuccess) return d;
+  if (cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, d.dev) != cudaSuccess)
+    return d;
+  cudaDeviceGetAttribute(&d.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, d.dev);
+  int coop = 0;
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, d.dev);
+  d.ok = coop != 0 && d.sms > 0;
+  return d;
+}
+
+// Reference group boundaries (core/kernel_glr.hpp:79-80 with +0.49 for the
+// single-pass kernel chosen when ceil(n_rows/G) <= 256, drot_glr.hpp:280;
+// core/kernel_glr.hpp:185-186 with +0.49999 otherwise).
+static void group_bounds(int nr, int G, int* out) {
+  const int small = ((nr + G - 1) / G) <= 256;
+  const double off = small ? 0.49 : 0.49999;
+  const float per = (float)nr / (float)G;
+  for (int k = 0; k <= G; ++k) {
+    const float f = per * (float)k;
+    out[k] = (int)((double)f + off);
+  }
+}
+
+static int occupancy(SolveFn fn, int threads, size_t smem) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void*)fn, threads, smem) !=
+      cudaSuccess)
+    return 0;
+  return nb;
+}
+
+// Warps per CTA on the TMA path (DROT_TMA_WARPS, 4..16, default 16).
+static int tma_warps() {
+  const char* e = getenv("DROT_TMA_WARPS");
+  const int w = e ? atoi(e) : 0;
+  return (w >= 4 && w <= 16) ? w : 16;
+}
+
+// Build the launch plan for one data path (tma: shared-memory TMA ring, else
+// register loads).  Returns a drot_status.
+static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma, Plan& pl) {
+  if (nr <= 0 || nc <= 0) return DROT_ERR_INVALID_ARG;
+  if (tma && vec != 4) return DROT_ERR_UNSUPPORTED;
+  const DeviceInfo dev = device_info();
+  if (!dev.ok) return DROT_ERR_CUDA;
+  pl = Plan();
+  pl.mode = mode;
+  pl.vec = vec;
+  pl.tma = tma;
+  const int SV = 32 * vec;
+  if (mode == MODE_QR) {
+    pl.kv = nr <= SV ? 1 : (nr <= 2 * SV ? 2 : 4);
+    pl.wt = 1;
+  } else {
+    if (G <= 0) return DROT_ERR_INVALID_ARG;
+    if (G > kMaxGroups) return DROT_ERR_UNSUPPORTED;
+    pl.bounds.resize(G + 1);
+    group_bounds(nr, G, pl.bounds.data());
+    int hmax = 0;
+    for (int g = 0; g < G; ++g) {
+      const int lo = pl.bounds[g];
+      const int base = lo - lo % vec;
+      hmax = std::max(hmax, pl.bounds[g + 1] - base);
+    }
+    hmax = std::max(hmax, 1);
+    pl.kv = 0;
+    for (int kv : {1, 2, 4, 8})
+      if (SV * kv >= hmax) { pl.kv = kv; break; }
+    if (pl.kv == 0) {
+      pl.kv = 8;
+      pl.wt = (hmax + 8 * SV - 1) / (8 * SV);
+      if (pl.wt > 16) return DROT_ERR_UNSUPPORTED;
+    } else {
+      pl.wt = 1;
+    }
+  }
+  const int S = SV * pl.kv;
+  SolveFn fn = kernel_for(mode, vec, pl.kv, tma);
+  if (!fn) return DROT_ERR_UNSUPPORTED;
+  const size_t budget = (size_t)std::max(dev.smem_optin, 48 * 1024) - 1024;
+
+  const int wtarget = tma ? tma_warps() : 8;
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    int teams = pl.wt >= wtarget ? 1 : std::max(1, wtarget / pl.wt);
+    int warps = teams * pl.wt;
+    if (tma) {
+      // Deepest ring that fits; fewer teams when two stages do not fit.
+      for (;;) {
+        const size_t fixed = solve_smem_bytes(warps, pl.wt, S, 0, true);
+        const size_t stage = solve_smem_bytes(warps, pl.wt, S, 1, true) - fixed;
+        const size_t fit = budget > fixed ? (budget - fixed) / stage : 0;
+        if (fit >= 2) {
+          pl.ns = (int)std::min<size_t>(fit, 8);
+          break;
+        }
+        if (teams == 1) return DROT_ERR_UNSUPPORTED;
+        teams = teams / 2;
+        warps = teams * pl.wt;
+      }
+    } else {
+      pl.ns = 1;
+    }
+    pl.threads = 32 * warps;
+    pl.smem = solve_smem_bytes(warps, pl.wt, S, pl.ns, tma);
+    if (pl.smem > budget) return DROT_ERR_UNSUPPORTED;
+    if (pl.smem > 48 * 1024 &&
+        cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)pl.smem) != cudaSuccess)
+      return DROT_ERR_CUDA;
+    const int occ = occupancy(fn, pl.threads, pl.smem);
+    if (occ <= 0) return DROT_ERR_CUDA;
+    const int max_grid = occ * dev.sms;
+    if (mode == MODE_QR) {
+      pl.band_h = pl.wt * S;
+      pl.nbands = (nr + pl.band_h - 1) / pl.band_h;
+      if (pl.nbands > max_grid) {
+        if (pl.wt >= 16) return DROT_ERR_UNSUPPORTED;
+        pl.wt = std::min(16, pl.wt * 2);
+        continue;
+      }
+    } else {
+      pl.nbands = G;
+      if (G > max_grid) return DROT_ERR_UNSUPPORTED;
+    }
+    const int per_band = std::max(1, max_grid / pl.nbands);
+    const int by_cols = std::max(1, (nc + teams * 2 - 1) / (teams * 2));
+    pl.P = std::max(1, std::min(per_band, by_cols));
+    pl.grid = pl.nbands * pl.P;
+    pl.nsb = pl.nbands * pl.wt;
+    break;
+  }
+  if (pl.grid <= 0 || pl.nbands <= 0) return DROT_ERR_UNSUPPORTED;
+
+  size_t off = 512;
+  pl.off_stats = 0;
+  pl.off_ctrl = 256;
+  pl.off_rowpart = off;
+  off = align_up(off + sizeof(float) * (size_t)pl.P * nr);
+  pl.off_colpart = off;
+  off = align_up(off + sizeof(float) * (size_t)pl.nsb * nc);
+  pl.off_sum = off;
+  off = align_up(off + sizeof(double) * pl.grid);
+  pl.off_obj = off;
+  off = align_up(off + sizeof(double) * pl.grid);
+  pl.off_res = off;
+  off = align_up(off + sizeof(double) * pl.grid);
+  pl.total = off;
+  return DROT_OK;
+}
+
+// Plans are cached per (device, mode, shape, path): planning queries the
+// occupancy calculator, which costs microseconds per call.
+struct PlanKey {
+  int dev, mode, nr, nc, G, vec, tma, warps;
+  bool operator==(const PlanKey& o) const {
+    return dev == o.dev && mode == o.mode && nr == o.nr && nc == o.nc && G == o.G &&
+           vec == o.vec && tma == o.tma && warps == o.warps;
+  }
+};
+
+static std::mutex g_plan_mu;
+static std::vector<std::pair<PlanKey, Plan>> g_plans;
+
+static int make_plan(int mode, int nr, int nc, int G, int vec, bool tma, Plan& pl) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return DROT_ERR_CUDA;
+  const PlanKey key = {dev, mode, nr, nc, mode == MODE_GL ? G : 0, vec, tma ? 1 : 0,
+                       tma ? tma_warps() : 8};
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    for (auto& e : g_plans)
+      if (e.first == key) { pl = e.second; return DROT_OK; }
+  }
+  const int rc = make_plan_uncached(mode, nr, nc, G, vec, tma, pl);
+  if (rc == DROT_OK) {
+    std::lock_guard<std::mutex> lk(g_plan_mu);
+    if (g_plans.size() >= 64) g_plans.erase(g_plans.begin());
+    g_plans.emplace_back(key, pl);
+  }
+  return rc;
+}
+
+// Data path override for tests and measurements: DROT_PATH=reg forces the
+// register path, DROT_PATH=tma requires the TMA ring.
+static int path_override() {
+  const char* e = getenv("DROT_PATH");
+  if (!e) return 0;
+  if (!strcmp(e, "reg")) return 1;
+  if (!strcmp(e, "tma")) return 2;
+  return 0;
+}
+
+// Plan for the given alignment: the TMA ring when the data allow it.
+static int choose_plan(int mode, int nr, int nc, int G, bool aligned4, Plan& pl) {
+  const int ov = path_override();
+  if (aligned4 && ov != 1) {
+    const int rc = make_plan(mode, nr, nc, G, 4, true, pl);
+    if (rc == DROT_OK || ov == 2) return rc;
+  }
+  if (ov == 2) return DROT_ERR_UNSUPPORTED;
+  return make_plan(mode, nr, nc, G, aligned4 ? 4 : 1, false, pl);
+}
+
+static size_t scratch_bytes(int mode, int nr, int nc, int G) {
+  size_t best = 0;
+  Plan pl;
+  if (make_plan(mode, nr, nc, G, 4, true, pl) == DROT_OK) best = std::max(best, pl.total);
+  if (make_plan(mode, nr, nc, G, 4, false, pl) == DROT_OK) best = std::max(best, pl.total);
+  if (make_plan(mode, nr, nc, G, 1, false, pl) == DROT_OK) best = std::max(best, pl.total);
+  return best;
+}
+
+static long long barrier_timeout_ns() {
+  const char* e = getenv("DROT_BARRIER_TIMEOUT_MS");
+  if (e && *e) {
+    const long long ms = atoll(e);
+    if (ms > 0) return ms * 1000000LL;
+  }
+  return 10000LL * 1000000LL;  // 10 s
+}
+
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+struct SolveArgs {
+  int mode;
+  const float *c, *p, *q;
+  int nr, nc, G;
+  float s, kappa, lambda;
+  int max_iters;
+  float eps;
+  float *x, *a, *b, *phi1, *phi2, *alpha;
+  void* ws;
+  size_t ws_bytes;
+  cudaStream_t stream;
+};
+
+static int read_stats(const void* ws, drot_result* r, cudaStream_t stream) {
+  DeviceStats st;
+  if (cudaMemcpyAsync(&st, ws, sizeof(st), cudaMemcpyDeviceToHost, stream) != cudaSuccess)
+    return DROT_ERR_CUDA;
+  if (cudaStreamSynchronize(stream) != cudaSuccess) return DROT_ERR_CUDA;
+  r->n_iter = st.n_iter;
+  r->iters_run = st.iters_run;
+  r->converged = st.converged;
+  r->status = st.status;
+  r->objective_valid = st.objective_valid;
+  r->objective = (float)st.objective;
+  r->objective_f64 = st.objective;
+  r->residual = st.residual;
+  for (int k = 0; k < 4; ++k) r->phase_ms[k] = st.phase_ns[k] * 1e-6;
+  return st.status == 0 ? DROT_OK : st.status;
+}
+
+static int run_solve(const SolveArgs& A, drot_result* result) {
+  if (!A.c || !A.p || !A.q || !A.x || !A.a || !A.b || !A.phi1 || !A.phi2 || !A.alpha || !A.ws)
+    return DROT_ERR_INVALID_ARG;
+  if (A.nr <= 0 || A.nc <= 0 || A.max_iters < 0) return DROT_ERR_INVALID_ARG;
+  if (((uintptr_t)A.ws & (kAlign - 1)) != 0) return DROT_ERR_WORKSPACE;
+  const long long ld = A.nr;
+  const bool aligned4 = ld % 4 == 0 && aligned16(A.x) && aligned16(A.c);
+  Plan pl;
+  int rc = choose_plan(A.mode, A.nr, A.nc, A.G, aligned4, pl);
+  if (rc != DROT_OK) return rc;
+  if (A.ws_bytes < pl.total) return DROT_ERR_WORKSPACE;
+
+  char* ws = (char*)A.ws;
+  SolveParams prm;
+  memset(&prm, 0, sizeof(prm));
+  prm.c = A.c; prm.p = A.p; prm.q = A.q; prm.x = A.x;
+  prm.a = A.a; prm.b = A.b; prm.phi1 = A.phi1; prm.phi2 = A.phi2; prm.alpha = A.alpha;
+  prm.ld = ld; prm.nr = A.nr; prm.nc = A.nc;
+  prm.s = A.s; prm.kappa = A.kappa; prm.lambda = A.lambda; prm.eps = A.eps;
+  // RN(1/kappa): the double quotient rounded to float is the correctly
+  // rounded float reciprocal (53 >= 2*24 + 2).
+  prm.kappa_rcp = (float)(1.0 / (double)A.kappa);
+  prm.norm_eps = 1e-9;
+  prm.max_iters = A.max_iters;
+  prm.nbands = pl.nbands; prm.P = pl.P; prm.Wt = pl.wt; prm.nsb = pl.nsb;
+  prm.band_h = pl.band_h;
+  prm.ns = pl.ns;
+  for (size_t k = 0; k < pl.bounds.size(); ++k) prm.gbounds[k] = pl.bounds[k];
+  prm.rowpart = (float*)(ws + pl.off_rowpart);
+  prm.colpart = (float*)(ws + pl.off_colpart);
+  prm.cta_sum = (double*)(ws + pl.off_sum);
+  prm.cta_obj = (double*)(ws + pl.off_obj);
+  prm.cta_res = (double*)(ws + pl.off_res);
+  prm.bar = (unsigned int*)(ws + pl.off_ctrl);
+  prm.abort_flag = (int*)(ws + pl.off_ctrl + 64);
+  prm.stats = (DeviceStats*)(ws + pl.off_stats);
+  prm.timeout_ns = barrier_timeout_ns();
+
+  if (cudaMemsetAsync(ws, 0, 512, A.stream) != cudaSuccess) return DROT_ERR_CUDA;
+  SolveFn fn = kernel_for(A.mode, pl.vec, pl.kv, pl.tma);
+  if (pl.smem > 48 * 1024 &&
+      cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)pl.smem) != cudaSuccess)
+    return DROT_ERR_CUDA;
+  void* args[] = {(void*)&prm};
+  if (cudaLaunchCooperativeKernel((const void*)fn, dim3(pl.grid), dim3(pl.threads), args,
+                                  pl.smem, A.stream) != cudaSuccess) {
+    cudaGetLastError();
+    return DROT_ERR_CUDA;
+  }
+  if (result) return read_stats(ws, result, A.stream);
+  return DROT_OK;
+}
+
+static int init_state(int nr, int nc, float s, int warm, const float* p, const float* q,
+                      float* x, float* a, float* b, float* phi1, float* phi2, float* alpha,
+                      cudaStream_t st) {
+  if (nr <= 0 || nc <= 0 || !x || !a || !b || !phi1 || !phi2 || !alpha)
+    return DROT_ERR_INVALID_ARG;
+  const int th = 256;
+  auto blocks = [](long long n) { return (int)std::min<long long>((n + 255) / 256, 4096); };
+  if (warm) {
+    // core/drot_qr.hpp:322-331: _k = 1*s*n*m - 2; phi1 = (_k+2)/n/(m+n); ...
+    const float n = (float)nr, m = (float)nc;
+    float k = 1.0f * s;
+    k = k * n;
+    k = k * m;
+    k = k - 2.0f;
+    float t = (k + 2.0f) / n;
+    const float v_phi1 = t / (m + n);
+    t = (k + 2.0f) / m;
+    const float v_phi2 = t / (m + n);
+    const float v_a = (k + 1.0f) / n;
+    const float v_b = (k + 1.0f) / m;
+    const float v_alpha = k + 1.0f;
+    if (cudaMemsetAsync(x, 0, sizeof(float) * (size_t)nr * nc, st) != cudaSuccess)
+      return DROT_ERR_CUDA;
+    fill_kernel<<<blocks(nr), th, 0, st>>>(phi1, nr, v_phi1);
+    fill_kernel<<<blocks(nc), th, 0, st>>>(phi2, nc, v_phi2);
+    fill_kernel<<<blocks(nr), th, 0, st>>>(a, nr, v_a);
+    fill_kernel<<<blocks(nc), th, 0, st>>>(b, nc, v_b);
+    fill_kernel<<<1, 32, 0, st>>>(alpha, 1, v_alpha);
+  } else {
+    if (!p || !q) return DROT_ERR_INVALID_ARG;
+    outer_kernel<<<blocks((long long)nr * nc), th, 0, st>>>(x, p, q, nr, nc);
+    fill_kernel<<<blocks(nr), th, 0, st>>>(phi1, nr, 0.0f);
+    fill_kernel<<<blocks(nc), th, 0, st>>>(phi2, nc, 0.0f);
+    fill_kernel<<<blocks(nr), th, 0, st>>>(a, nr, 0.0f);
+    fill_kernel<<<blocks(nc), th, 0, st>>>(b, nc, 0.0f);
+    fill_kernel<<<1, 32, 0, st>>>(alpha, 1, 0.0f);
+  }
+  return cudaGetLastError() == cudaSuccess ? DROT_OK : DROT_ERR_CUDA;
+}
+
+// State region used by the operator-style entry points: a, b, phi1, phi2, alpha.
+struct StateLayout {
+  size_t off_a, off_b, off_phi1, off_phi2, off_alpha, total;
+};
+
+static StateLayout state_layout(size_t base, int nr, int nc) {
+  StateLayout L;
+  size_t off = align_up(base);
+  L.off_a = off; off = align_up(off + sizeof(float) * nr);
+  L.off_b = off; off = align_up(off + sizeof(float) * nc);
+  L.off_phi1 = off; off = align_up(off + sizeof(float) * nr);
+  L.off_phi2 = off; off = align_up(off + sizeof(float) * nc);
+  L.off_alpha = off; off = align_up(off + sizeof(float));
+  L.total = off;
+  return L;
+}
+
+static thread_local int g_last_status = DROT_OK;
+
+}  // namespace drot
+
+using namespace drot;
+
+// ---------------------------------------------------------------------------
+// extern "C" entry points
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+const char* drot_status_string(int status) {
+  switch (status) {
+    case DROT_OK: return "ok";
+    case DROT_ERR_INVALID_ARG: return "invalid argument";
+    case DROT_ERR_CUDA: return "CUDA runtime error";
+    case DROT_ERR_BARRIER_TIMEOUT: return "device grid barrier timed out";
+    case DROT_ERR_UNSUPPORTED: return "unsupported shape";
+    case DROT_ERR_WORKSPACE: return "workspace too small or misaligned";
+    default: return "unknown status";
+  }
+}
+
+int drot_last_status(void) { return g_last_status; }
+
+int drot_q_get_work_size_update_x(int n_rows, int n_cols) {
+  // core/drot_qr.hpp:236-239
+  const int l2 = (int)round(log2(std::max(n_rows, n_cols) * 0.002793 + 3.480));
+  return (int)exp2((double)std::min(std::max(l2, 2), 6));
+}
+
+int drot_gl_get_work_size_update_x(int n_rows, int n_cols) {
+  // core/drot_glr.hpp:357-360 (same heuristic)
+  return drot_q_get_work_size_update_x(n_rows, n_cols);
+}
+
+int drot_gl_group_bounds(int n_rows, int n_groups, int* bounds) {
+  if (n_rows <= 0 || n_groups <= 0 || !bounds) return DROT_ERR_INVALID_ARG;
+  group_bounds(n_rows, n_groups, bounds);
+  return DROT_OK;
+}
+
+int drot_init_state(int n_rows, int n_cols, float step_size, int warm, const float* p,
+                    const float* q, float* x, float* a, float* b, float* phi1, float* phi2,
+                    float* alpha, drot_stream_t stream) {
+  return init_state(n_rows, n_cols, step_size, warm, p, q, x, a, b, phi1, phi2, alpha,
+                    (cudaStream_t)stream);
+}
+
+size_t drot_qr_workspace_bytes(int n_rows, int n_cols) {
+  return scratch_bytes(MODE_QR, n_rows, n_cols, 0);
+}
+
+size_t drot_gl_workspace_bytes(int n_rows, int n_cols, int n_groups) {
+  return scratch_bytes(MODE_GL, n_rows, n_cols, n_groups);
+}
+
+int drot_qr_solve(const float* c, const float* p, const float* q, int n_rows, int n_cols,
+                  float step_size, float scale, int max_iters, float eps, float* x, float* a,
+                  float* b, float* phi1, float* phi2, float* alpha, void* workspace,
+                  size_t workspace_bytes, drot_result* result, drot_stream_t stream) {
+  SolveArgs A = {MODE_QR, c, p, q, n_rows, n_cols, 0, step_size, scale, 0.0f, max_iters,
+                 eps, x, a, b, phi1, phi2, alpha, workspace, workspace_bytes,
+                 (cudaStream_t)stream};
+  if (!(scale > 0.0f)) return DROT_ERR_INVALID_ARG;
+  return run_solve(A, result);
+}
+
+int drot_gl_solve(const float* c, const float* p, const float* q, int n_rows, int n_cols,
+                  int n_groups, float step_size, float lambda, int max_iters, float eps,
+                  float* x, float* a, float* b, float* phi1, float* phi2, float* alpha,
+                  void* workspace, size_t workspace_bytes, drot_result* result,
+                  drot_stream_t stream) {
+  if (n_groups <= 0) return DROT_ERR_INVALID_ARG;
+  SolveArgs A = {MODE_GL, c, p, q, n_rows, n_cols, n_groups, step_size, 1.0f, lambda,
+                 max_iters, eps, x, a, b, phi1, phi2, alpha, workspace, workspace_bytes,
+                 (cudaStream_t)stream};
+  return run_solve(A, result);
+}
+
+int drot_read_result(const void* workspace, drot_result* result, drot_stream_t stream) {
+  if (!workspace || !result) return DROT_ERR_INVALID_ARG;
+  return read_stats(workspace, result, (cudaStream_t)stream);
+}
+
+size_t drot_quadratic_drot_workspace_bytes(int n_rows, int n_cols) {
+  const size_t sc = scratch_bytes(MODE_QR, n_rows, n_cols, 0);
+  if (sc == 0) return 0;
+  return state_layout(sc, n_rows, n_cols).total;
+}
+
+size_t drot_group_lasso_drot_workspace_bytes(int n_rows, int n_cols, int n_class) {
+  const size_t sc = scratch_bytes(MODE_GL, n_rows, n_cols, n_class);
+  if (sc == 0) return 0;
+  return state_layout(sc, n_rows, n_cols).total;
+}
+
+int drot_quadratic_drot(const float* c, const float* p, const float* q, int n_rows, int n_cols,
+                        float rho, float r_weight, int max_iters, float eps, float* x,
+                        void* workspace, size_t workspace_bytes, drot_result* result,
+                        drot_stream_t stream) {
+  if (n_rows <= 0 || n_cols <= 0 || !workspace) return DROT_ERR_INVALID_ARG;
+  const size_t sc = scratch_bytes(MODE_QR, n_rows, n_cols, 0);
+  if (sc == 0) return DROT_ERR_UNSUPPORTED;
+  const StateLayout L = state_layout(sc, n_rows, n_cols);
+  if (workspace_bytes < L.total) return DROT_ERR_WORKSPACE;
+  char* ws = (char*)workspace;
+  // pytorch/src/qr_drot_cuda_kernel.cu:100-102
+  const float s = rho / ((float)n_rows + (float)n_cols);
+  float t = s * r_weight;
+  t = t * (float)(n_rows + n_cols);
+  const float kappa = 1.0f + t;
+  float *a = (float*)(ws + L.off_a), *b = (float*)(ws + L.off_b);
+  float *phi1 = (float*)(ws + L.off_phi1), *phi2 = (float*)(ws + L.off_phi2);
+  float* alpha = (float*)(ws + L.off_alpha);
+  int rc = init_state(n_rows, n_cols, s, 1, p, q, x, a, b, phi1, phi2, alpha,
+                      (cudaStream_t)stream);
+  if (rc != DROT_OK) return rc;
+  return drot_qr_solve(c, p, q, n_rows, n_cols, s, kappa, max_iters, eps, x, a, b, phi1, phi2,
+                       alpha, workspace, sc, result, stream);
+}
+
+int drot_group_lasso_drot(const float* c, const float* p, const float* q, int n_rows,
+                          int n_cols, int n_class, float rho, float r_weight, int max_iters,
+                          float eps, float* x, void* workspace, size_t workspace_bytes,
+                          drot_result* result, drot_stream_t stream) {
+  if (n_rows <= 0 || n_cols <= 0 || n_class <= 0 || !workspace) return DROT_ERR_INVALID_ARG;
+  const size_t sc = scratch_bytes(MODE_GL, n_rows, n_cols, n_class);
+  if (sc == 0) return DROT_ERR_UNSUPPORTED;
+  const StateLayout L = state_layout(sc, n_rows, n_cols);
+  if (workspace_bytes < L.total) return DROT_ERR_WORKSPACE;
+  char* ws = (char*)workspace;
+  // pytorch/src/glr_drot_cuda_kernel.cu:255-257
+  const float s = rho / ((float)n_rows + (float)n_cols);
+  const float lambda = (float)((double)r_weight * sqrt((double)(n_rows / n_class)));
+  float *a = (float*)(ws + L.off_a), *b = (float*)(ws + L.off_b);
+  float *phi1 = (float*)(ws + L.off_phi1), *phi2 = (float*)(ws + L.off_phi2);
+  float* alpha = (float*)(ws + L.off_alpha);
+  int rc = init_state(n_rows, n_cols, s, 1, p, q, x, a, b, phi1, phi2, alpha,
+                      (cudaStream_t)stream);
+  if (rc != DROT_OK) return rc;
+  return drot_gl_solve(c, p, q, n_rows, n_cols, n_class, s, lambda, max_iters, eps, x, a, b,
+                       phi1, phi2, alpha, workspace, sc, result, stream);
+}
+
+// Host-buffer wrappers ------------------------------------------------------
+
+static float* wrapper_impl(int mode, const float* hc, const float* hp, const float* hq,
+                           int nr, int nc, int G, float s, float r_weight, int max_iters,
+                           float eps, float* dur_ms, float* prep_ms, int* n_iter,
+                           float* objective, int warm, int return_x) {
+  g_last_status = DROT_OK;
+  if (!hc || !hp || !hq || nr <= 0 || nc <= 0 || (mode == MODE_GL && G <= 0)) {
+    g_last_status = DROT_ERR_INVALID_ARG;
+    return nullptr;
+  }
+  const size_t mat = sizeof(float) * (size_t)nr * nc;
+  const size_t sc = mode == MODE_QR ? scratch_bytes(MODE_QR, nr, nc, 0)
+                                    : scratch_bytes(MODE_GL, nr, nc, G);
+  if (sc == 0) {
+    g_last_status = DROT_ERR_UNSUPPORTED;
+    return nullptr;
+  }
+  const StateLayout L = state_layout(sc, nr, nc);
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventCreate(&e2);
+  cudaEventRecord(e0, 0);
+  cudaEventSynchronize(e0);
+  float *c = nullptr, *p = nullptr, *q = nullptr, *x = nullptr;
+  char* ws = nullptr;
+  int rc = DROT_OK;
+  float* out = nullptr;
+  drot_result res;
+  memset(&res, 0, sizeof(res));
+  if (cudaMalloc(&c, mat) != cudaSuccess || cudaMalloc(&x, mat) != cudaSuccess ||
+      cudaMalloc(&p, sizeof(float) * nr) != cudaSuccess ||
+      cudaMalloc(&q, sizeof(float) * nc) != cudaSuccess ||
+      cudaMalloc(&ws, L.total) != cudaSuccess) {
+    rc = DROT_ERR_CUDA;
+  }
+  if (rc == DROT_OK &&
+      (cudaMemcpy(c, hc, mat, cudaMemcpyHostToDevice) != cudaSuccess ||
+       cudaMemcpy(p, hp, sizeof(float) * nr, cudaMemcpyHostToDevice) != cudaSuccess ||
+       cudaMemcpy(q, hq, sizeof(float) * nc, cudaMemcpyHostToDevice) != cudaSuccess))
+    rc = DROT_ERR_CUDA;
+  float *a = (float*)(ws + L.off_a), *b = (float*)(ws + L.off_b);
+  float *phi1 = (float*)(ws + L.off_phi1), *phi2 = (float*)(ws + L.off_phi2);
+  float* alpha = (float*)(ws + L.off_alpha);
+  if (rc == DROT_OK) rc = init_state(nr, nc, s, warm, p, q, x, a, b, phi1, phi2, alpha, 0);
+  cudaEventRecord(e1, 0);
+  cudaEventSynchronize(e1);
+  if (rc == DROT_OK) {
+    if (mode == MODE_QR) {
+      // core/drot_qr.hpp:262: scale = 1 + step_size * T(n_rows + n_cols) * r_weight
+      float t = s * (float)(nr + nc);
+      t = t * r_weight;
+      const float kappa = 1.0f + t;
+      rc = drot_qr_solve(c, p, q, nr, nc, s, kappa, max_iters, eps, x, a, b, phi1, phi2, alpha,
+                         ws, sc, &res, 0);
+    } else {
+      // core/drot_glr.hpp:385: lambda = r_weight / sqrt(n_rows / NGROUPS)
+      const float lambda = (float)((double)r_weight / sqrt((double)(nr / G)));
+      rc = drot_gl_solve(c, p, q, nr, nc, G, s, lambda, max_iters, eps, x, a, b, phi1, phi2,
+                         alpha, ws, sc, &res, 0);
+    }
+  }
+  cudaEventRecord(e2, 0);
+  cudaEventSynchronize(e2);
+  if (dur_ms) cudaEventElapsedTime(dur_ms, e1, e2);
+  if (prep_ms) cudaEventElapsedTime(prep_ms, e0, e1);
+  if (rc == DROT_OK) {
+    if (n_iter) *n_iter = res.n_iter;
+    if (objective && res.objective_valid) *objective = res.objective;
+    if (return_x) {
+      out = (float*)malloc(mat);
+      if (!out || cudaMemcpy(out, x, mat, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        free(out);
+        out = nullptr;
+        rc = DROT_ERR_CUDA;
+      }
+    }
+  }
+  cudaFree(c);
+  cudaFree(x);
+  cudaFree(p);
+  cudaFree(q);
+  cudaFree(ws);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  g_last_status = rc;
+  return out;
+}
+
+float* drot_qr_wrapper(const float* c, const float* p, const float* q, int n_rows, int n_cols,
+                       float step_size, float r_weight, int max_iters, float eps,
+                       float* dur_in_ms, float* prep_dur_in_ms, int* n_iter, float* objective,
+                       int use_warmup_init, int return_x) {
+  return wrapper_impl(MODE_QR, c, p, q, n_rows, n_cols, 0, step_size, r_weight, max_iters, eps,
+                      dur_in_ms, prep_dur_in_ms, n_iter, objective, use_warmup_init, return_x);
+}
+
+float* drot_gl_wrapper(const float* c, const float* p, const float* q, int n_rows, int n_cols,
+                       int n_groups, float step_size, float r_weight, int max_iters, float eps,
+                       float* dur_in_ms, float* prep_dur_in_ms, int* n_iter, float* objective,
+                       int use_warmup_init, int return_x) {
+  return wrapper_impl(MODE_GL, c, p, q, n_rows, n_cols, n_groups, step_size, r_weight,
+                      max_iters, eps, dur_in_ms, prep_dur_in_ms, n_iter, objective,
+                      use_warmup_init, return_x);
+}
+
+void drot_free_host(float* ptr) { free(ptr); }
+
+}  // extern "C"

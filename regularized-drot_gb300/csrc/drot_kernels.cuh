@@ -1,0 +1,774 @@
+// drot_kernels.cuh -- persistent fused DROT solve kernel for sm_103a.
+//
+// One cooperative launch runs the whole Douglas-Rachford solve of the
+// reference's quadratic-regularised (core/drot_qr.hpp:159-234) or
+// group-lasso-regularised (core/drot_glr.hpp:242-355) loop.
+//
+// Work split.  X and C are column-major (element (i, j) at j*ld + i).  Rows
+// are cut into "bands": fixed-height bands for QR, the reference's group row
+// ranges for GL.  CTA b owns band b / P and column chunk b % P for the whole
+// solve.  Inside a CTA, warps form teams of Wt warps; a team processes one
+// column of the band at a time, warp k of the team covering sub-band k
+// (S = 32*VEC*KV rows; lane l holds rows base + k*S + v*32*VEC + l*VEC + e,
+// v < KV, e < VEC).  One (band, column) segment is register resident, so the
+// GL group norm needs no second pass over X.
+//
+// Data path.  When X and C are 16-byte aligned with a leading dimension that
+// is a multiple of 4 (TMA = true), every warp streams its column segments
+// through a private ring of shared-memory stages filled by cp.async.bulk
+// (TMA bulk copies) and tracked by mbarriers, NS columns ahead of the one it
+// computes; the bytes in flight are bounded by shared memory, not registers.
+// Otherwise (TMA = false) the warp loads its segment straight into registers.
+//
+// Per iteration (all on device, no host round trip):
+//   phase 1  fused X-update over the CTA's tile: prox (QR divisor or GL group
+//            shrink), store, per-lane row partials, per-warp column partials,
+//            per-CTA FP64 mass and objective partials;
+//   barrier A
+//   phase 2  CTA b reduces rows [b*nr/G, (b+1)*nr/G) and the same share of
+//            columns: marginal residuals, duals a/b, phi1/phi2 (the
+//            reference's update_aux, kernel_qr.hpp:405-467), and an FP64
+//            residual partial;
+//   barrier B
+//   stop test on the FP64 residual (QR: even iterations only, "< eps";
+//            GL: every iteration, "<= eps"), identical in every CTA.
+//
+// Every wait is bounded by wall time (globaltimer): a grid barrier or an
+// mbarrier that waits longer than the limit raises an abort flag, every CTA
+// leaves its loop, and the host reads DROT_ERR_BARRIER_TIMEOUT.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+#include "drot_math.cuh"
+
+namespace drot {
+
+enum { MODE_QR = 0, MODE_GL = 1 };
+
+// Largest number of GL groups (classes); the boundaries travel in the
+// kernel parameter block.
+constexpr int kMaxGroups = 256;
+
+// Device-side result block (lives at offset 0 of the workspace).
+struct DeviceStats {
+  int n_iter;          // reference convention (see drot_gb300.h)
+  int iters_run;       // iterations actually executed
+  int converged;
+  int status;          // 0 ok, 3 wait time limit hit
+  int objective_valid; // QR: 0 until an even iteration ran
+  int pad;
+  double objective;    // <C, X> of the last objective-bearing iteration
+  double residual;     // absolute marginal residual at the last stop test
+  double sigma;        // total mass sum(X) of the last iteration
+  // Wall time of CTA 0 per stage, summed over iterations (globaltimer ns):
+  // phase 1, barrier A, phase 2, barrier B + stop test.
+  double phase_ns[4];
+};
+
+struct SolveParams {
+  const float* c;
+  const float* p;
+  const float* q;
+  float* x;
+  float* a;
+  float* b;
+  float* phi1;
+  float* phi2;
+  float* alpha;        // device scalar
+  long long ld;        // leading dimension of X and C (elements)
+  int nr, nc;
+  float s;             // step size
+  float kappa;         // QR divisor
+  float kappa_rcp;     // RN(1 / kappa)
+  float lambda;        // GL threshold
+  float eps;           // absolute residual tolerance
+  double norm_eps;     // GL: constant added to the group norm (1e-9)
+  int max_iters;
+  int nbands;          // QR: row bands; GL: groups
+  int P;               // CTAs per band (column chunks)
+  int Wt;              // warps per team (sub-bands per band)
+  int nsb;             // nbands * Wt sub-bands (column partial rows)
+  int band_h;          // QR: rows per band
+  int ns;              // TMA ring stages per warp
+  float* rowpart;      // [P][nr]
+  float* colpart;      // [nsb][nc]
+  double* cta_sum;     // [grid]
+  double* cta_obj;     // [grid]
+  double* cta_res;     // [grid]
+  unsigned int* bar;   // barrier arrival counter (zeroed before launch)
+  int* abort_flag;     // zeroed before launch
+  DeviceStats* stats;
+  long long timeout_ns;
+  int gbounds[kMaxGroups + 1];  // GL: group row boundaries
+};
+
+// ---------------------------------------------------------------------------
+// device helpers
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ int ld_volatile_i32(const int* p) {
+  int v;
+  asm volatile("ld.volatile.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Deterministic block-wide FP64 sum; every thread receives the result.
+// `scratch` holds blockDim/32 + 1 doubles.  FP64 runs on a narrow pipe here,
+// so only warp 0 combines the per-warp sums.
+__device__ __forceinline__ double block_sum_d(double v, double* scratch) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum_d(v);
+  __syncthreads();
+  if (lane == 0) scratch[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double t = lane < nw ? scratch[lane] : 0.0;
+    t = warp_sum_d(t);
+    if (lane == 0) scratch[nw] = t;
+  }
+  __syncthreads();
+  return scratch[nw];
+}
+
+// Grid barrier.  Returns false when the run was aborted (time limit hit here
+// or in another CTA).  `epoch` counts barriers passed by this CTA.
+__device__ __forceinline__ bool grid_barrier(const SolveParams& P, unsigned& epoch,
+                                             int* s_flag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    epoch += 1u;
+    const unsigned target = epoch * gridDim.x;
+    __threadfence();
+    red_release_add_u32(P.bar, 1u);
+    int ok = 1;
+    const unsigned long long t0 = globaltimer_ns();
+    unsigned spins = 0;
+    while ((int)(ld_acquire_u32(P.bar) - target) < 0) {
+      if ((++spins & 31u) == 0u) {
+        if (ld_volatile_i32(P.abort_flag)) { ok = 0; break; }
+        if ((long long)(globaltimer_ns() - t0) > P.timeout_ns) {
+          atomicExch(P.abort_flag, 1);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    *s_flag = ok;
+  }
+  __syncthreads();
+  return *s_flag != 0;
+}
+
+// ---- shared-memory addresses, mbarriers and TMA bulk copies -------------
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+               :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the phase `parity` of an mbarrier.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer_ns();
+  unsigned spins = 0;
+  while (!mbar_try_wait(bar, parity)) {
+    if ((++spins & 63u) == 0u && (long long)(globaltimer_ns() - t0) > limit_ns) return false;
+  }
+  return true;
+}
+
+// 1-D TMA bulk copy global -> shared, completing on `bar` (both addresses
+// 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+      :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_shared() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_all() {
+  asm volatile("fence.proxy.async;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+template <int VEC>
+__device__ __forceinline__ void load_vec(const float* ptr, float (&v)[VEC]) {
+  if constexpr (VEC == 4) {
+    const float4 t = *reinterpret_cast<const float4*>(ptr);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  } else {
+    v[0] = *ptr;
+  }
+}
+
+template <int VEC>
+__device__ __forceinline__ void load_vec_nc(const float* ptr, float (&v)[VEC]) {
+  if constexpr (VEC == 4) {
+    const float4 t = __ldg(reinterpret_cast<const float4*>(ptr));
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  } else {
+    v[0] = __ldg(ptr);
+  }
+}
+
+template <int VEC>
+__device__ __forceinline__ void store_vec(float* ptr, const float (&v)[VEC]) {
+  if constexpr (VEC == 4) {
+    *reinterpret_cast<float4*>(ptr) = make_float4(v[0], v[1], v[2], v[3]);
+  } else {
+    *ptr = v[0];
+  }
+}
+
+// Sums the np partials of each item i in [i0, i1) (partial pp of item i at
+// part[pp * stride + i]) with g threads per item, g a power of two <= 32
+// chosen so the items fill the block; partial order and shuffle tree are
+// fixed, so the sums are deterministic.  fin(i, sum) runs on the item's
+// first thread.
+template <typename Fin>
+__device__ __forceinline__ void reduce_partials(int i0, int i1, const float* part,
+                                                long long stride, int np, Fin fin) {
+  const int items = i1 - i0;
+  if (items <= 0) return;
+  int g = 32;
+  while (g > 1 && items * g > (int)blockDim.x) g >>= 1;
+  const int per_round = blockDim.x / g;
+  const int sub = threadIdx.x & (g - 1);
+  for (int base = 0; base < items; base += per_round) {
+    const int idx = base + (int)threadIdx.x / g;
+    const bool live = idx < items;
+    double t = 0.0;
+    if (live) {
+      const float* pp = part + i0 + idx;
+#pragma unroll 4
+      for (int k = sub; k < np; k += g) t += (double)__ldcg(pp + (long long)k * stride);
+    }
+    for (int o = g >> 1; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (live && sub == 0) fin(i0 + idx, t);
+  }
+}
+
+// Dynamic shared memory of the solve kernel (must match the device layout).
+//   ring    TMA: W * ns * 2 * S floats (stage: X segment, C segment)
+//           reg: W * S floats (row-partial staging only)
+//   f1s     Wt * S floats (phi1 of the band rows)
+//   dscr    W + 1 doubles
+//   nslot   2 * W floats (GL team norms, double-buffered)
+//   mbar    W * ns uint64 (TMA only)
+__host__ __device__ constexpr size_t solve_smem_bytes(int warps, int wt, int S, int ns, bool tma) {
+  return sizeof(float) * (size_t)warps * S * (tma ? 2 * ns : 1) + sizeof(float) * (size_t)wt * S +
+         sizeof(double) * (warps + 1) + sizeof(double) * 2 * warps +
+         (tma ? sizeof(uint64_t) * (size_t)warps * ns : 0);
+}
+
+// ---------------------------------------------------------------------------
+// The solve kernel
+// ---------------------------------------------------------------------------
+
+template <int MODE, int VEC, int KV, bool TMA>
+__global__ void __launch_bounds__(512, 1)
+drot_solve_kernel(const SolveParams P) {
+  static_assert(!TMA || VEC == 4, "the TMA path moves 16-byte vectors");
+  constexpr int SV = 32 * VEC;        // rows per vector slot of a warp
+  constexpr int S = SV * KV;          // rows per sub-band (one warp)
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int W = blockDim.x >> 5;
+  const int Wt = P.Wt;
+  const int NS = TMA ? P.ns : 1;
+  float* ring = reinterpret_cast<float*>(smem_raw);
+  float* red = ring;  // row-partial staging aliases the ring (ring idle then)
+  float* f1s = ring + (size_t)W * S * (TMA ? 2 * NS : 1);
+  double* dscr = reinterpret_cast<double*>(f1s + (size_t)Wt * S);
+  double* nslot = dscr + W + 1;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(nslot + 2 * W);
+  __shared__ int s_flag;
+
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int nteams = W / Wt;
+  const int team = warp / Wt;
+  const int k = warp - team * Wt;     // sub-band within the band
+  const bool active_warp = team < nteams;
+
+  const int band = blockIdx.x / P.P;
+  const int chunk = blockIdx.x - band * P.P;
+  int lo, hi;
+  if constexpr (MODE == MODE_QR) {
+    lo = min(band * P.band_h, P.nr);
+    hi = min(lo + P.band_h, P.nr);
+  } else {
+    lo = P.gbounds[band];
+    hi = P.gbounds[band + 1];
+  }
+  const int base = lo - (lo % VEC);
+  const int c0 = (int)(((long long)P.nc * chunk) / P.P);
+  const int c1 = (int)(((long long)P.nc * (chunk + 1)) / P.P);
+  const long long ld = P.ld;
+  const int sb = band * Wt + k;
+
+  // Rows owned by this lane and their validity masks (loop invariant).
+  int row0[KV];
+  bool vany[KV], vall[KV];
+  bool ein[KV][VEC];
+#pragma unroll
+  for (int v = 0; v < KV; ++v) {
+    row0[v] = base + k * S + v * SV + lane * VEC;
+    bool any = false, all = true;
+#pragma unroll
+    for (int e = 0; e < VEC; ++e) {
+      const int r = row0[v] + e;
+      ein[v][e] = active_warp && r >= lo && r < hi;
+      any |= ein[v][e];
+      all &= ein[v][e];
+    }
+    vany[v] = any;
+    vall[v] = all;
+  }
+
+  // TMA segment of this warp: rows [seg_lo, seg_lo + seg_rows), 16-byte granular.
+  const int seg_lo = base + k * S;
+  const int hi4 = (hi + 3) & ~3;
+  const int seg_rows = (TMA && active_warp) ? max(0, min(seg_lo + S, hi4) - seg_lo) : 0;
+  const uint32_t seg_bytes = (uint32_t)seg_rows * 4u;
+  float* wring = ring + (size_t)warp * NS * 2 * S;
+  uint64_t* wbar = mbar + (size_t)warp * NS;
+  uint32_t pipe_cnt = 0;  // columns waited on by this warp (monotonic)
+  if constexpr (TMA) {
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < W * NS; ++i) mbar_init(mbar + i, 1);
+      fence_mbar_init();
+      fence_proxy_async_shared();
+    }
+    __syncthreads();
+  }
+
+  // Phase-2 slices.
+  const int G = gridDim.x;
+  const int r_lo = (int)(((long long)P.nr * blockIdx.x) / G);
+  const int r_hi = (int)(((long long)P.nr * (blockIdx.x + 1)) / G);
+  const int k_lo = (int)(((long long)P.nc * blockIdx.x) / G);
+  const int k_hi = (int)(((long long)P.nc * (blockIdx.x + 1)) / G);
+
+  const float s = P.s;
+  const float kappa = P.kappa;
+  const float kappa_rcp = P.kappa_rcp;
+  float alpha = *P.alpha;
+  unsigned epoch = 0;
+  int it = 0;
+  bool converged = false;
+  bool aborted = false;
+  double last_obj = 0.0;
+  int obj_valid = 0;
+  double last_res = -1.0;
+  double last_sigma = 0.0;
+
+  const bool timer = blockIdx.x == 0;
+  unsigned long long tp[5] = {0, 0, 0, 0, 0};
+  double tacc[4] = {0.0, 0.0, 0.0, 0.0};
+  auto stamp = [&](int k2) {  // CTA 0 only (block-uniform)
+    if (timer) {
+      __syncthreads();
+      tp[k2] = globaltimer_ns();
+      if (k2 > 0) tacc[k2 - 1] += (double)(tp[k2] - tp[k2 - 1]);
+    }
+  };
+
+  for (; it < P.max_iters; ++it) {
+    const bool even = (it & 1) == 0;
+    const bool with_c = (MODE == MODE_GL) || even;
+    stamp(0);
+
+    // ------------------------------------------------------------ phase 1
+    // phi1 of the band rows -> shared memory.
+    for (int idx = threadIdx.x; idx < Wt * S; idx += blockDim.x) {
+      const int r = base + idx;
+      f1s[idx] = (r >= lo && r < hi) ? __ldcg(P.phi1 + r) : 0.0f;
+    }
+    __syncthreads();
+    float acc[KV][VEC];
+#pragma unroll
+    for (int v = 0; v < KV; ++v)
+#pragma unroll
+      for (int e = 0; e < VEC; ++e) acc[v][e] = 0.0f;
+    double wsum = 0.0, wobj = 0.0;  // lane 0 of each warp accumulates
+    bool wfail = false;
+
+    // One column of the band per team step.  EV selects the QR step that
+    // reads C and stores the folded value X^ - sC (kernel_qr.hpp:171-278);
+    // the odd QR step reads X only (kernel_qr.hpp:280-376).
+    auto run_columns = [&](auto even_tag) {
+      constexpr bool EV = decltype(even_tag)::value;
+      constexpr bool WITH_C = (MODE == MODE_GL) || EV;
+      const int ncw = (c1 - c0 - team + nteams - 1) / nteams;  // columns of this warp
+      const uint32_t tx_bytes = seg_bytes * (WITH_C ? 2u : 1u);
+      uint32_t issued = pipe_cnt;
+      auto issue = [&](int n) {  // lane 0: fetch column n of this warp into its stage
+        const int jn = c0 + team + n * nteams;
+        const int st = (int)(issued % (uint32_t)NS);
+        float* dx = wring + (size_t)st * 2 * S;
+        mbar_arrive_expect_tx(wbar + st, tx_bytes);
+        bulk_g2s(dx, P.x + (long long)jn * ld + seg_lo, seg_bytes, wbar + st);
+        if constexpr (WITH_C) bulk_g2s(dx + S, P.c + (long long)jn * ld + seg_lo, seg_bytes, wbar + st);
+        ++issued;
+      };
+      if constexpr (TMA) {
+        if (seg_rows > 0 && lane == 0) {
+          // X was last written by generic stores; order them before the
+          // async-proxy reads.
+          fence_proxy_async_all();
+          const int pre = min(NS, ncw);
+          for (int n = 0; n < pre; ++n) issue(n);
+        }
+      }
+      int par = 0;
+      for (int n = 0; n < ncw; ++n, par ^= 1) {
+        const int j = c0 + team + n * nteams;
+        const float f2 = __ldcg(P.phi2 + j);
+        float* xcol = P.x + (long long)j * ld;
+        const float* ccol = P.c + (long long)j * ld;
+        float xv[KV][VEC];
+        float cv[KV][VEC];
+        if constexpr (TMA) {
+          if (seg_rows > 0) {
+            const int st = (int)(pipe_cnt % (uint32_t)NS);
+            const uint32_t parity = (pipe_cnt / (uint32_t)NS) & 1u;
+            if (!wfail && !mbar_wait(wbar + st, parity, P.timeout_ns)) wfail = true;
+            ++pipe_cnt;
+            const float* sx = wring + (size_t)st * 2 * S;
+#pragma unroll
+            for (int v = 0; v < KV; ++v) {
+              const float4 t = *reinterpret_cast<const float4*>(sx + v * SV + lane * 4);
+              xv[v][0] = t.x; xv[v][1] = t.y; xv[v][2] = t.z; xv[v][3] = t.w;
+              if constexpr (WITH_C) {
+                const float4 u = *reinterpret_cast<const float4*>(sx + S + v * SV + lane * 4);
+                cv[v][0] = u.x; cv[v][1] = u.y; cv[v][2] = u.z; cv[v][3] = u.w;
+              } else {
+                cv[v][0] = cv[v][1] = cv[v][2] = cv[v][3] = 0.0f;
+              }
+              if (!vall[v]) {
+                // Stage bytes outside this warp's rows are stale: zero them so
+                // masked lanes add exact zeros to the objective.
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                  xv[v][e] = ein[v][e] ? xv[v][e] : 0.0f;
+                  cv[v][e] = ein[v][e] ? cv[v][e] : 0.0f;
+                }
+              }
+            }
+            __syncwarp();
+            if (lane == 0 && n + NS < ncw && !wfail) {
+              fence_proxy_async_shared();
+              issue(n + NS);
+            }
+          } else {
+#pragma unroll
+            for (int v = 0; v < KV; ++v)
+#pragma unroll
+              for (int e = 0; e < VEC; ++e) { xv[v][e] = 0.0f; cv[v][e] = 0.0f; }
+          }
+        } else {
+#pragma unroll
+          for (int v = 0; v < KV; ++v) {
+            if (vany[v]) {
+              load_vec<VEC>(xcol + row0[v], xv[v]);
+              if constexpr (WITH_C) load_vec_nc<VEC>(ccol + row0[v], cv[v]);
+              else {
+#pragma unroll
+                for (int e = 0; e < VEC; ++e) cv[v][e] = 0.0f;
+              }
+            } else {
+#pragma unroll
+              for (int e = 0; e < VEC; ++e) { xv[v][e] = 0.0f; cv[v][e] = 0.0f; }
+            }
+          }
+        }
+
+        float f1[KV][VEC];
+#pragma unroll
+        for (int v = 0; v < KV; ++v) {
+          if constexpr (VEC == 4) {
+            const float4 t = *reinterpret_cast<const float4*>(f1s + k * S + v * SV + lane * 4);
+            f1[v][0] = t.x; f1[v][1] = t.y; f1[v][2] = t.z; f1[v][3] = t.w;
+          } else {
+            f1[v][0] = f1s[k * S + v * SV + lane];
+          }
+        }
+
+        float colp = 0.0f, objp = 0.0f;
+        if constexpr (MODE == MODE_QR) {
+#pragma unroll
+          for (int v = 0; v < KV; ++v)
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) {
+              float t = (xv[v][e] + f1[v][e]) + f2;
+              if constexpr (EV) t = fmaf(-s, cv[v][e], t);
+              float y = div_rn_by(fmaxf(t, 0.0f), kappa, kappa_rcp);
+              y = ein[v][e] ? y : 0.0f;
+              if constexpr (EV) {
+                xv[v][e] = fmaf(-s, cv[v][e], y);
+                objp = fmaf(y, cv[v][e], objp);
+              } else {
+                xv[v][e] = y;
+              }
+              acc[v][e] += y;
+              colp += y;
+            }
+        } else {
+          float nsl = 0.0f;
+#pragma unroll
+          for (int v = 0; v < KV; ++v)
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) {
+              const float t = fmaf(-s, cv[v][e], (xv[v][e] + f1[v][e]) + f2);
+              float y = fmaxf(t, 0.0f);
+              y = ein[v][e] ? y : 0.0f;
+              xv[v][e] = y;
+              nsl = fmaf(y, y, nsl);
+            }
+          // Group norm: a float sum, as the reference's atomics make it.
+          nsl = warp_sum(nsl);
+          if (Wt > 1) {
+            float* slot = reinterpret_cast<float*>(nslot) + par * W + team * Wt;
+            if (lane == 0) slot[k] = nsl;
+            asm volatile("bar.sync %0, %1;" :: "r"(1 + team), "r"(Wt * 32) : "memory");
+            nsl = 0.0f;
+            for (int kk = 0; kk < Wt; ++kk) nsl += slot[kk];
+          }
+          const float scale = gl_shrink(nsl, P.lambda);
+#pragma unroll
+          for (int v = 0; v < KV; ++v)
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) {
+              const float y = xv[v][e] * scale;
+              xv[v][e] = y;
+              acc[v][e] += y;
+              colp += y;
+              objp = fmaf(y, cv[v][e], objp);
+            }
+        }
+
+#pragma unroll
+        for (int v = 0; v < KV; ++v) {
+          if (vall[v]) {
+            store_vec<VEC>(xcol + row0[v], xv[v]);
+          } else if (vany[v]) {
+#pragma unroll
+            for (int e = 0; e < VEC; ++e)
+              if (ein[v][e]) xcol[row0[v] + e] = xv[v][e];
+          }
+        }
+
+        colp = warp_sum(colp);
+        if constexpr (WITH_C) objp = warp_sum(objp);
+        if (lane == 0) {
+          P.colpart[(long long)sb * P.nc + j] = colp;
+          wsum += (double)colp;
+          if constexpr (WITH_C) wobj += (double)objp;
+        }
+      }
+    };
+    if (active_warp) {
+      if (with_c) run_columns(std::integral_constant<bool, true>());
+      else run_columns(std::integral_constant<bool, false>());
+    }
+    if (wfail && lane == 0) atomicExch(P.abort_flag, 1);
+
+    // CTA reduction of the row partials (fixed order over teams).
+    __syncthreads();
+#pragma unroll
+    for (int v = 0; v < KV; ++v)
+#pragma unroll
+      for (int e = 0; e < VEC; ++e)
+        red[(size_t)warp * S + v * SV + lane * VEC + e] = acc[v][e];
+    if (lane == 0) dscr[warp] = wsum;
+    __syncthreads();
+    {
+      const int cover = Wt * S;
+      for (int idx = threadIdx.x; idx < cover; idx += blockDim.x) {
+        const int row = base + idx;
+        if (row >= lo && row < hi) {
+          const int kk = idx / S, r = idx - kk * S;
+          float t = 0.0f;
+          for (int tm = 0; tm < nteams; ++tm) t += red[(size_t)(tm * Wt + kk) * S + r];
+          P.rowpart[(long long)chunk * P.nr + row] = t;
+        }
+      }
+    }
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < W; ++w) t += dscr[w];
+      P.cta_sum[blockIdx.x] = t;
+    }
+    __syncthreads();
+    if (lane == 0) dscr[warp] = wobj;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < W; ++w) t += dscr[w];
+      P.cta_obj[blockIdx.x] = t;
+    }
+
+    stamp(1);
+    if (!grid_barrier(P, epoch, &s_flag)) { aborted = true; break; }
+    stamp(2);
+
+    // ------------------------------------------------------------ phase 2
+    double sig = 0.0;
+    for (int i = threadIdx.x; i < G; i += blockDim.x) sig += __ldcg(P.cta_sum + i);
+    sig = block_sum_d(sig, dscr);
+    double objall = 0.0;
+    if (with_c && blockIdx.x == 0) {
+      for (int i = threadIdx.x; i < G; i += blockDim.x) objall += __ldcg(P.cta_obj + i);
+      objall = block_sum_d(objall, dscr);
+    }
+    const float sigma = (float)sig;
+    const float gamma =
+        (float)((2.0 * ((double)sigma - 1.0) - (double)alpha) / (double)(P.nr + P.nc));
+    double res = 0.0;
+    // Rows and columns of this CTA's slice: partial sums over the column
+    // chunks / sub-bands (grouped loads, fixed order), then the dual update.
+    reduce_partials(r_lo, r_hi, P.rowpart, P.nr, P.P, [&](int i, double t) {
+      const float rs = (float)t - __ldg(P.p + i);
+      const float ab = P.a[i] - rs;
+      P.phi1[i] = ((ab - rs) + gamma) / (float)P.nc;
+      P.a[i] = ab;
+      res += (double)rs * (double)rs;
+    });
+    reduce_partials(k_lo, k_hi, P.colpart, P.nc, P.nsb, [&](int j, double t) {
+      const float cs = (float)t - __ldg(P.q + j);
+      const float ab = P.b[j] - cs;
+      P.phi2[j] = ((ab - cs) + gamma) / (float)P.nr;
+      P.b[j] = ab;
+      res += (double)cs * (double)cs;
+    });
+    const bool check = (MODE == MODE_GL) || even;
+    if (check) {
+      res = block_sum_d(res, dscr);
+      if (threadIdx.x == 0) P.cta_res[blockIdx.x] = res;
+    }
+    alpha = (float)(((double)alpha + 1.0) - (double)sigma);
+    last_sigma = sig;
+    if (with_c) {
+      last_obj = objall;
+      obj_valid = 1;
+    }
+
+    stamp(3);
+    if (!grid_barrier(P, epoch, &s_flag)) { aborted = true; break; }
+
+    if (check) {
+      double r2 = 0.0;
+      for (int i = threadIdx.x; i < G; i += blockDim.x) r2 += __ldcg(P.cta_res + i);
+      r2 = block_sum_d(r2, dscr);
+      last_res = sqrt(r2);
+      const bool stop = (MODE == MODE_QR) ? (last_res < (double)P.eps)
+                                          : (last_res <= (double)P.eps);
+      if (stop) {
+        converged = true;
+        stamp(4);
+        break;
+      }
+    }
+    stamp(4);
+  }
+
+  // ------------------------------------------------------------ epilogue
+  if (MODE == MODE_QR && converged && active_warp) {
+    // fix_x (kernel_qr.hpp:469-482): undo the fold of the last even step.
+    for (int j = c0 + team; j < c1; j += nteams) {
+      float* xcol = P.x + (long long)j * ld;
+      const float* ccol = P.c + (long long)j * ld;
+#pragma unroll
+      for (int v = 0; v < KV; ++v) {
+        if (!vany[v]) continue;
+        float xv[VEC], cv[VEC];
+        load_vec<VEC>(xcol + row0[v], xv);
+        load_vec_nc<VEC>(ccol + row0[v], cv);
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) xv[e] = fmaxf(fmaf(s, cv[e], xv[e]), 0.0f);
+        if (vall[v]) store_vec<VEC>(xcol + row0[v], xv);
+        else {
+#pragma unroll
+          for (int e = 0; e < VEC; ++e)
+            if (ein[v][e]) xcol[row0[v] + e] = xv[e];
+        }
+      }
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    DeviceStats* st = P.stats;
+    st->iters_run = converged ? it + 1 : it;
+    // QR reports the index of the last iteration + 1, and max_iters + 1 when
+    // it never converged (drot_qr.hpp:233); GL the iterations run (drot_glr.hpp:354).
+    st->n_iter = (MODE == MODE_QR) ? it + 1 : st->iters_run;
+    st->converged = converged ? 1 : 0;
+    st->status = (aborted || ld_volatile_i32(P.abort_flag)) ? 3 : 0;
+    st->objective_valid = obj_valid;
+    st->objective = last_obj;
+    st->residual = last_res;
+    st->sigma = last_sigma;
+    for (int q = 0; q < 4; ++q) st->phase_ns[q] = tacc[q];
+    *P.alpha = alpha;
+  }
+}
+
+}  // namespace drot

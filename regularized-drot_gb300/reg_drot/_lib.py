@@ -1,0 +1,106 @@
+"""ctypes binding of libdrot_gb300.so (the C ABI in include/drot_gb300.h).
+
+The library is built in tree by ``regularized-drot_gb300/build.py``.  There is
+no fallback: if the shared library is missing or fails to load, every solver
+call raises.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libdrot_gb300.so")
+
+# Symbols declared in include/drot_gb300.h, with ctypes signatures.
+_c_int, _c_float, _c_double, _c_size = ctypes.c_int, ctypes.c_float, ctypes.c_double, ctypes.c_size_t
+_vp = ctypes.c_void_p
+_ip = ctypes.POINTER(ctypes.c_int)
+_fp = ctypes.POINTER(ctypes.c_float)
+
+
+class DrotResult(ctypes.Structure):
+    _fields_ = [
+        ("n_iter", ctypes.c_int),
+        ("iters_run", ctypes.c_int),
+        ("converged", ctypes.c_int),
+        ("status", ctypes.c_int),
+        ("objective_valid", ctypes.c_int),
+        ("objective", ctypes.c_float),
+        ("objective_f64", ctypes.c_double),
+        ("residual", ctypes.c_double),
+        ("phase_ms", ctypes.c_double * 4),
+    ]
+
+    def as_dict(self):
+        d = {name: getattr(self, name) for name, _ in self._fields_}
+        d["phase_ms"] = list(self.phase_ms)
+        return d
+
+
+_RP = ctypes.POINTER(DrotResult)
+
+SIGNATURES = {
+    "drot_status_string": (ctypes.c_char_p, [_c_int]),
+    "drot_last_status": (_c_int, []),
+    "drot_q_get_work_size_update_x": (_c_int, [_c_int, _c_int]),
+    "drot_gl_get_work_size_update_x": (_c_int, [_c_int, _c_int]),
+    "drot_gl_group_bounds": (_c_int, [_c_int, _c_int, _ip]),
+    "drot_init_state": (_c_int, [_c_int, _c_int, _c_float, _c_int, _vp, _vp, _vp, _vp, _vp,
+                                 _vp, _vp, _vp, _vp]),
+    "drot_qr_workspace_bytes": (_c_size, [_c_int, _c_int]),
+    "drot_gl_workspace_bytes": (_c_size, [_c_int, _c_int, _c_int]),
+    "drot_qr_solve": (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_float, _c_float, _c_int,
+                               _c_float, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _c_size, _RP, _vp]),
+    "drot_gl_solve": (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_int, _c_float, _c_float,
+                               _c_int, _c_float, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _c_size,
+                               _RP, _vp]),
+    "drot_read_result": (_c_int, [_vp, _RP, _vp]),
+    "drot_quadratic_drot_workspace_bytes": (_c_size, [_c_int, _c_int]),
+    "drot_quadratic_drot": (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_float, _c_float, _c_int,
+                                     _c_float, _vp, _vp, _c_size, _RP, _vp]),
+    "drot_group_lasso_drot_workspace_bytes": (_c_size, [_c_int, _c_int, _c_int]),
+    "drot_group_lasso_drot": (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_int, _c_float,
+                                       _c_float, _c_int, _c_float, _vp, _vp, _c_size, _RP,
+                                       _vp]),
+    "drot_qr_wrapper": (_fp, [_vp, _vp, _vp, _c_int, _c_int, _c_float, _c_float, _c_int,
+                              _c_float, _fp, _fp, _ip, _fp, _c_int, _c_int]),
+    "drot_gl_wrapper": (_fp, [_vp, _vp, _vp, _c_int, _c_int, _c_int, _c_float, _c_float,
+                              _c_int, _c_float, _fp, _fp, _ip, _fp, _c_int, _c_int]),
+    "drot_free_host": (None, [_fp]),
+}
+
+_lib = None
+
+
+class DrotError(RuntimeError):
+    """A solver entry point returned a non-zero drot_status."""
+
+    def __init__(self, status, where=""):
+        self.status = status
+        msg = status_string(status) if _lib is not None else str(status)
+        super().__init__(f"{where}: {msg} (drot_status {status})" if where else msg)
+
+
+def lib():
+    """Load libdrot_gb300.so (once) and attach the C signatures."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is not built; run `python regularized-drot_gb300/build.py` "
+                "(or __graft_entry__.build()) first")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def status_string(status):
+    return lib().drot_status_string(int(status)).decode()
+
+
+def check(status, where=""):
+    if status != 0:
+        raise DrotError(status, where)

@@ -1,0 +1,281 @@
+"""GPU parity: the CUDA solver (through the C ABI) against the oracle.
+
+Every solve here goes through libdrot_gb300.so: the drop-in operators
+reg_drot.quadratic_drot / group_lasso_drot (pytorch/src/drot_cuda.cpp:26-62)
+or the device-pointer loops drot_qr_solve / drot_gl_solve
+(core/drot_qr.hpp:159-234, core/drot_glr.hpp:242-355).
+
+Tolerances (FP32 solver vs the FP32 oracle on the same inputs): the element
+operations are the same FP32 operations in the same order, but the row,
+column, norm and mass sums are accumulated in a different order (per-lane
+FP32 partials, FP64 across lanes, warps and CTAs, vs the oracle's FP64), so
+the iterates agree to FP32 rounding:
+  * ||X - X_o||_F <= 1e-5 * ||X_o||_F  (the 1e-5 relative bar on X),
+  * max|X - X_o| <= 1e-4 * max|X_o|    (single entries; the GL shrink factor
+    1 - lambda/||Y_g|| amplifies rounding in groups it nearly zeroes),
+  * objective within 1e-5 relative,
+  * the same iteration count (a tie at the stop threshold may move the stop
+    by one check: 2 iterations for QR, 1 for GL).
+Each parity case runs on both data paths: the TMA shared-memory ring
+(default for 16-byte aligned data) and the register path (DROT_PATH=reg).
+"""
+import ctypes
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+from oracle import oracle as O  # noqa: E402
+
+RTOL_X = 1e-5       # relative Frobenius error on X
+RTOL_XMAX = 1e-4    # relative max-entry error on X
+RTOL_OBJ = 1e-5
+
+
+@pytest.fixture(params=["default", "reg"])
+def path(request, monkeypatch):
+    if request.param == "reg":
+        monkeypatch.setenv("DROT_PATH", "reg")
+    else:
+        monkeypatch.delenv("DROT_PATH", raising=False)
+    return request.param
+
+
+def _problem(nr, nc, seed, marg="uniform"):
+    """Seeded inputs in the reference test's style (pytorch/test.py:436-440)."""
+    g = torch.Generator().manual_seed(seed)
+    c = torch.rand(nc, nr, generator=g, dtype=torch.float32) + 1e-3
+    c = c / c.max()
+    if marg == "uniform":
+        p = torch.ones(nr, dtype=torch.float32) / nr
+        q = torch.ones(nc, dtype=torch.float32) / nc
+    else:
+        rng = np.random.default_rng(seed)
+        p = torch.from_numpy(rng.dirichlet(np.ones(nr)).astype(np.float32))
+        q = torch.from_numpy(rng.dirichlet(np.ones(nc)).astype(np.float32))
+    return c, p, q
+
+
+def _assert_close_x(xg, xo):
+    xg = np.asarray(xg, dtype=np.float64)
+    xo = np.asarray(xo, dtype=np.float64)
+    fro = np.linalg.norm(xg - xo) / max(np.linalg.norm(xo), 1e-300)
+    mx = np.abs(xg - xo).max() / max(np.abs(xo).max(), 1e-300)
+    assert fro <= RTOL_X and mx <= RTOL_XMAX, (fro, mx)
+
+
+# (n_rows, n_cols, rho, r_weight, eps, max_iters): the reference's own QR
+# test set (pytorch/test.py:9-17) at the sizes the oracle solves in seconds,
+# plus shapes for the 128-bit path (n_rows % 4 == 0), the scalar path
+# (n_rows % 4 != 0), multi-band grids and tall/wide panels.
+QR_CASES = [
+    (2, 3, 2.0, 1e-2, 1e-4, 20000),
+    (10, 20, 2.0, 1e-3, 1e-4, 20000),
+    (100, 100, 2.0, 1e-2, 1e-4, 20000),
+    (20, 10, 2.0, 10.0, 1e-4, 20000),
+    (130, 67, 2.0, 1e-2, 1e-4, 20000),
+    (257, 300, 2.0, 1e-3, 1e-4, 20000),
+    (1000, 600, 2.0, 1e-3, 1e-4, 20000),
+    (999, 301, 2.0, 1e-3, 1e-4, 20000),
+    (2048, 96, 2.0, 1e-2, 1e-4, 20000),
+    (40, 3000, 2.0, 1e-2, 1e-4, 20000),
+]
+
+
+@pytest.mark.parametrize("nr,nc,rho,rw,eps,mi", QR_CASES,
+                         ids=[f"{c[0]}x{c[1]}" for c in QR_CASES])
+def test_quadratic_drot_matches_oracle(cuda, path, nr, nc, rho, rw, eps, mi):
+    import reg_drot
+    c, p, q = _problem(nr, nc, seed=nr * 7 + nc)
+    x, info, _ = reg_drot.solve_qr(c.to(cuda), p.to(cuda), q.to(cuda), rho, rw, mi, eps)
+    o = O.quadratic_drot(c.numpy(), p.numpy(), q.numpy(), rho, rw, mi, eps)
+    assert info["status"] == 0
+    assert abs(info["n_iter"] - o["n_iter"]) <= 2, (info, o["n_iter"])
+    if info["n_iter"] == o["n_iter"]:
+        _assert_close_x(x.cpu().numpy(), o["x"])
+        assert abs(info["objective"] - o["objective"]) <= RTOL_OBJ * abs(o["objective"])
+    # The reference test's own acceptance check (pytorch/test.py:451-457).
+    resid = torch.sqrt(torch.sum((p.to(cuda) - x.sum(0)) ** 2) +
+                       torch.sum((q.to(cuda) - x.sum(1)) ** 2)).item()
+    assert resid <= eps * 1.0001
+    assert info["converged"] == 1
+
+
+GL_CASES = [
+    (2, 4, 2, 2.0, 1e-2, 1e-4, 20000),
+    (10, 20, 2, 2.0, 1e-3, 1e-4, 20000),
+    (100, 100, 5, 2.0, 1e-2, 1e-4, 20000),
+    (20, 10, 2, 2.0, 10.0, 1e-4, 20000),
+    (1500, 1000, 2, 2.0, 1e-3, 1e-4, 20000),
+    (600, 300, 2, 2.0, 1e-3, 1e-4, 20000),
+    (1001, 200, 3, 2.0, 1e-3, 1e-4, 20000),
+    (3000, 64, 2, 2.0, 1e-3, 1e-4, 20000),
+]
+
+
+@pytest.mark.parametrize("nr,nc,G,rho,rw,eps,mi", GL_CASES,
+                         ids=[f"{c[0]}x{c[1]}g{c[2]}" for c in GL_CASES])
+def test_group_lasso_drot_matches_oracle(cuda, path, nr, nc, G, rho, rw, eps, mi):
+    """GL parity, anchored on the FP64 oracle.
+
+    The group shrink max(1 - lambda/||Y_g||, 0) amplifies rounding in groups
+    it nearly zeroes, so FP32 arithmetic in the reference's own operation
+    order (the FP32 oracle) already lands 1e-5..1e-4 away from the FP64
+    solution on these inputs.  The solver must be as close to the FP64
+    solution as that: within max(1e-5, 2 x the FP32 oracle's error) on X and
+    on the objective.
+    """
+    import reg_drot
+    c, p, q = _problem(nr, nc, seed=nr * 11 + nc + G)
+    x, info, _ = reg_drot.solve_gl(c.to(cuda), p.to(cuda), q.to(cuda), G, rho, rw, mi, eps)
+    o32 = O.group_lasso_drot(c.numpy(), p.numpy(), q.numpy(), G, rho, rw, mi, eps)
+    o64 = O.group_lasso_drot(c.numpy(), p.numpy(), q.numpy(), G, rho, rw, mi, eps,
+                             dtype=np.float64)
+    assert info["status"] == 0 and info["converged"] == 1
+    assert abs(info["n_iter"] - o32["n_iter"]) <= max(1, o32["n_iter"] // 50), \
+        (info, o32["n_iter"])
+    x64 = o64["x"]
+    ref_err = np.linalg.norm(o32["x"] - x64) / np.linalg.norm(x64)
+    gpu_err = np.linalg.norm(x.cpu().numpy().astype(np.float64) - x64) / np.linalg.norm(x64)
+    assert gpu_err <= max(RTOL_X, 2.0 * ref_err), (gpu_err, ref_err)
+    ref_obj = abs(o32["objective"] - o64["objective"])
+    assert abs(info["objective"] - o64["objective"]) <= max(RTOL_OBJ * abs(o64["objective"]),
+                                                            2.0 * ref_obj)
+    resid = torch.sqrt(torch.sum((p.to(cuda) - x.sum(0)) ** 2) +
+                       torch.sum((q.to(cuda) - x.sum(1)) ** 2)).item()
+    assert resid <= eps * 1.0001
+
+
+@pytest.mark.parametrize("kind", ["qr", "gl"])
+@pytest.mark.parametrize("iters", [0, 1, 2, 5, 17])
+def test_fixed_iteration_counts_match_oracle(cuda, path, kind, iters):
+    """Stopping at max_iters, including an odd max_iters where the reference
+    returns the still-folded even iterate X^ - sC (core/drot_qr.hpp:190-233)."""
+    import reg_drot
+    nr, nc = 516, 203
+    c, p, q = _problem(nr, nc, seed=5, marg="dirichlet")
+    if kind == "qr":
+        x, info, _ = reg_drot.solve_qr(c.to(cuda), p.to(cuda), q.to(cuda), 2.0, 1e-2, iters, 1e-9)
+        o = O.quadratic_drot(c.numpy(), p.numpy(), q.numpy(), 2.0, 1e-2, iters, 1e-9)
+        assert info["n_iter"] == iters + 1 == o["n_iter"]
+    else:
+        x, info, _ = reg_drot.solve_gl(c.to(cuda), p.to(cuda), q.to(cuda), 3, 2.0, 1e-2, iters,
+                                       1e-9)
+        o = O.group_lasso_drot(c.numpy(), p.numpy(), q.numpy(), 3, 2.0, 1e-2, iters, 1e-9)
+        assert info["n_iter"] == iters == o["n_iter"]
+    assert info["converged"] == 0
+    if iters == 0:
+        assert float(x.abs().max()) == 0.0
+    else:
+        _assert_close_x(x.cpu().numpy(), o["x"])
+
+
+def test_first_iteration_is_bitwise_identical_to_oracle(cuda, path):
+    """One iteration from the warm start involves no cross-element sums in X,
+    so the solver and the FP32 oracle agree bit for bit."""
+    import reg_drot
+    for kind in ("qr", "gl"):
+        for nr, nc in ((1000, 333), (777, 129)):
+            c, p, q = _problem(nr, nc, seed=nr)
+            if kind == "qr":
+                x, _, _ = reg_drot.solve_qr(c.to(cuda), p.to(cuda), q.to(cuda), 2.0, 1e-2, 1, 0.0)
+                o = O.quadratic_drot(c.numpy(), p.numpy(), q.numpy(), 2.0, 1e-2, 1, 0.0)
+            else:
+                x, _, _ = reg_drot.solve_gl(c.to(cuda), p.to(cuda), q.to(cuda), 2, 2.0, 1e-2, 1,
+                                            0.0)
+                o = O.group_lasso_drot(c.numpy(), p.numpy(), q.numpy(), 2, 2.0, 1e-2, 1, 0.0)
+            assert np.array_equal(x.cpu().numpy(), o["x"]), (kind, nr, nc)
+
+
+def test_solver_is_deterministic(cuda, path):
+    import reg_drot
+    c, p, q = _problem(1200, 700, seed=9)
+    c, p, q = c.to(cuda), p.to(cuda), q.to(cuda)
+    def strip(info):
+        return {k: v for k, v in info.items() if k != "phase_ms"}  # wall-clock timers
+
+    x1, i1, _ = reg_drot.solve_qr(c, p, q, 2.0, 1e-3, 20000, 1e-4)
+    x2, i2, _ = reg_drot.solve_qr(c, p, q, 2.0, 1e-3, 20000, 1e-4)
+    assert torch.equal(x1, x2) and strip(i1) == strip(i2)
+    g1, j1, _ = reg_drot.solve_gl(c, p, q, 3, 2.0, 1e-3, 20000, 1e-4)
+    g2, j2, _ = reg_drot.solve_gl(c, p, q, 3, 2.0, 1e-3, 20000, 1e-4)
+    assert torch.equal(g1, g2) and strip(j1) == strip(j2)
+
+
+def test_operator_argument_errors(cuda):
+    import reg_drot
+    c = torch.rand(3, 2, device=cuda)
+    p = torch.ones(2, device=cuda) / 2
+    q = torch.ones(3, device=cuda) / 3
+    with pytest.raises(RuntimeError, match="C.size\\(0\\) does not match"):
+        reg_drot.quadratic_drot(c, p, torch.ones(4, device=cuda), 2.0, 1e-2, 10, 1e-4)
+    with pytest.raises(RuntimeError, match="C.size\\(1\\) does not match"):
+        reg_drot.quadratic_drot(c, torch.ones(5, device=cuda), q, 2.0, 1e-2, 10, 1e-4)
+    with pytest.raises(RuntimeError, match="must be contiguous"):
+        reg_drot.quadratic_drot(c.t(), q, p, 2.0, 1e-2, 10, 1e-4)
+    with pytest.raises(RuntimeError, match="scalar type Float"):
+        reg_drot.group_lasso_drot(c.double(), p, q, 2, 2.0, 1e-2, 10, 1e-4)
+
+
+# --------------------------------------------------------------------------- golden vectors
+
+GOLD = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                            "npdrot_golden.npz"))
+MANIFEST = json.loads(bytes(GOLD["manifest"]).decode())
+ITER_CASES = [m for m in MANIFEST if m["kind"] in ("qr", "gl") and m["T"] >= 2]
+
+
+@pytest.mark.parametrize("case", ITER_CASES, ids=[m["name"] for m in ITER_CASES])
+def test_device_loop_matches_reference_numpy_iterates(cuda, solver_lib, case):
+    """drot_qr_solve / drot_gl_solve from the reference's cold and warm starts
+    against the reference numpy iterates (FP64), within FP32 accuracy."""
+    from reg_drot._lib import DrotResult
+    key = case["inputs"]
+    C64, p64, q64 = GOLD[key + "/C"], GOLD[key + "/p"], GOLD[key + "/q"]
+    nr, nc, T = case["nr"], case["nc"], case["T"]
+    C = torch.tensor(C64, dtype=torch.float32, device=cuda).contiguous()
+    p = torch.tensor(p64, dtype=torch.float32, device=cuda)
+    q = torch.tensor(q64, dtype=torch.float32, device=cuda)
+    s = float(np.float32(case["s"]))
+    x = torch.empty_like(C)
+    a = torch.empty(nr, device=cuda)
+    b = torch.empty(nc, device=cuda)
+    f1 = torch.empty(nr, device=cuda)
+    f2 = torch.empty(nc, device=cuda)
+    al = torch.empty(1, device=cuda)
+    st = torch.cuda.current_stream().cuda_stream
+    warm = 1 if case["start"] == "warm" else 0
+    assert solver_lib.drot_init_state(nr, nc, s, warm, p.data_ptr(), q.data_ptr(), x.data_ptr(),
+                                      a.data_ptr(), b.data_ptr(), f1.data_ptr(), f2.data_ptr(),
+                                      al.data_ptr(), st) == 0
+    res = DrotResult()
+    if case["kind"] == "qr":
+        nbytes = solver_lib.drot_qr_workspace_bytes(nr, nc)
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=cuda)
+        kappa = float(np.float32(1.0 + case["s"] * case["r_weight"] * (nr + nc)))
+        rc = solver_lib.drot_qr_solve(C.data_ptr(), p.data_ptr(), q.data_ptr(), nr, nc, s, kappa,
+                                      T, -1.0, x.data_ptr(), a.data_ptr(), b.data_ptr(),
+                                      f1.data_ptr(), f2.data_ptr(), al.data_ptr(), ws.data_ptr(),
+                                      nbytes, ctypes.byref(res), st)
+        xs = x.double()
+        if (T - 1) % 2 == 0:
+            xs = xs + s * C.double()
+    else:
+        G = len(case["bounds"]) - 1
+        nbytes = solver_lib.drot_gl_workspace_bytes(nr, nc, G)
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=cuda)
+        lam = float(np.float32(case["lam"]))
+        rc = solver_lib.drot_gl_solve(C.data_ptr(), p.data_ptr(), q.data_ptr(), nr, nc, G, s, lam,
+                                      T, -1.0, x.data_ptr(), a.data_ptr(), b.data_ptr(),
+                                      f1.data_ptr(), f2.data_ptr(), al.data_ptr(), ws.data_ptr(),
+                                      nbytes, ctypes.byref(res), st)
+        xs = x.double()
+    assert rc == 0
+    ref = GOLD[case["name"] + "/x"]
+    err = np.abs(xs.cpu().numpy() - ref).max() / np.abs(ref).max()
+    assert err <= 2e-5, err
