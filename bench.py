@@ -1,0 +1,437 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 DROT solver.
+
+Headline workload (one step = one full solve):
+  quadratic-regularised DROT, m = n = 3000, C ~ U[0,1) float32, p, q ~
+  Dirichlet(1), r_weight (alpha) = 1e-3, rho = 2, warm start, stop at a
+  relative marginal residual ||(X1-p, X^T1-q)||_2 / ||(p;q)||_2 < 1e-4.
+  Metric: solves/s (whole job).
+
+  value  solves with C, p, q resident in HBM, through reg_drot.solve_qr (the
+         drop-in operator's C-ABI entry point); L2 flushed between solves.
+  e2e    the same solve through the host-buffer C-ABI wrapper
+         (drot_qr_wrapper, the reference's quadratic_regularizer_drot_wrapper):
+         device allocation, H2D of C/p/q, solve, D2H of X per step.
+  roofline  the solve kernel: algorithmic bytes (12 B/element on iterations
+         that read C, 8 B on the others, 12 B for the final unfold) over its
+         measured time, against the measured HBM copy bandwidth.
+  cpu_baseline  the oracle (C restatement of the reference loop, OpenMP on all
+         host cores) timed on a bounded number of iterations of the same
+         solve and scaled to the iterations a solve takes.
+
+`--impl reference` times that CPU implementation alone (the reference's
+solver is CUDA and its CPU implementation is numpy; neither runs on the GPU
+host, so the oracle port stands in for it).
+
+Multi-GPU: the solve does not shard; N ranks run N independent replicas.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "regularized-drot_gb300")
+for _p in (REPO, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+N = 3000
+ALPHA = 1e-3
+RHO = 2.0
+REL_EPS = 1e-4
+SEED = 1234
+# DR iterations one solve of this workload takes (measured on the GPU solver;
+# the CPU restatement runs the same iteration map).  Used to scale the
+# bounded CPU samples to a full solve.
+ITERS_PER_SOLVE = 113831
+WORKLOAD = (f"QR-DROT {N}x{N}, C~U[0,1) fp32, p,q~Dirichlet(1), alpha={ALPHA}, rho={RHO}, "
+            f"warm start, stop at relative marginal residual {REL_EPS}")
+METRIC = f"solves/s at relative marginal error {REL_EPS} (QR-DROT {N}x{N}, alpha={ALPHA})"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def make_problem(n, seed=SEED):
+    rng = np.random.default_rng(seed)
+    c = rng.random((n, n), dtype=np.float32)
+    p = rng.dirichlet(np.ones(n)).astype(np.float32)
+    q = rng.dirichlet(np.ones(n)).astype(np.float32)
+    eps = REL_EPS * math.sqrt(float((p.astype(np.float64) ** 2).sum() +
+                                    (q.astype(np.float64) ** 2).sum()))
+    return c, p, q, eps
+
+
+def measured_peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic_per_iteration():
+    """DRAM bytes per DR iteration of the solve kernel from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "drot_solve_qr_3000.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_iteration:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+# --------------------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- CPU legs
+
+def cpu_sample(budget_s=12.0, threads=None):
+    """Time the oracle on a bounded number of iterations of the workload."""
+    from oracle import oracle as O
+    c, p, q, eps = make_problem(N)  # c is [n_cols, n_rows], the operator's layout
+    s = O.step_size(RHO, N, N)
+    kappa = O.qr_scale(s, ALPHA, N, N, "torch")
+    threads = threads or O.lib().oracle_max_threads()
+    O.qr_solve(c, p, q, s, kappa, 2, eps, threads=threads)  # page in, spin up threads
+    iters, spent = 0, 0.0
+    chunk = 10
+    while spent < budget_s:
+        t0 = time.perf_counter()
+        O.qr_solve(c, p, q, s, kappa, chunk, eps, threads=threads)
+        spent += time.perf_counter() - t0
+        iters += chunk
+        chunk = min(chunk * 2, 400)
+    per_iter = spent / iters
+    value = 1.0 / (per_iter * ITERS_PER_SOLVE)
+    return {"value": value, "unit": "solves/s", "cores": int(threads), "kind": "port",
+            "sample": (f"{iters} DR iterations of the {N}x{N} QR solve from the warm start "
+                       f"(FP32 oracle, {threads} OpenMP threads, {spent:.1f} s), scaled to the "
+                       f"{ITERS_PER_SOLVE} iterations of a full solve"),
+            "s_per_iteration": per_iter}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    for _ in range(args.warmup):
+        cpu_sample(budget_s=0.5)
+    vals = [cpu_sample(budget_s=10.0) for _ in range(args.steps)]
+    value = statistics.median(v["value"] for v in vals)
+    base = dict(vals[0])
+    base["value"] = value
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_rows": N, "n_cols": N, "alpha": ALPHA, "rho": RHO,
+                   "rel_eps": REL_EPS, "seed": SEED},
+        "cpu_baseline": base,
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------------- GPU legs
+
+def e2e_wrapper(c, p, q, eps, steps):
+    """Solves through drot_qr_wrapper with pinned host buffers (host in, host out)."""
+    import torch
+    from reg_drot import _lib
+    L = _lib.lib()
+    ct = torch.from_numpy(c).pin_memory()  # column-major n_rows x n_cols
+    pt = torch.from_numpy(p).pin_memory()
+    qt = torch.from_numpy(q).pin_memory()
+    s = float(np.float32(RHO) / (np.float32(N) + np.float32(N)))
+    dur, prep = ctypes.c_float(), ctypes.c_float()
+    nit, obj = ctypes.c_int(), ctypes.c_float()
+
+    def once():
+        ptr = L.drot_qr_wrapper(ct.data_ptr(), pt.data_ptr(), qt.data_ptr(), N, N, s, ALPHA,
+                                10 ** 9, eps, ctypes.byref(dur), ctypes.byref(prep),
+                                ctypes.byref(nit), ctypes.byref(obj), 1, 1)
+        if not ptr:
+            raise RuntimeError(f"drot_qr_wrapper failed: {_lib.status_string(L.drot_last_status())}")
+        L.drot_free_host(ptr)
+
+    once()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        once()
+    wall = time.perf_counter() - t0
+    return {"value": steps / wall, "unit": "solves/s",
+            "h2d_bytes_per_step": (N * N + 2 * N) * 4, "d2h_bytes_per_step": N * N * 4,
+            "n_iter": nit.value, "wall_s_per_step": wall / steps}
+
+
+def hbm_point(dev, flush):
+    """QR at 10000^2 (X + C = 800 MB, beyond L2) for a fixed iteration count."""
+    import torch
+    import reg_drot
+    n, iters = 10000, 400
+    c, p, q, _ = make_problem(n)
+    cd = torch.from_numpy(c).to(dev)
+    pd = torch.from_numpy(p).to(dev)
+    qd = torch.from_numpy(q).to(dev)
+    x, info, ws = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, 10, 0.0)
+    times = []
+    for _ in range(3):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        x, info, ws = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, iters, 0.0, out=x, workspace=ws)
+        b.record()
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b) / 1e3)
+    t = min(times)
+    it = info["iters_run"]
+    nbytes = float(n) * n * (12 * ((it + 1) // 2) + 8 * (it // 2))
+    ph = [v / it for v in info["phase_ms"]]
+    del cd, x, ws
+    return {"workload": f"QR-DROT {n}x{n}, {iters} iterations (X + C = 800 MB, HBM resident)",
+            "us_per_iteration": t / it * 1e6, "achieved_GBps": nbytes / t / 1e9,
+            "phase_us_per_iteration_cta0": [round(v * 1e3, 2) for v in ph]}
+
+
+def gl_da_point(dev):
+    """Group-lasso domain-adaptation solve (1500 source x 1000 target, 2 classes)."""
+    import reg_drot  # noqa: F401
+    from reg_drot import _lib
+    L = _lib.lib()
+    times, iters = [], []
+    for seed in range(5):
+        rng = np.random.default_rng(1234 + seed)
+        ns, nt = 1500, 1000
+        ys = np.repeat([0, 1], ns // 2)
+        xs = rng.normal(size=(ns, 2)) + np.where(ys[:, None] == 0, -2.0, 2.0) * np.array([1.0, 0.0])
+        A = np.eye(2) + 0.3 * rng.normal(size=(2, 2))
+        b = rng.normal(size=2)
+        yt = np.repeat([0, 1], nt // 2)
+        xt0 = rng.normal(size=(nt, 2)) + np.where(yt[:, None] == 0, -2.0, 2.0) * np.array([1.0, 0.0])
+        xt = xt0 @ A.T + b
+        C = ((xs[:, None, :] - xt[None, :, :]) ** 2).sum(-1)
+        C = (C / C.max()).astype(np.float32)          # [n_rows=source, n_cols=target]
+        cm = np.ascontiguousarray(C.T)                # column-major n_rows x n_cols
+        p = np.full(ns, 1.0 / ns, np.float32)
+        q = np.full(nt, 1.0 / nt, np.float32)
+        s = float(np.float32(RHO) / (np.float32(ns) + np.float32(nt)))
+        dur, prep = ctypes.c_float(), ctypes.c_float()
+        nit, obj = ctypes.c_int(), ctypes.c_float()
+        for rep in range(2):
+            ptr = L.drot_gl_wrapper(cm.ctypes.data, p.ctypes.data, q.ctypes.data, ns, nt, 2, s,
+                                    1e-3, 20000, 1e-4, ctypes.byref(dur), ctypes.byref(prep),
+                                    ctypes.byref(nit), ctypes.byref(obj), 1, 0)
+        times.append(dur.value / 1e3)
+        iters.append(nit.value)
+    return {"workload": "GL-DROT domain adaptation 1500 src x 1000 tgt, 2 classes, GL weight 1e-3 "
+                        "(C++ wrapper convention), eps 1e-4, rho 2, 20000 max iterations",
+            "median_solve_s": statistics.median(times), "median_iterations": statistics.median(iters),
+            "published_v100_median_s": 0.0619}
+
+
+def run_gpu(args):
+    import torch
+    import reg_drot
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    c, p, q, eps = make_problem(N, SEED)
+    cd = torch.from_numpy(c).to(dev)
+    pd = torch.from_numpy(p).to(dev)
+    qd = torch.from_numpy(q).to(dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    x, info, ws = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, 10 ** 9, eps)
+    for _ in range(max(args.warmup - 1, 0)):
+        flush.zero_()
+        x, info, ws = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, 10 ** 9, eps, out=x, workspace=ws)
+    torch.cuda.synchronize()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record()
+            x, _, ws = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, 10 ** 9, eps, out=x,
+                                         workspace=ws, sync=False)
+            ends[i].record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    info = reg_drot.read_result(ws)
+    step_s = [a.elapsed_time(b) / 1e3 for a, b in zip(starts, ends)]
+    total = sum(step_s)
+    if dist:
+        t = torch.tensor([total, wall], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total, wall = float(t[0]), float(t[1])
+    value = world * args.steps / total
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    it = info["iters_run"]
+    n_even = (it + 1) // 2
+    kernel_bytes = float(N) * N * (12 * n_even + 8 * (it - n_even) + (12 if info["converged"] else 0))
+    kernel_s = total / args.steps
+    peak, peak_kind = measured_peak()
+    achieved = kernel_bytes / kernel_s / 1e9
+    traffic_it = profile_traffic_per_iteration()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind,
+                "traffic": traffic_it * it if traffic_it is not None else None,
+                "algorithmic_bytes_per_launch": kernel_bytes,
+                "note": ("X + C = 72 MB stays L2-resident across the iterations of a solve; "
+                         "the 10000^2 point in extra.hbm_point is the HBM-resident case")}
+
+    e2e = e2e_wrapper(c, p, q, eps, args.steps)
+    extra = {"hbm_point": hbm_point(dev, flush), "gl_da": gl_da_point(dev)}
+    cpu = cpu_sample(budget_s=12.0) if world == 1 else None
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_rows": N, "n_cols": N, "alpha": ALPHA, "rho": RHO,
+                   "rel_eps": REL_EPS, "eps_abs": eps, "seed": SEED,
+                   "l2": "flushed (512 MB write) before every timed solve",
+                   "parallelism": f"replicas x{world}"},
+        "iterations_per_solve": it, "iterations_per_s": it / kernel_s,
+        "converged": info["converged"], "residual": info["residual"],
+        "phase_ms_per_solve_cta0": info["phase_ms"],
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")},
+        "e2e_detail": {"n_iter": e2e["n_iter"], "wall_s_per_step": e2e["wall_s_per_step"]},
+        "gpu_launches": 6 * args.steps,
+        "clocks": clk.summary(),
+        "wall_s_timed_region": wall,
+        "extra": extra,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_case(spec):
+    """One solve of the headline workload at size n for a fixed iteration count
+    (for profiler captures): --case n:iters[:gl]."""
+    import torch
+    import reg_drot
+    parts = spec.split(":")
+    n, iters = int(parts[0]), int(parts[1])
+    dev = torch.device("cuda", 0)
+    c, p, q, _ = make_problem(n)
+    cd, pd, qd = (torch.from_numpy(a).to(dev) for a in (c, p, q))
+    if len(parts) > 2 and parts[2] == "gl":
+        x, info, _ = reg_drot.solve_gl(cd, pd, qd, 2, RHO, ALPHA, iters, 0.0)
+    else:
+        x, info, _ = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, iters, 0.0)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": spec, "iters_run": info["iters_run"],
+                      "phase_ms": info["phase_ms"]}), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--case", default=None,
+                    help="n:iters[:gl] -- one fixed-length solve, for profiler captures")
+    args = ap.parse_args()
+    if args.case:
+        return run_case(args.case)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

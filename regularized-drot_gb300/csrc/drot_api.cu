@@ -99,7 +99,7 @@ static inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAl
 //   cta_sum/obj/res  grid doubles each
 struct Plan {
   int mode = 0, vec = 4, kv = 4, wt = 1, threads = 256, nbands = 1, P = 1, grid = 1, nsb = 1;
-  int band_h = 0, ns = 1;
+  int band_h = 0, ns = 1, p2_smem = 0, p2_cap_r = 0, p2_cap_c = 0;
   bool tma = false;
   size_t smem = 0;
   std::vector<int> bounds;
@@ -227,13 +227,17 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
     if (occ <= 0) return DROT_ERR_CUDA;
     const int max_grid = occ * dev.sms;
     if (mode == MODE_QR) {
-      pl.band_h = pl.wt * S;
-      pl.nbands = (nr + pl.band_h - 1) / pl.band_h;
+      // Fewest bands of at most wt*S rows, then equal heights (multiples of
+      // 4) so every band carries the same work.
+      const int cover = pl.wt * S;
+      pl.nbands = (nr + cover - 1) / cover;
       if (pl.nbands > max_grid) {
         if (pl.wt >= 16) return DROT_ERR_UNSUPPORTED;
         pl.wt = std::min(16, pl.wt * 2);
         continue;
       }
+      pl.band_h = (((nr + pl.nbands - 1) / pl.nbands) + 3) & ~3;
+      pl.nbands = (nr + pl.band_h - 1) / pl.band_h;
     } else {
       pl.nbands = G;
       if (G > max_grid) return DROT_ERR_UNSUPPORTED;
@@ -246,6 +250,30 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
     break;
   }
   if (pl.grid <= 0 || pl.nbands <= 0) return DROT_ERR_UNSUPPORTED;
+
+  // Phase-2 state of each CTA's row / column slice in shared memory when it
+  // is small and the CTAs stay co-resident with it.
+  {
+    const int capr = ((nr + pl.grid - 1) / pl.grid + 3) & ~3;
+    const int capc = ((nc + pl.grid - 1) / pl.grid + 3) & ~3;
+    const int p2f = 3 * (capr + capc);
+    const int warps = pl.threads / 32;
+    const size_t smem2 = solve_smem_bytes(warps, pl.wt, S, pl.ns, tma, p2f);
+    pl.p2_smem = 0;
+    pl.p2_cap_r = pl.p2_cap_c = 0;
+    if ((size_t)p2f * sizeof(float) <= 48 * 1024 && smem2 <= budget) {
+      bool ok = true;
+      if (smem2 > 48 * 1024)
+        ok = cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem2) == cudaSuccess;
+      if (ok && occupancy(fn, pl.threads, smem2) * dev.sms >= pl.grid) {
+        pl.p2_smem = 1;
+        pl.p2_cap_r = capr;
+        pl.p2_cap_c = capc;
+        pl.smem = smem2;
+      }
+    }
+  }
 
   size_t off = 512;
   pl.off_stats = 0;
@@ -306,14 +334,16 @@ static int path_override() {
   return 0;
 }
 
-// Plan for the given alignment: the TMA ring when the data allow it.
+// Plan for the given alignment.  The register path is the default: on this
+// part the fused update is bound by per-warp instruction latency, and two
+// 8-warp CTAs per SM with register-resident segments beat one 16-warp CTA
+// fed by the shared-memory TMA ring.  DROT_PATH=tma selects the ring.
 static int choose_plan(int mode, int nr, int nc, int G, bool aligned4, Plan& pl) {
   const int ov = path_override();
-  if (aligned4 && ov != 1) {
-    const int rc = make_plan(mode, nr, nc, G, 4, true, pl);
-    if (rc == DROT_OK || ov == 2) return rc;
+  if (ov == 2) {
+    if (!aligned4) return DROT_ERR_UNSUPPORTED;
+    return make_plan(mode, nr, nc, G, 4, true, pl);
   }
-  if (ov == 2) return DROT_ERR_UNSUPPORTED;
   return make_plan(mode, nr, nc, G, aligned4 ? 4 : 1, false, pl);
 }
 
@@ -389,11 +419,16 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
   // RN(1/kappa): the double quotient rounded to float is the correctly
   // rounded float reciprocal (53 >= 2*24 + 2).
   prm.kappa_rcp = (float)(1.0 / (double)A.kappa);
+  prm.nc_rcp = (float)(1.0 / (double)(float)A.nc);
+  prm.nr_rcp = (float)(1.0 / (double)(float)A.nr);
   prm.norm_eps = 1e-9;
   prm.max_iters = A.max_iters;
   prm.nbands = pl.nbands; prm.P = pl.P; prm.Wt = pl.wt; prm.nsb = pl.nsb;
   prm.band_h = pl.band_h;
   prm.ns = pl.ns;
+  prm.p2_smem = pl.p2_smem;
+  prm.p2_cap_r = pl.p2_cap_r;
+  prm.p2_cap_c = pl.p2_cap_c;
   for (size_t k = 0; k < pl.bounds.size(); ++k) prm.gbounds[k] = pl.bounds[k];
   prm.rowpart = (float*)(ws + pl.off_rowpart);
   prm.colpart = (float*)(ws + pl.off_colpart);

@@ -84,6 +84,8 @@ struct SolveParams {
   float s;             // step size
   float kappa;         // QR divisor
   float kappa_rcp;     // RN(1 / kappa)
+  float nc_rcp;        // RN(1 / float(nc))
+  float nr_rcp;        // RN(1 / float(nr))
   float lambda;        // GL threshold
   float eps;           // absolute residual tolerance
   double norm_eps;     // GL: constant added to the group norm (1e-9)
@@ -94,6 +96,9 @@ struct SolveParams {
   int nsb;             // nbands * Wt sub-bands (column partial rows)
   int band_h;          // QR: rows per band
   int ns;              // TMA ring stages per warp
+  int p2_smem;         // phase-2 state (p, q, a, b slices) in shared memory
+  int p2_cap_r;        // rows / columns per CTA slice (multiples of 4)
+  int p2_cap_c;
   float* rowpart;      // [P][nr]
   float* colpart;      // [nsb][nc]
   double* cta_sum;     // [grid]
@@ -160,6 +165,21 @@ __device__ __forceinline__ double block_sum_d(double v, double* scratch) {
   }
   __syncthreads();
   return scratch[nw];
+}
+
+// Sum of v[0..n) (FP64) over one warp: every lane loads its strided share
+// with the loads issued back to back, then a shuffle tree; all lanes get the
+// (deterministic) result.
+__device__ __forceinline__ double warp_sum_strided(const double* v, int n, int lane) {
+  double t = 0.0;
+  int i = lane;
+  for (; i + 96 < n; i += 128) {
+    const double a0 = __ldcg(v + i), a1 = __ldcg(v + i + 32), a2 = __ldcg(v + i + 64),
+                 a3 = __ldcg(v + i + 96);
+    t += (a0 + a1) + (a2 + a3);
+  }
+  for (; i < n; i += 32) t += __ldcg(v + i);
+  return warp_sum_d(t);
 }
 
 // Grid barrier.  Returns false when the run was aborted (time limit hit here
@@ -296,11 +316,11 @@ __device__ __forceinline__ void reduce_partials(int i0, int i1, const float* par
   for (int base = 0; base < items; base += per_round) {
     const int idx = base + (int)threadIdx.x / g;
     const bool live = idx < items;
-    double t = 0.0;
+    float t = 0.0f;
     if (live) {
       const float* pp = part + i0 + idx;
 #pragma unroll 4
-      for (int k = sub; k < np; k += g) t += (double)__ldcg(pp + (long long)k * stride);
+      for (int k = sub; k < np; k += g) t += __ldcg(pp + (long long)k * stride);
     }
     for (int o = g >> 1; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
     if (live && sub == 0) fin(i0 + idx, t);
@@ -311,13 +331,16 @@ __device__ __forceinline__ void reduce_partials(int i0, int i1, const float* par
 //   ring    TMA: W * ns * 2 * S floats (stage: X segment, C segment)
 //           reg: W * S floats (row-partial staging only)
 //   f1s     Wt * S floats (phi1 of the band rows)
+//   st2     3 * (cap_r + cap_c) floats when the phase-2 state is in shared
+//           memory (p, a, staged phi1 of the CTA's rows; q, b, phi2 of its columns)
 //   dscr    W + 1 doubles
-//   nslot   2 * W floats (GL team norms, double-buffered)
+//   nslot   2 * W doubles (per-warp objective sums; GL team norms)
 //   mbar    W * ns uint64 (TMA only)
-__host__ __device__ constexpr size_t solve_smem_bytes(int warps, int wt, int S, int ns, bool tma) {
+__host__ __device__ constexpr size_t solve_smem_bytes(int warps, int wt, int S, int ns, bool tma,
+                                                      int p2_floats = 0) {
   return sizeof(float) * (size_t)warps * S * (tma ? 2 * ns : 1) + sizeof(float) * (size_t)wt * S +
-         sizeof(double) * (warps + 1) + sizeof(double) * 2 * warps +
-         (tma ? sizeof(uint64_t) * (size_t)warps * ns : 0);
+         sizeof(float) * (size_t)p2_floats + sizeof(double) * (warps + 1) +
+         sizeof(double) * 2 * warps + (tma ? sizeof(uint64_t) * (size_t)warps * ns : 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -334,13 +357,23 @@ drot_solve_kernel(const SolveParams P) {
   const int W = blockDim.x >> 5;
   const int Wt = P.Wt;
   const int NS = TMA ? P.ns : 1;
+  const int capr = P.p2_smem ? P.p2_cap_r : 0;
+  const int capc = P.p2_smem ? P.p2_cap_c : 0;
   float* ring = reinterpret_cast<float*>(smem_raw);
   float* red = ring;  // row-partial staging aliases the ring (ring idle then)
   float* f1s = ring + (size_t)W * S * (TMA ? 2 * NS : 1);
-  double* dscr = reinterpret_cast<double*>(f1s + (size_t)Wt * S);
+  float* s_p = f1s + (size_t)Wt * S;
+  float* s_a = s_p + capr;
+  float* s_t1 = s_a + capr;
+  float* s_q = s_t1 + capr;
+  float* s_b = s_q + capc;
+  float* s_t2 = s_b + capc;
+  double* dscr = reinterpret_cast<double*>(s_t2 + capc);
   double* nslot = dscr + W + 1;
   uint64_t* mbar = reinterpret_cast<uint64_t*>(nslot + 2 * W);
   __shared__ int s_flag;
+  __shared__ float s_misc_f[2];
+  __shared__ double s_misc_d[2];
 
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
@@ -369,6 +402,7 @@ drot_solve_kernel(const SolveParams P) {
   int row0[KV];
   bool vany[KV], vall[KV];
   bool ein[KV][VEC];
+  bool full = active_warp;
 #pragma unroll
   for (int v = 0; v < KV; ++v) {
     row0[v] = base + k * S + v * SV + lane * VEC;
@@ -382,7 +416,10 @@ drot_solve_kernel(const SolveParams P) {
     }
     vany[v] = any;
     vall[v] = all;
+    full &= all;
   }
+  // Interior sub-bands (every lane's rows inside the band) skip all masking.
+  const bool wfull = __all_sync(0xffffffffu, full);
 
   // TMA segment of this warp: rows [seg_lo, seg_lo + seg_rows), 16-byte granular.
   const int seg_lo = base + k * S;
@@ -398,20 +435,32 @@ drot_solve_kernel(const SolveParams P) {
       fence_mbar_init();
       fence_proxy_async_shared();
     }
-    __syncthreads();
   }
 
-  // Phase-2 slices.
+  // Phase-2 slices; their marginals and duals stay in shared memory.
   const int G = gridDim.x;
   const int r_lo = (int)(((long long)P.nr * blockIdx.x) / G);
   const int r_hi = (int)(((long long)P.nr * (blockIdx.x + 1)) / G);
   const int k_lo = (int)(((long long)P.nc * blockIdx.x) / G);
   const int k_hi = (int)(((long long)P.nc * (blockIdx.x + 1)) / G);
+  if (P.p2_smem) {
+    for (int i = threadIdx.x; i < r_hi - r_lo; i += blockDim.x) {
+      s_p[i] = P.p[r_lo + i];
+      s_a[i] = P.a[r_lo + i];
+    }
+    for (int j = threadIdx.x; j < k_hi - k_lo; j += blockDim.x) {
+      s_q[j] = P.q[k_lo + j];
+      s_b[j] = P.b[k_lo + j];
+    }
+  }
+  __syncthreads();
 
   const float s = P.s;
   const float kappa = P.kappa;
   const float kappa_rcp = P.kappa_rcp;
-  float alpha = *P.alpha;
+  const float nc_f = (float)P.nc, nr_f = (float)P.nr;
+  const float nc_rcp = P.nc_rcp, nr_rcp = P.nr_rcp;
+  float alpha = *P.alpha;  // maintained by thread 0
   unsigned epoch = 0;
   int it = 0;
   bool converged = false;
@@ -449,14 +498,18 @@ drot_solve_kernel(const SolveParams P) {
     for (int v = 0; v < KV; ++v)
 #pragma unroll
       for (int e = 0; e < VEC; ++e) acc[v][e] = 0.0f;
-    double wsum = 0.0, wobj = 0.0;  // lane 0 of each warp accumulates
+    // Per-lane mass and objective sums over the warp's columns, carried as
+    // exact float pairs (TwoSum); FP64 only once per iteration.
+    float ms_hi = 0.0f, ms_lo = 0.0f, ob_hi = 0.0f, ob_lo = 0.0f;
     bool wfail = false;
 
     // One column of the band per team step.  EV selects the QR step that
     // reads C and stores the folded value X^ - sC (kernel_qr.hpp:171-278);
-    // the odd QR step reads X only (kernel_qr.hpp:280-376).
-    auto run_columns = [&](auto even_tag) {
+    // the odd QR step reads X only (kernel_qr.hpp:280-376).  FULL drops the
+    // row masks of interior sub-bands.
+    auto run_columns = [&](auto even_tag, auto full_tag) {
       constexpr bool EV = decltype(even_tag)::value;
+      constexpr bool FULL = decltype(full_tag)::value;
       constexpr bool WITH_C = (MODE == MODE_GL) || EV;
       const int ncw = (c1 - c0 - team + nteams - 1) / nteams;  // columns of this warp
       const uint32_t tx_bytes = seg_bytes * (WITH_C ? 2u : 1u);
@@ -470,78 +523,72 @@ drot_solve_kernel(const SolveParams P) {
         if constexpr (WITH_C) bulk_g2s(dx + S, P.c + (long long)jn * ld + seg_lo, seg_bytes, wbar + st);
         ++issued;
       };
-      if constexpr (TMA) {
-        if (seg_rows > 0 && lane == 0) {
-          // X was last written by generic stores; order them before the
-          // async-proxy reads.
-          fence_proxy_async_all();
-          const int pre = min(NS, ncw);
-          for (int n = 0; n < pre; ++n) issue(n);
-        }
-      }
-      int par = 0;
-      for (int n = 0; n < ncw; ++n, par ^= 1) {
-        const int j = c0 + team + n * nteams;
-        const float f2 = __ldcg(P.phi2 + j);
-        float* xcol = P.x + (long long)j * ld;
+
+      // Register path: the warp's segment of column j straight into registers.
+      auto load_reg = [&](int j, float (&xv)[KV][VEC], float (&cv)[KV][VEC]) {
+        const float* xcol = P.x + (long long)j * ld;
         const float* ccol = P.c + (long long)j * ld;
-        float xv[KV][VEC];
-        float cv[KV][VEC];
-        if constexpr (TMA) {
-          if (seg_rows > 0) {
-            const int st = (int)(pipe_cnt % (uint32_t)NS);
-            const uint32_t parity = (pipe_cnt / (uint32_t)NS) & 1u;
-            if (!wfail && !mbar_wait(wbar + st, parity, P.timeout_ns)) wfail = true;
-            ++pipe_cnt;
-            const float* sx = wring + (size_t)st * 2 * S;
 #pragma unroll
-            for (int v = 0; v < KV; ++v) {
-              const float4 t = *reinterpret_cast<const float4*>(sx + v * SV + lane * 4);
-              xv[v][0] = t.x; xv[v][1] = t.y; xv[v][2] = t.z; xv[v][3] = t.w;
-              if constexpr (WITH_C) {
-                const float4 u = *reinterpret_cast<const float4*>(sx + S + v * SV + lane * 4);
-                cv[v][0] = u.x; cv[v][1] = u.y; cv[v][2] = u.z; cv[v][3] = u.w;
-              } else {
-                cv[v][0] = cv[v][1] = cv[v][2] = cv[v][3] = 0.0f;
-              }
-              if (!vall[v]) {
-                // Stage bytes outside this warp's rows are stale: zero them so
-                // masked lanes add exact zeros to the objective.
+        for (int v = 0; v < KV; ++v) {
+          if (FULL || vany[v]) {
+            load_vec<VEC>(xcol + row0[v], xv[v]);
+            if constexpr (WITH_C) load_vec_nc<VEC>(ccol + row0[v], cv[v]);
+            else {
 #pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                  xv[v][e] = ein[v][e] ? xv[v][e] : 0.0f;
-                  cv[v][e] = ein[v][e] ? cv[v][e] : 0.0f;
-                }
-              }
-            }
-            __syncwarp();
-            if (lane == 0 && n + NS < ncw && !wfail) {
-              fence_proxy_async_shared();
-              issue(n + NS);
+              for (int e = 0; e < VEC; ++e) cv[v][e] = 0.0f;
             }
           } else {
 #pragma unroll
-            for (int v = 0; v < KV; ++v)
+            for (int e = 0; e < VEC; ++e) { xv[v][e] = 0.0f; cv[v][e] = 0.0f; }
+          }
+        }
+      };
+
+      // TMA path: wait for the stage of this warp's next column and read it.
+      auto load_tma = [&](int n, float (&xv)[KV][VEC], float (&cv)[KV][VEC]) {
+        if (seg_rows > 0) {
+          const int st = (int)(pipe_cnt % (uint32_t)NS);
+          const uint32_t parity = (pipe_cnt / (uint32_t)NS) & 1u;
+          if (!wfail && !mbar_wait(wbar + st, parity, P.timeout_ns)) wfail = true;
+          ++pipe_cnt;
+          const float* sx = wring + (size_t)st * 2 * S;
 #pragma unroll
-              for (int e = 0; e < VEC; ++e) { xv[v][e] = 0.0f; cv[v][e] = 0.0f; }
+          for (int v = 0; v < KV; ++v) {
+            const float4 t = *reinterpret_cast<const float4*>(sx + v * SV + lane * 4);
+            xv[v][0] = t.x; xv[v][1] = t.y; xv[v][2] = t.z; xv[v][3] = t.w;
+            if constexpr (WITH_C) {
+              const float4 u = *reinterpret_cast<const float4*>(sx + S + v * SV + lane * 4);
+              cv[v][0] = u.x; cv[v][1] = u.y; cv[v][2] = u.z; cv[v][3] = u.w;
+            } else {
+              cv[v][0] = cv[v][1] = cv[v][2] = cv[v][3] = 0.0f;
+            }
+            if (!FULL && !vall[v]) {
+              // Stage bytes outside this warp's rows are stale: zero them so
+              // masked lanes add exact zeros to the objective.
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                xv[v][e] = ein[v][e] ? xv[v][e] : 0.0f;
+                cv[v][e] = ein[v][e] ? cv[v][e] : 0.0f;
+              }
+            }
+          }
+          __syncwarp();
+          if (lane == 0 && n + NS < ncw && !wfail) {
+            fence_proxy_async_shared();
+            issue(n + NS);
           }
         } else {
 #pragma unroll
-          for (int v = 0; v < KV; ++v) {
-            if (vany[v]) {
-              load_vec<VEC>(xcol + row0[v], xv[v]);
-              if constexpr (WITH_C) load_vec_nc<VEC>(ccol + row0[v], cv[v]);
-              else {
+          for (int v = 0; v < KV; ++v)
 #pragma unroll
-                for (int e = 0; e < VEC; ++e) cv[v][e] = 0.0f;
-              }
-            } else {
-#pragma unroll
-              for (int e = 0; e < VEC; ++e) { xv[v][e] = 0.0f; cv[v][e] = 0.0f; }
-            }
-          }
+            for (int e = 0; e < VEC; ++e) { xv[v][e] = 0.0f; cv[v][e] = 0.0f; }
         }
+      };
 
+      // Prox, store and partial sums of column j (segment in xv / cv).
+      auto finish = [&](int j, float (&xv)[KV][VEC], const float (&cv)[KV][VEC], int par) {
+        const float f2 = __ldcg(P.phi2 + j);
+        float* xcol = P.x + (long long)j * ld;
         float f1[KV][VEC];
 #pragma unroll
         for (int v = 0; v < KV; ++v) {
@@ -555,23 +602,40 @@ drot_solve_kernel(const SolveParams P) {
 
         float colp = 0.0f, objp = 0.0f;
         if constexpr (MODE == MODE_QR) {
+          // t = X + phi1 + phi2 (- sC); the rare nonzero t below 2^-90 sends
+          // the whole column through the IEEE division (one warp vote).
+          unsigned tmin = 0xffffffffu;
 #pragma unroll
           for (int v = 0; v < KV; ++v)
 #pragma unroll
             for (int e = 0; e < VEC; ++e) {
               float t = (xv[v][e] + f1[v][e]) + f2;
               if constexpr (EV) t = fmaf(-s, cv[v][e], t);
-              float y = div_rn_by(fmaxf(t, 0.0f), kappa, kappa_rcp);
-              y = ein[v][e] ? y : 0.0f;
-              if constexpr (EV) {
-                xv[v][e] = fmaf(-s, cv[v][e], y);
-                objp = fmaf(y, cv[v][e], objp);
-              } else {
-                xv[v][e] = y;
-              }
-              acc[v][e] += y;
-              colp += y;
+              xv[v][e] = t;
+              tmin = min(tmin, (unsigned)__float_as_int(t) - 1u);
             }
+          const bool slow = __any_sync(0xffffffffu, tmin < kDivTinyBitsM1);
+          auto body = [&](auto slow_tag) {
+            constexpr bool SLOW = decltype(slow_tag)::value;
+#pragma unroll
+            for (int v = 0; v < KV; ++v)
+#pragma unroll
+              for (int e = 0; e < VEC; ++e) {
+                const float a = fmaxf(xv[v][e], 0.0f);
+                float y = SLOW ? a / kappa : div_rn_by_fma(a, kappa, kappa_rcp);
+                if constexpr (!FULL) y = ein[v][e] ? y : 0.0f;
+                if constexpr (EV) {
+                  xv[v][e] = fmaf(-s, cv[v][e], y);
+                  objp = fmaf(y, cv[v][e], objp);
+                } else {
+                  xv[v][e] = y;
+                }
+                acc[v][e] += y;
+                colp += y;
+              }
+          };
+          if (slow) body(std::true_type());
+          else body(std::false_type());
         } else {
           float nsl = 0.0f;
 #pragma unroll
@@ -580,7 +644,7 @@ drot_solve_kernel(const SolveParams P) {
             for (int e = 0; e < VEC; ++e) {
               const float t = fmaf(-s, cv[v][e], (xv[v][e] + f1[v][e]) + f2);
               float y = fmaxf(t, 0.0f);
-              y = ein[v][e] ? y : 0.0f;
+              if constexpr (!FULL) y = ein[v][e] ? y : 0.0f;
               xv[v][e] = y;
               nsl = fmaf(y, y, nsl);
             }
@@ -608,7 +672,7 @@ drot_solve_kernel(const SolveParams P) {
 
 #pragma unroll
         for (int v = 0; v < KV; ++v) {
-          if (vall[v]) {
+          if (FULL || vall[v]) {
             store_vec<VEC>(xcol + row0[v], xv[v]);
           } else if (vany[v]) {
 #pragma unroll
@@ -617,29 +681,82 @@ drot_solve_kernel(const SolveParams P) {
           }
         }
 
+        float e1;
+        two_sum(ms_hi, colp, ms_hi, e1);
+        ms_lo += e1;
+        if constexpr (WITH_C) {
+          two_sum(ob_hi, objp, ob_hi, e1);
+          ob_lo += e1;
+        }
         colp = warp_sum(colp);
-        if constexpr (WITH_C) objp = warp_sum(objp);
-        if (lane == 0) {
-          P.colpart[(long long)sb * P.nc + j] = colp;
-          wsum += (double)colp;
-          if constexpr (WITH_C) wobj += (double)objp;
+        if (lane == 0) P.colpart[(long long)sb * P.nc + j] = colp;
+      };
+
+      if constexpr (TMA) {
+        if (seg_rows > 0 && lane == 0) {
+          // X was last written by generic stores; order them before the
+          // async-proxy reads.
+          fence_proxy_async_all();
+          const int pre = min(NS, ncw);
+          for (int n = 0; n < pre; ++n) issue(n);
+        }
+        int par = 0;
+        for (int n = 0; n < ncw; ++n, par ^= 1) {
+          float xv[KV][VEC], cv[KV][VEC];
+          load_tma(n, xv, cv);
+          finish(c0 + team + n * nteams, xv, cv, par);
+        }
+      } else if constexpr (!WITH_C) {
+        // X-only QR step: two columns in flight per warp (the registers the
+        // C segment uses on even steps).
+        float cz[KV][VEC];
+#pragma unroll
+        for (int v = 0; v < KV; ++v)
+#pragma unroll
+          for (int e = 0; e < VEC; ++e) cz[v][e] = 0.0f;
+        for (int n = 0; n < ncw; n += 2) {
+          const int ja = c0 + team + n * nteams;
+          const bool two = n + 1 < ncw;
+          float xa[KV][VEC], xb[KV][VEC], dummy[KV][VEC];
+          load_reg(ja, xa, dummy);
+          if (two) load_reg(ja + nteams, xb, dummy);
+          finish(ja, xa, cz, 0);
+          if (two) finish(ja + nteams, xb, cz, 0);
+        }
+      } else {
+        int par = 0;
+        for (int n = 0; n < ncw; ++n, par ^= 1) {
+          float xv[KV][VEC], cv[KV][VEC];
+          load_reg(c0 + team + n * nteams, xv, cv);
+          finish(c0 + team + n * nteams, xv, cv, par);
         }
       }
     };
     if (active_warp) {
-      if (with_c) run_columns(std::integral_constant<bool, true>());
-      else run_columns(std::integral_constant<bool, false>());
+      if (with_c) {
+        if (wfull) run_columns(std::true_type(), std::true_type());
+        else run_columns(std::true_type(), std::false_type());
+      } else {
+        if (wfull) run_columns(std::false_type(), std::true_type());
+        else run_columns(std::false_type(), std::false_type());
+      }
     }
     if (wfail && lane == 0) atomicExch(P.abort_flag, 1);
 
-    // CTA reduction of the row partials (fixed order over teams).
+    // CTA reduction of the row partials (fixed order over teams) and of the
+    // mass / objective (FP64 across lanes and warps).
+    const double wsum = warp_sum_d((double)ms_hi + (double)ms_lo);
+    const double wobj = with_c ? warp_sum_d((double)ob_hi + (double)ob_lo) : 0.0;
     __syncthreads();
 #pragma unroll
     for (int v = 0; v < KV; ++v)
 #pragma unroll
       for (int e = 0; e < VEC; ++e)
         red[(size_t)warp * S + v * SV + lane * VEC + e] = acc[v][e];
-    if (lane == 0) dscr[warp] = wsum;
+    if (lane == 0) {
+      dscr[warp] = wsum;
+      nslot[warp] = wobj;
+    }
     __syncthreads();
     {
       const int cover = Wt * S;
@@ -653,18 +770,15 @@ drot_solve_kernel(const SolveParams P) {
         }
       }
     }
-    if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (int w = 0; w < W; ++w) t += dscr[w];
-      P.cta_sum[blockIdx.x] = t;
-    }
-    __syncthreads();
-    if (lane == 0) dscr[warp] = wobj;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (int w = 0; w < W; ++w) t += dscr[w];
-      P.cta_obj[blockIdx.x] = t;
+    if (warp == 0) {
+      double t = lane < W ? dscr[lane] : 0.0;
+      double o = lane < W ? nslot[lane] : 0.0;
+      t = warp_sum_d(t);
+      if (with_c) o = warp_sum_d(o);
+      if (lane == 0) {
+        P.cta_sum[blockIdx.x] = t;
+        if (with_c) P.cta_obj[blockIdx.x] = o;
+      }
     }
 
     stamp(1);
@@ -672,54 +786,85 @@ drot_solve_kernel(const SolveParams P) {
     stamp(2);
 
     // ------------------------------------------------------------ phase 2
-    double sig = 0.0;
-    for (int i = threadIdx.x; i < G; i += blockDim.x) sig += __ldcg(P.cta_sum + i);
-    sig = block_sum_d(sig, dscr);
-    double objall = 0.0;
-    if (with_c && blockIdx.x == 0) {
-      for (int i = threadIdx.x; i < G; i += blockDim.x) objall += __ldcg(P.cta_obj + i);
-      objall = block_sum_d(objall, dscr);
-    }
-    const float sigma = (float)sig;
-    const float gamma =
-        (float)((2.0 * ((double)sigma - 1.0) - (double)alpha) / (double)(P.nr + P.nc));
-    double res = 0.0;
-    // Rows and columns of this CTA's slice: partial sums over the column
-    // chunks / sub-bands (grouped loads, fixed order), then the dual update.
-    reduce_partials(r_lo, r_hi, P.rowpart, P.nr, P.P, [&](int i, double t) {
-      const float rs = (float)t - __ldg(P.p + i);
-      const float ab = P.a[i] - rs;
-      P.phi1[i] = ((ab - rs) + gamma) / (float)P.nc;
-      P.a[i] = ab;
-      res += (double)rs * (double)rs;
-    });
-    reduce_partials(k_lo, k_hi, P.colpart, P.nc, P.nsb, [&](int j, double t) {
-      const float cs = (float)t - __ldg(P.q + j);
-      const float ab = P.b[j] - cs;
-      P.phi2[j] = ((ab - cs) + gamma) / (float)P.nr;
-      P.b[j] = ab;
-      res += (double)cs * (double)cs;
-    });
+    // (a) warp 0 sums the CTA masses (FP64) into sigma and derives gamma and
+    //     the next alpha (thread 0 owns alpha);
+    // (b) meanwhile every thread reduces the partials of its rows / columns
+    //     (float tree, fixed order) and updates the marginal residuals and
+    //     the duals a, b; (dual - residual) is staged until gamma is known;
+    // (c) one block sync, then phi = (staged + gamma) / n_cols (or n_rows).
     const bool check = (MODE == MODE_GL) || even;
+    if (warp == 0) {
+      const double t = warp_sum_strided(P.cta_sum, G, lane);
+      if (lane == 0) {
+        const float sigma = (float)t;
+        s_misc_f[0] = (float)((2.0 * ((double)sigma - 1.0) - (double)alpha) /
+                              (double)(P.nr + P.nc));
+        alpha = (float)(((double)alpha + 1.0) - (double)sigma);
+        s_misc_d[0] = t;
+      }
+    }
+    double res = 0.0;
+    const bool sm2 = P.p2_smem != 0;
+    reduce_partials(r_lo, r_hi, P.rowpart, P.nr, P.P, [&](int i, float t) {
+      const int li = i - r_lo;
+      const float rs = t - (sm2 ? s_p[li] : __ldg(P.p + i));
+      const float ab = (sm2 ? s_a[li] : P.a[i]) - rs;
+      if (sm2) {
+        s_a[li] = ab;
+        s_t1[li] = ab - rs;
+      } else {
+        P.a[i] = ab;
+        P.phi1[i] = ab - rs;
+      }
+      res = fma((double)rs, (double)rs, res);
+    });
+    reduce_partials(k_lo, k_hi, P.colpart, P.nc, P.nsb, [&](int j, float t) {
+      const int lj = j - k_lo;
+      const float cs = t - (sm2 ? s_q[lj] : __ldg(P.q + j));
+      const float ab = (sm2 ? s_b[lj] : P.b[j]) - cs;
+      if (sm2) {
+        s_b[lj] = ab;
+        s_t2[lj] = ab - cs;
+      } else {
+        P.b[j] = ab;
+        P.phi2[j] = ab - cs;
+      }
+      res = fma((double)cs, (double)cs, res);
+    });
     if (check) {
-      res = block_sum_d(res, dscr);
-      if (threadIdx.x == 0) P.cta_res[blockIdx.x] = res;
+      res = warp_sum_d(res);
+      if (lane == 0) dscr[warp] = res;
     }
-    alpha = (float)(((double)alpha + 1.0) - (double)sigma);
-    last_sigma = sig;
-    if (with_c) {
-      last_obj = objall;
-      obj_valid = 1;
+    __syncthreads();
+    {
+      const float gamma = s_misc_f[0];
+      for (int i = threadIdx.x; i < r_hi - r_lo; i += blockDim.x) {
+        const float t = sm2 ? s_t1[i] : __ldcg(P.phi1 + r_lo + i);
+        P.phi1[r_lo + i] = div_rn_by(t + gamma, nc_f, nc_rcp);
+      }
+      for (int j = threadIdx.x; j < k_hi - k_lo; j += blockDim.x) {
+        const float t = sm2 ? s_t2[j] : __ldcg(P.phi2 + k_lo + j);
+        P.phi2[k_lo + j] = div_rn_by(t + gamma, nr_f, nr_rcp);
+      }
     }
+    if (check && warp == 0) {
+      double t = lane < W ? dscr[lane] : 0.0;
+      t = warp_sum_d(t);
+      if (lane == 0) P.cta_res[blockIdx.x] = t;
+    }
+    last_sigma = s_misc_d[0];
+    if (with_c) obj_valid = 1;
 
     stamp(3);
     if (!grid_barrier(P, epoch, &s_flag)) { aborted = true; break; }
 
     if (check) {
-      double r2 = 0.0;
-      for (int i = threadIdx.x; i < G; i += blockDim.x) r2 += __ldcg(P.cta_res + i);
-      r2 = block_sum_d(r2, dscr);
-      last_res = sqrt(r2);
+      if (warp == 0) {
+        const double t = warp_sum_strided(P.cta_res, G, lane);
+        if (lane == 0) s_misc_d[1] = t;
+      }
+      __syncthreads();
+      last_res = sqrt(s_misc_d[1]);
       const bool stop = (MODE == MODE_QR) ? (last_res < (double)P.eps)
                                           : (last_res <= (double)P.eps);
       if (stop) {
@@ -754,6 +899,16 @@ drot_solve_kernel(const SolveParams P) {
       }
     }
   }
+  // Duals of this CTA's slice back to global memory (the state outputs).
+  if (P.p2_smem) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < r_hi - r_lo; i += blockDim.x) P.a[r_lo + i] = s_a[i];
+    for (int j = threadIdx.x; j < k_hi - k_lo; j += blockDim.x) P.b[k_lo + j] = s_b[j];
+  }
+  // <C, X> of the last objective-bearing iteration: the CTA partials of that
+  // iteration are the last ones written (visible since its barriers).
+  if (blockIdx.x == 0 && warp == 0 && obj_valid && !aborted)
+    last_obj = warp_sum_strided(P.cta_obj, G, lane);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     DeviceStats* st = P.stats;
     st->iters_run = converged ? it + 1 : it;

@@ -35,6 +35,20 @@ namespace drot {
 // Smallest dividend handled by the FMA sequence (2^-90).
 constexpr float kDivTiny = 8.0779356e-28f;
 
+// Bit pattern of kDivTiny minus one: a float t >= 0 with
+// (uint32)(bits(t) - 1) < kDivTinyBitsM1 is a nonzero dividend below 2^-90.
+constexpr unsigned kDivTinyBitsM1 = 0x12800000u - 1u;
+
+// The FMA sequence alone: a / b correctly rounded for a == 0 or
+// |a| >= 2^-90, b > 0 finite, y == RN(1/b).
+DROT_HD float div_rn_by_fma(float a, float b, float y) {
+  const float q0 = a * y;
+  const float r0 = fmaf(-b, q0, a);
+  const float q1 = fmaf(r0, y, q0);
+  const float r1 = fmaf(-b, q1, a);
+  return fmaf(r1, y, q1);
+}
+
 // a / b correctly rounded, for b > 0 finite and y == RN(1/b).  Zero takes
 // the FMA path too (every step is exact); only nonzero dividends below 2^-90
 // use the plain division.
@@ -42,11 +56,7 @@ DROT_HD float div_rn_by(float a, float b, float y) {
   if (a != 0.0f && fabsf(a) < kDivTiny) {
     return a / b;
   }
-  const float q0 = a * y;
-  const float r0 = fmaf(-b, q0, a);
-  const float q1 = fmaf(r0, y, q0);
-  const float r1 = fmaf(-b, q1, a);
-  return fmaf(r1, y, q1);
+  return div_rn_by_fma(a, b, y);
 }
 
 }  // namespace drot
