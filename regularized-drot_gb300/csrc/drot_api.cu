@@ -165,6 +165,8 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
   pl.tma = tma;
   const int SV = 32 * vec;
   if (mode == MODE_QR) {
+    // Four 128-bit vectors per lane (512-row sub-bands); short panels use
+    // fewer so lanes are not left idle.
     pl.kv = nr <= SV ? 1 : (nr <= 2 * SV ? 2 : 4);
     pl.wt = 1;
   } else {
@@ -193,11 +195,17 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
   const int S = SV * pl.kv;
   SolveFn fn = kernel_for(mode, vec, pl.kv, tma);
   if (!fn) return DROT_ERR_UNSUPPORTED;
-  const size_t budget = (size_t)std::max(dev.smem_optin, 48 * 1024) - 1024;
+  // TMA ring: DROT_TMA_CTAS (1 or 2) CTAs per SM share the shared memory.
+  const int tma_ctas = tma ? std::max(1, std::min(2, getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1)) : 1;
+  const size_t budget = (size_t)std::max(dev.smem_optin, 48 * 1024) / tma_ctas - 1024;
 
+  // Warps per CTA: 8 on the register path (two CTAs per SM), up to 16 when
+  // a band needs teams of 3 or more warps (fewer CTAs per band keeps the
+  // phase-2 partial count down).
   const int wtarget = tma ? tma_warps() : 8;
   for (int attempt = 0; attempt < 8; ++attempt) {
-    int teams = pl.wt >= wtarget ? 1 : std::max(1, wtarget / pl.wt);
+    const int wcap = (!tma && pl.wt >= 3) ? 16 : wtarget;
+    int teams = pl.wt >= wcap ? 1 : std::max(1, wcap / pl.wt);
     int warps = teams * pl.wt;
     if (tma) {
       // Deepest ring that fits; fewer teams when two stages do not fit.
@@ -295,10 +303,10 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
 // Plans are cached per (device, mode, shape, path): planning queries the
 // occupancy calculator, which costs microseconds per call.
 struct PlanKey {
-  int dev, mode, nr, nc, G, vec, tma, warps;
+  int dev, mode, nr, nc, G, vec, tma, warps, ctas;
   bool operator==(const PlanKey& o) const {
     return dev == o.dev && mode == o.mode && nr == o.nr && nc == o.nc && G == o.G &&
-           vec == o.vec && tma == o.tma && warps == o.warps;
+           vec == o.vec && tma == o.tma && warps == o.warps && ctas == o.ctas;
   }
 };
 
@@ -309,7 +317,8 @@ static int make_plan(int mode, int nr, int nc, int G, int vec, bool tma, Plan& p
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return DROT_ERR_CUDA;
   const PlanKey key = {dev, mode, nr, nc, mode == MODE_GL ? G : 0, vec, tma ? 1 : 0,
-                       tma ? tma_warps() : 8};
+                       tma ? tma_warps() : 8,
+                       tma && getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1};
   {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     for (auto& e : g_plans)

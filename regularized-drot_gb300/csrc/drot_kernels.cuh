@@ -167,18 +167,22 @@ __device__ __forceinline__ double block_sum_d(double v, double* scratch) {
   return scratch[nw];
 }
 
-// Sum of v[0..n) (FP64) over one warp: every lane loads its strided share
-// with the loads issued back to back, then a shuffle tree; all lanes get the
-// (deterministic) result.
+// Sum of v[0..n) (FP64) over one warp: every lane issues its first 16
+// strided loads at once (grids up to 512 CTAs take one round trip), then a
+// fixed add tree and a shuffle tree; all lanes get the same result.
 __device__ __forceinline__ double warp_sum_strided(const double* v, int n, int lane) {
-  double t = 0.0;
-  int i = lane;
-  for (; i + 96 < n; i += 128) {
-    const double a0 = __ldcg(v + i), a1 = __ldcg(v + i + 32), a2 = __ldcg(v + i + 64),
-                 a3 = __ldcg(v + i + 96);
-    t += (a0 + a1) + (a2 + a3);
+  double a[16];
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    const int i = lane + 32 * u;
+    a[u] = i < n ? __ldcg(v + i) : 0.0;
   }
-  for (; i < n; i += 32) t += __ldcg(v + i);
+#pragma unroll
+  for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+    for (int u = 0; u < w; ++u) a[u] += a[u + w];
+  double t = a[0];
+  for (int i = lane + 512; i < n; i += 32) t += __ldcg(v + i);
   return warp_sum_d(t);
 }
 
@@ -299,15 +303,19 @@ __device__ __forceinline__ void store_vec(float* ptr, const float (&v)[VEC]) {
   }
 }
 
-// Sums the np partials of each item i in [i0, i1) (partial pp of item i at
-// part[pp * stride + i]) with g threads per item, g a power of two <= 32
-// chosen so the items fill the block; partial order and shuffle tree are
-// fixed, so the sums are deterministic.  fin(i, sum) runs on the item's
-// first thread.
-template <typename Fin>
-__device__ __forceinline__ void reduce_partials(int i0, int i1, const float* part,
-                                                long long stride, int np, Fin fin) {
-  const int items = i1 - i0;
+// Sums the partials of the CTA's rows [r0, r1) (np_r partials, row i's
+// partial k at rowpart[k * nr + i]) and columns [k0, k1) (np_c partials at
+// colpart[k * nc + j]) in one pass: g threads per item, g a power of two
+// <= 32 chosen so the items fill the block, every thread's loads issued
+// together; load order, add tree and shuffle tree are fixed, so the sums are
+// deterministic.  fin_r(i, sum) / fin_c(j, sum) run on the item's first thread.
+template <typename FinR, typename FinC>
+__device__ __forceinline__ void reduce_partials(int r0, int r1, int k0, int k1,
+                                                const float* rowpart, const float* colpart,
+                                                long long nr, long long nc, int np_r, int np_c,
+                                                FinR fin_r, FinC fin_c) {
+  const int R = r1 - r0;
+  const int items = R + (k1 - k0);
   if (items <= 0) return;
   int g = 32;
   while (g > 1 && items * g > (int)blockDim.x) g >>= 1;
@@ -316,14 +324,26 @@ __device__ __forceinline__ void reduce_partials(int i0, int i1, const float* par
   for (int base = 0; base < items; base += per_round) {
     const int idx = base + (int)threadIdx.x / g;
     const bool live = idx < items;
+    const bool is_row = idx < R;
+    const float* pp = is_row ? rowpart + r0 + idx : colpart + k0 + (idx - R);
+    const long long stride = is_row ? nr : nc;
+    const int np = is_row ? np_r : np_c;
     float t = 0.0f;
     if (live) {
-      const float* pp = part + i0 + idx;
-#pragma unroll 4
-      for (int k = sub; k < np; k += g) t += __ldcg(pp + (long long)k * stride);
+      float a[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int kk = sub + u * g;
+        a[u] = kk < np ? __ldcg(pp + (long long)kk * stride) : 0.0f;
+      }
+      t = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+      for (int kk = sub + 8 * g; kk < np; kk += g) t += __ldcg(pp + (long long)kk * stride);
     }
     for (int o = g >> 1; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (live && sub == 0) fin(i0 + idx, t);
+    if (live && sub == 0) {
+      if (is_row) fin_r(r0 + idx, t);
+      else fin_c(k0 + idx - R, t);
+    }
   }
 }
 
@@ -398,26 +418,25 @@ drot_solve_kernel(const SolveParams P) {
   const long long ld = P.ld;
   const int sb = band * Wt + k;
 
-  // Rows owned by this lane and their validity masks (loop invariant).
-  int row0[KV];
-  bool vany[KV], vall[KV];
-  bool ein[KV][VEC];
+  // Rows owned by this lane; validity is recomputed where needed (masks held
+  // in registers would cost more than the two compares).
+  const int lrow = base + k * S + lane * VEC;
+  auto row0f = [&](int v) { return lrow + v * SV; };
+  auto einf = [&](int v, int e) {
+    const int r = lrow + v * SV + e;
+    return active_warp && r >= lo && r < hi;
+  };
+  auto vanyf = [&](int v) {
+    const int r = lrow + v * SV;
+    return active_warp && r + VEC > lo && r < hi;
+  };
+  auto vallf = [&](int v) {
+    const int r = lrow + v * SV;
+    return active_warp && r >= lo && r + VEC <= hi;
+  };
   bool full = active_warp;
 #pragma unroll
-  for (int v = 0; v < KV; ++v) {
-    row0[v] = base + k * S + v * SV + lane * VEC;
-    bool any = false, all = true;
-#pragma unroll
-    for (int e = 0; e < VEC; ++e) {
-      const int r = row0[v] + e;
-      ein[v][e] = active_warp && r >= lo && r < hi;
-      any |= ein[v][e];
-      all &= ein[v][e];
-    }
-    vany[v] = any;
-    vall[v] = all;
-    full &= all;
-  }
+  for (int v = 0; v < KV; ++v) full &= vallf(v);
   // Interior sub-bands (every lane's rows inside the band) skip all masking.
   const bool wfull = __all_sync(0xffffffffu, full);
 
@@ -470,14 +489,23 @@ drot_solve_kernel(const SolveParams P) {
   double last_res = -1.0;
   double last_sigma = 0.0;
 
+  // Stage timers of CTA 0 (thread 0, in shared memory to keep them out of
+  // the registers of every thread).
   const bool timer = blockIdx.x == 0;
-  unsigned long long tp[5] = {0, 0, 0, 0, 0};
-  double tacc[4] = {0.0, 0.0, 0.0, 0.0};
+  __shared__ unsigned long long s_tp;
+  __shared__ double s_tacc[4];
+  if (threadIdx.x == 0) {
+    s_tp = 0;
+    for (int q = 0; q < 4; ++q) s_tacc[q] = 0.0;
+  }
   auto stamp = [&](int k2) {  // CTA 0 only (block-uniform)
     if (timer) {
       __syncthreads();
-      tp[k2] = globaltimer_ns();
-      if (k2 > 0) tacc[k2 - 1] += (double)(tp[k2] - tp[k2 - 1]);
+      if (threadIdx.x == 0) {
+        const unsigned long long now = globaltimer_ns();
+        if (k2 > 0) s_tacc[k2 - 1] += (double)(now - s_tp);
+        s_tp = now;
+      }
     }
   };
 
@@ -530,9 +558,9 @@ drot_solve_kernel(const SolveParams P) {
         const float* ccol = P.c + (long long)j * ld;
 #pragma unroll
         for (int v = 0; v < KV; ++v) {
-          if (FULL || vany[v]) {
-            load_vec<VEC>(xcol + row0[v], xv[v]);
-            if constexpr (WITH_C) load_vec_nc<VEC>(ccol + row0[v], cv[v]);
+          if (FULL || vanyf(v)) {
+            load_vec<VEC>(xcol + row0f(v), xv[v]);
+            if constexpr (WITH_C) load_vec_nc<VEC>(ccol + row0f(v), cv[v]);
             else {
 #pragma unroll
               for (int e = 0; e < VEC; ++e) cv[v][e] = 0.0f;
@@ -562,13 +590,13 @@ drot_solve_kernel(const SolveParams P) {
             } else {
               cv[v][0] = cv[v][1] = cv[v][2] = cv[v][3] = 0.0f;
             }
-            if (!FULL && !vall[v]) {
+            if (!FULL && !vallf(v)) {
               // Stage bytes outside this warp's rows are stale: zero them so
               // masked lanes add exact zeros to the objective.
 #pragma unroll
               for (int e = 0; e < 4; ++e) {
-                xv[v][e] = ein[v][e] ? xv[v][e] : 0.0f;
-                cv[v][e] = ein[v][e] ? cv[v][e] : 0.0f;
+                xv[v][e] = einf(v, e) ? xv[v][e] : 0.0f;
+                cv[v][e] = einf(v, e) ? cv[v][e] : 0.0f;
               }
             }
           }
@@ -623,7 +651,7 @@ drot_solve_kernel(const SolveParams P) {
               for (int e = 0; e < VEC; ++e) {
                 const float a = fmaxf(xv[v][e], 0.0f);
                 float y = SLOW ? a / kappa : div_rn_by_fma(a, kappa, kappa_rcp);
-                if constexpr (!FULL) y = ein[v][e] ? y : 0.0f;
+                if constexpr (!FULL) y = einf(v, e) ? y : 0.0f;
                 if constexpr (EV) {
                   xv[v][e] = fmaf(-s, cv[v][e], y);
                   objp = fmaf(y, cv[v][e], objp);
@@ -644,7 +672,7 @@ drot_solve_kernel(const SolveParams P) {
             for (int e = 0; e < VEC; ++e) {
               const float t = fmaf(-s, cv[v][e], (xv[v][e] + f1[v][e]) + f2);
               float y = fmaxf(t, 0.0f);
-              if constexpr (!FULL) y = ein[v][e] ? y : 0.0f;
+              if constexpr (!FULL) y = einf(v, e) ? y : 0.0f;
               xv[v][e] = y;
               nsl = fmaf(y, y, nsl);
             }
@@ -672,12 +700,12 @@ drot_solve_kernel(const SolveParams P) {
 
 #pragma unroll
         for (int v = 0; v < KV; ++v) {
-          if (FULL || vall[v]) {
-            store_vec<VEC>(xcol + row0[v], xv[v]);
-          } else if (vany[v]) {
+          if (FULL || vallf(v)) {
+            store_vec<VEC>(xcol + row0f(v), xv[v]);
+          } else if (vanyf(v)) {
 #pragma unroll
             for (int e = 0; e < VEC; ++e)
-              if (ein[v][e]) xcol[row0[v] + e] = xv[v][e];
+              if (einf(v, e)) xcol[row0f(v) + e] = xv[v][e];
           }
         }
 
@@ -805,32 +833,34 @@ drot_solve_kernel(const SolveParams P) {
     }
     double res = 0.0;
     const bool sm2 = P.p2_smem != 0;
-    reduce_partials(r_lo, r_hi, P.rowpart, P.nr, P.P, [&](int i, float t) {
-      const int li = i - r_lo;
-      const float rs = t - (sm2 ? s_p[li] : __ldg(P.p + i));
-      const float ab = (sm2 ? s_a[li] : P.a[i]) - rs;
-      if (sm2) {
-        s_a[li] = ab;
-        s_t1[li] = ab - rs;
-      } else {
-        P.a[i] = ab;
-        P.phi1[i] = ab - rs;
-      }
-      res = fma((double)rs, (double)rs, res);
-    });
-    reduce_partials(k_lo, k_hi, P.colpart, P.nc, P.nsb, [&](int j, float t) {
-      const int lj = j - k_lo;
-      const float cs = t - (sm2 ? s_q[lj] : __ldg(P.q + j));
-      const float ab = (sm2 ? s_b[lj] : P.b[j]) - cs;
-      if (sm2) {
-        s_b[lj] = ab;
-        s_t2[lj] = ab - cs;
-      } else {
-        P.b[j] = ab;
-        P.phi2[j] = ab - cs;
-      }
-      res = fma((double)cs, (double)cs, res);
-    });
+    reduce_partials(
+        r_lo, r_hi, k_lo, k_hi, P.rowpart, P.colpart, P.nr, P.nc, P.P, P.nsb,
+        [&](int i, float t) {
+          const int li = i - r_lo;
+          const float rs = t - (sm2 ? s_p[li] : __ldg(P.p + i));
+          const float ab = (sm2 ? s_a[li] : P.a[i]) - rs;
+          if (sm2) {
+            s_a[li] = ab;
+            s_t1[li] = ab - rs;
+          } else {
+            P.a[i] = ab;
+            P.phi1[i] = ab - rs;
+          }
+          res = fma((double)rs, (double)rs, res);
+        },
+        [&](int j, float t) {
+          const int lj = j - k_lo;
+          const float cs = t - (sm2 ? s_q[lj] : __ldg(P.q + j));
+          const float ab = (sm2 ? s_b[lj] : P.b[j]) - cs;
+          if (sm2) {
+            s_b[lj] = ab;
+            s_t2[lj] = ab - cs;
+          } else {
+            P.b[j] = ab;
+            P.phi2[j] = ab - cs;
+          }
+          res = fma((double)cs, (double)cs, res);
+        });
     if (check) {
       res = warp_sum_d(res);
       if (lane == 0) dscr[warp] = res;
@@ -884,17 +914,17 @@ drot_solve_kernel(const SolveParams P) {
       const float* ccol = P.c + (long long)j * ld;
 #pragma unroll
       for (int v = 0; v < KV; ++v) {
-        if (!vany[v]) continue;
+        if (!vanyf(v)) continue;
         float xv[VEC], cv[VEC];
-        load_vec<VEC>(xcol + row0[v], xv);
-        load_vec_nc<VEC>(ccol + row0[v], cv);
+        load_vec<VEC>(xcol + row0f(v), xv);
+        load_vec_nc<VEC>(ccol + row0f(v), cv);
 #pragma unroll
         for (int e = 0; e < VEC; ++e) xv[e] = fmaxf(fmaf(s, cv[e], xv[e]), 0.0f);
-        if (vall[v]) store_vec<VEC>(xcol + row0[v], xv);
+        if (vallf(v)) store_vec<VEC>(xcol + row0f(v), xv);
         else {
 #pragma unroll
           for (int e = 0; e < VEC; ++e)
-            if (ein[v][e]) xcol[row0[v] + e] = xv[e];
+            if (einf(v, e)) xcol[row0f(v) + e] = xv[e];
         }
       }
     }
@@ -921,7 +951,7 @@ drot_solve_kernel(const SolveParams P) {
     st->objective = last_obj;
     st->residual = last_res;
     st->sigma = last_sigma;
-    for (int q = 0; q < 4; ++q) st->phase_ns[q] = tacc[q];
+    for (int q = 0; q < 4; ++q) st->phase_ns[q] = s_tacc[q];
     *P.alpha = alpha;
   }
 }
