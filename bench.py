@@ -246,6 +246,7 @@ def hbm_point(dev, flush):
     times = []
     for _ in range(3):
         flush.zero_()
+        torch.cuda._sleep(20_000_000)
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
         x, info, ws = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, iters, 0.0, out=x, workspace=ws)
@@ -330,6 +331,10 @@ def run_gpu(args):
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
+        # A short GPU-side wait ahead of the first timed step: the host
+        # enqueues every step while it runs, so a host stall cannot leave the
+        # GPU idle inside the timed events.
+        torch.cuda._sleep(100_000_000)
         for i in range(args.steps):
             flush.zero_()
             starts[i].record()
