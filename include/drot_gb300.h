@@ -179,6 +179,35 @@ float *drot_gl_wrapper(const float *c, const float *p, const float *q,
 /* Frees a matrix returned by the wrappers. */
 void drot_free_host(float *ptr);
 
+/* ---------------------------------------------------------------------------
+ * Solve without any device allocation
+ * ------------------------------------------------------------------------- */
+
+/* Bytes of the fixed workspace array of drot_quadratic_drot_noalloc.  Every
+ * GPU that loads the library holds this much device memory until exit. */
+#define DROT_NOALLOC_WORKSPACE_BYTES (16u << 20)
+
+/* No counterpart in the reference.  Same solve as drot_quadratic_drot (the
+ * reg_drot.quadratic_drot operator), for callers that may not allocate
+ * device memory when they call it -- e.g. a latency-critical loop, where
+ * cudaMalloc/cudaFree would synchronise the device, or a host whose device
+ * memory belongs to another allocator.  It allocates nothing: its workspace
+ * is a fixed 16 MiB array in the library's device memory (one per GPU),
+ * enough for n_rows x n_cols problems whose drot_quadratic_drot_workspace_bytes
+ * is at most DROT_NOALLOC_WORKSPACE_BYTES (square problems up to about
+ * 35 000); larger problems get DROT_ERR_WORKSPACE and nothing runs.  The
+ * caller passes the inputs c, p, q and the output x (device pointers).
+ * The first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls on a device share the one array:
+ * calls whose work overlaps on the GPU (other streams, other host threads)
+ * race and corrupt each other; serialise them.  Each call re-initialises
+ * everything it reads from the array. */
+int drot_quadratic_drot_noalloc(const float *c, const float *p, const float *q,
+                                int n_rows, int n_cols, float rho, float r_weight,
+                                int max_iters, float eps, float *x,
+                                drot_result *result, drot_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

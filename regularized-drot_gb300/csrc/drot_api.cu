@@ -779,3 +779,66 @@ float* drot_gl_wrapper(const float* c, const float* p, const float* q, int n_row
 void drot_free_host(float* ptr) { free(ptr); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Solve without any device allocation
+// ---------------------------------------------------------------------------
+//
+// Some callers cannot allocate device memory when they call the solver: a
+// latency-critical loop in which cudaMalloc / cudaFree would synchronise the
+// whole device, or a host (a plugin, a caller in another language) whose
+// device memory is owned by a different allocator that it may not bypass.
+// For them drot_quadratic_drot_noalloc keeps the solver's workspace (partial
+// sums, barrier words, result record and the dual state) in a fixed array in
+// the library's own device memory.  Every GPU that loads the library holds
+// this array until the process exits.
+
+namespace drot {
+
+// Workspace of the allocation-free entry point, one per device.
+static __device__ __align__(256) unsigned char g_noalloc_ws[DROT_NOALLOC_WORKSPACE_BYTES];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[64];  // device address of g_noalloc_ws per device ordinal
+
+// The array's name in host code is only a host-side handle; the kernels need
+// its device address, which the runtime gives per device.  Looked up once per
+// device, with that device current.
+static int noalloc_workspace(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return DROT_ERR_CUDA;
+  if (dev < 0 || dev >= 64) return DROT_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_noalloc_ws) != cudaSuccess || !ptr) {
+      cudaGetLastError();
+      return DROT_ERR_CUDA;
+    }
+    g_noalloc_ptr[dev] = ptr;
+  }
+  *out = g_noalloc_ptr[dev];
+  return DROT_OK;
+}
+
+}  // namespace drot
+
+extern "C" int drot_quadratic_drot_noalloc(const float* c, const float* p, const float* q,
+                                           int n_rows, int n_cols, float rho, float r_weight,
+                                           int max_iters, float eps, float* x,
+                                           drot_result* result, drot_stream_t stream) {
+  if (!c || !p || !q || !x || n_rows <= 0 || n_cols <= 0 || max_iters < 0)
+    return DROT_ERR_INVALID_ARG;
+  // Size check first: nothing is launched for a problem that does not fit.
+  const size_t need = drot_quadratic_drot_workspace_bytes(n_rows, n_cols);
+  if (need == 0) return DROT_ERR_UNSUPPORTED;
+  if (need > (size_t)DROT_NOALLOC_WORKSPACE_BYTES) return DROT_ERR_WORKSPACE;
+  void* ws = nullptr;
+  const int rc = noalloc_workspace(&ws);
+  if (rc != DROT_OK) return rc;
+  // drot_quadratic_drot clears the barrier words, writes the warm start into
+  // the dual state and every partial before it is read, so nothing left in
+  // the array by an earlier call is used.
+  return drot_quadratic_drot(c, p, q, n_rows, n_cols, rho, r_weight, max_iters, eps, x, ws,
+                             (size_t)DROT_NOALLOC_WORKSPACE_BYTES, result, stream);
+}

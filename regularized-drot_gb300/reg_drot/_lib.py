@@ -66,6 +66,8 @@ SIGNATURES = {
     "drot_gl_wrapper": (_fp, [_vp, _vp, _vp, _c_int, _c_int, _c_int, _c_float, _c_float,
                               _c_int, _c_float, _fp, _fp, _ip, _fp, _c_int, _c_int]),
     "drot_free_host": (None, [_fp]),
+    "drot_quadratic_drot_noalloc": (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_float, _c_float,
+                                             _c_int, _c_float, _vp, _RP, _vp]),
 }
 
 _lib = None
