@@ -152,6 +152,13 @@ static int tma_warps() {
   return (w >= 4 && w <= 16) ? w : 16;
 }
 
+// Warps per CTA on the register path (DROT_REG_WARPS, 4..16, default 8).
+static int reg_warps() {
+  const char* e = getenv("DROT_REG_WARPS");
+  const int w = e ? atoi(e) : 0;
+  return (w >= 4 && w <= 16) ? w : 8;
+}
+
 // Build the launch plan for one data path (tma: shared-memory TMA ring, else
 // register loads).  Returns a drot_status.
 static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma, Plan& pl) {
@@ -202,7 +209,7 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
   // Warps per CTA: 8 on the register path (two CTAs per SM), up to 16 when
   // a band needs teams of 3 or more warps (fewer CTAs per band keeps the
   // phase-2 partial count down).
-  const int wtarget = tma ? tma_warps() : 8;
+  const int wtarget = tma ? tma_warps() : reg_warps();
   for (int attempt = 0; attempt < 8; ++attempt) {
     const int wcap = (!tma && pl.wt >= 3) ? 16 : wtarget;
     int teams = pl.wt >= wcap ? 1 : std::max(1, wcap / pl.wt);
@@ -317,7 +324,7 @@ static int make_plan(int mode, int nr, int nc, int G, int vec, bool tma, Plan& p
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return DROT_ERR_CUDA;
   const PlanKey key = {dev, mode, nr, nc, mode == MODE_GL ? G : 0, vec, tma ? 1 : 0,
-                       tma ? tma_warps() : 8,
+                       tma ? tma_warps() : reg_warps(),
                        tma && getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1};
   {
     std::lock_guard<std::mutex> lk(g_plan_mu);
