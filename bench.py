@@ -404,7 +404,7 @@ def run_gpu(args):
 
 def run_case(spec):
     """One solve of the headline workload at size n for a fixed iteration count
-    (for profiler captures): --case n:iters[:gl]."""
+    (for profiler captures): --case n:iters[:gl][:bf16]."""
     import torch
     import reg_drot
     parts = spec.split(":")
@@ -412,7 +412,9 @@ def run_case(spec):
     dev = torch.device("cuda", 0)
     c, p, q, _ = make_problem(n)
     cd, pd, qd = (torch.from_numpy(a).to(dev) for a in (c, p, q))
-    if len(parts) > 2 and parts[2] == "gl":
+    if "bf16" in parts[2:]:
+        cd = cd.to(torch.bfloat16)
+    if "gl" in parts[2:]:
         x, info, _ = reg_drot.solve_gl(cd, pd, qd, 2, RHO, ALPHA, iters, 0.0)
     else:
         x, info, _ = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, iters, 0.0)

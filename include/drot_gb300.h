@@ -53,6 +53,13 @@ typedef struct {
                           dual update, second grid barrier + stop test */
 } drot_result;
 
+/* Storage types of the cost matrix C for the *_ex entry points.  Iterates
+ * and sums stay FP32; a BF16-stored C is widened exactly to FP32 in the
+ * kernel, so the solver solves the problem whose cost is the BF16-rounded C
+ * (10 bytes per element on iterations that read C instead of 12). */
+#define DROT_C_F32 0
+#define DROT_C_BF16 1
+
 /* Text for a drot_status code. */
 const char *drot_status_string(int status);
 
@@ -121,6 +128,22 @@ int drot_gl_solve(const float *c, const float *p, const float *q, int n_rows,
                   size_t workspace_bytes, drot_result *result,
                   drot_stream_t stream);
 
+/* drot_qr_solve / drot_gl_solve with the cost matrix stored as c_dtype
+ * (DROT_C_F32 or DROT_C_BF16).  No counterpart in the reference (its C is
+ * float only); the FP32 case is exactly drot_qr_solve / drot_gl_solve. */
+int drot_qr_solve_ex(const void *c, int c_dtype, const float *p, const float *q,
+                     int n_rows, int n_cols, float step_size, float scale,
+                     int max_iters, float eps, float *x, float *a, float *b,
+                     float *phi1, float *phi2, float *alpha, void *workspace,
+                     size_t workspace_bytes, drot_result *result,
+                     drot_stream_t stream);
+int drot_gl_solve_ex(const void *c, int c_dtype, const float *p, const float *q,
+                     int n_rows, int n_cols, int n_groups, float step_size,
+                     float lambda, int max_iters, float eps, float *x, float *a,
+                     float *b, float *phi1, float *phi2, float *alpha,
+                     void *workspace, size_t workspace_bytes, drot_result *result,
+                     drot_stream_t stream);
+
 /* Copy the result block of the last solve that used `workspace` to the host
  * (waits for `stream`). */
 int drot_read_result(const void *workspace, drot_result *result,
@@ -149,6 +172,19 @@ int drot_group_lasso_drot(const float *c, const float *p, const float *q,
                           float r_weight, int max_iters, float eps, float *x,
                           void *workspace, size_t workspace_bytes,
                           drot_result *result, drot_stream_t stream);
+
+/* The operator entry points with the cost stored as c_dtype (DROT_C_F32 or
+ * DROT_C_BF16); no counterpart in the reference. */
+int drot_quadratic_drot_ex(const void *c, int c_dtype, const float *p,
+                           const float *q, int n_rows, int n_cols, float rho,
+                           float r_weight, int max_iters, float eps, float *x,
+                           void *workspace, size_t workspace_bytes,
+                           drot_result *result, drot_stream_t stream);
+int drot_group_lasso_drot_ex(const void *c, int c_dtype, const float *p,
+                             const float *q, int n_rows, int n_cols, int n_class,
+                             float rho, float r_weight, int max_iters, float eps,
+                             float *x, void *workspace, size_t workspace_bytes,
+                             drot_result *result, drot_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * Host-buffer wrappers

@@ -27,39 +27,47 @@ namespace drot {
 
 typedef void (*SolveFn)(const SolveParams);
 
-template <int MODE, bool TMA>
+template <int MODE, bool TMA, typename CT>
 static SolveFn kernel_kv(int vec, int kv) {
   if constexpr (TMA) {
     if (vec != 4) return nullptr;
-    if (kv == 1) return drot_solve_kernel<MODE, 4, 1, true>;
-    if (kv == 2) return drot_solve_kernel<MODE, 4, 2, true>;
-    if (kv == 4) return drot_solve_kernel<MODE, 4, 4, true>;
+    if (kv == 1) return drot_solve_kernel<MODE, 4, 1, true, CT>;
+    if (kv == 2) return drot_solve_kernel<MODE, 4, 2, true, CT>;
+    if (kv == 4) return drot_solve_kernel<MODE, 4, 4, true, CT>;
     if constexpr (MODE == MODE_GL) {
-      if (kv == 8) return drot_solve_kernel<MODE, 4, 8, true>;
+      if (kv == 8) return drot_solve_kernel<MODE, 4, 8, true, CT>;
     }
   } else {
     if (vec == 4) {
-      if (kv == 1) return drot_solve_kernel<MODE, 4, 1, false>;
-      if (kv == 2) return drot_solve_kernel<MODE, 4, 2, false>;
-      if (kv == 4) return drot_solve_kernel<MODE, 4, 4, false>;
+      if (kv == 1) return drot_solve_kernel<MODE, 4, 1, false, CT>;
+      if (kv == 2) return drot_solve_kernel<MODE, 4, 2, false, CT>;
+      if (kv == 4) return drot_solve_kernel<MODE, 4, 4, false, CT>;
       if constexpr (MODE == MODE_GL) {
-        if (kv == 8) return drot_solve_kernel<MODE, 4, 8, false>;
+        if (kv == 8) return drot_solve_kernel<MODE, 4, 8, false, CT>;
       }
     } else {
-      if (kv == 1) return drot_solve_kernel<MODE, 1, 1, false>;
-      if (kv == 2) return drot_solve_kernel<MODE, 1, 2, false>;
-      if (kv == 4) return drot_solve_kernel<MODE, 1, 4, false>;
+      if (kv == 1) return drot_solve_kernel<MODE, 1, 1, false, CT>;
+      if (kv == 2) return drot_solve_kernel<MODE, 1, 2, false, CT>;
+      if (kv == 4) return drot_solve_kernel<MODE, 1, 4, false, CT>;
       if constexpr (MODE == MODE_GL) {
-        if (kv == 8) return drot_solve_kernel<MODE, 1, 8, false>;
+        if (kv == 8) return drot_solve_kernel<MODE, 1, 8, false, CT>;
       }
     }
   }
   return nullptr;
 }
 
-static SolveFn kernel_for(int mode, int vec, int kv, bool tma) {
-  if (mode == MODE_QR) return tma ? kernel_kv<MODE_QR, true>(vec, kv) : kernel_kv<MODE_QR, false>(vec, kv);
-  return tma ? kernel_kv<MODE_GL, true>(vec, kv) : kernel_kv<MODE_GL, false>(vec, kv);
+// Kernel instance for (mode, vector width, vectors per lane, data path, cost
+// type).  The TMA ring exists for float costs only.
+static SolveFn kernel_for(int mode, int vec, int kv, bool tma, int ctype = DROT_C_F32) {
+  if (ctype == DROT_C_BF16) {
+    if (tma) return nullptr;
+    return mode == MODE_QR ? kernel_kv<MODE_QR, false, __nv_bfloat16>(vec, kv)
+                           : kernel_kv<MODE_GL, false, __nv_bfloat16>(vec, kv);
+  }
+  if (mode == MODE_QR)
+    return tma ? kernel_kv<MODE_QR, true, float>(vec, kv) : kernel_kv<MODE_QR, false, float>(vec, kv);
+  return tma ? kernel_kv<MODE_GL, true, float>(vec, kv) : kernel_kv<MODE_GL, false, float>(vec, kv);
 }
 
 // ---------------------------------------------------------------------------
@@ -99,7 +107,7 @@ static inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAl
 //   cta_sum/obj/res  grid doubles each
 struct Plan {
   int mode = 0, vec = 4, kv = 4, wt = 1, threads = 256, nbands = 1, P = 1, grid = 1, nsb = 1;
-  int band_h = 0, ns = 1, p2_smem = 0, p2_cap_r = 0, p2_cap_c = 0;
+  int band_h = 0, ns = 1, p2_smem = 0, p2_cap_r = 0, p2_cap_c = 0, ctype = DROT_C_F32;
   bool tma = false;
   size_t smem = 0;
   std::vector<int> bounds;
@@ -161,7 +169,8 @@ static int reg_warps() {
 
 // Build the launch plan for one data path (tma: shared-memory TMA ring, else
 // register loads).  Returns a drot_status.
-static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma, Plan& pl) {
+static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma, int ctype,
+                              Plan& pl) {
   if (nr <= 0 || nc <= 0) return DROT_ERR_INVALID_ARG;
   if (tma && vec != 4) return DROT_ERR_UNSUPPORTED;
   const DeviceInfo dev = device_info();
@@ -200,8 +209,9 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
     }
   }
   const int S = SV * pl.kv;
-  SolveFn fn = kernel_for(mode, vec, pl.kv, tma);
+  SolveFn fn = kernel_for(mode, vec, pl.kv, tma, ctype);
   if (!fn) return DROT_ERR_UNSUPPORTED;
+  pl.ctype = ctype;
   // TMA ring: DROT_TMA_CTAS (1 or 2) CTAs per SM share the shared memory.
   const int tma_ctas = tma ? std::max(1, std::min(2, getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1)) : 1;
   const size_t budget = (size_t)std::max(dev.smem_optin, 48 * 1024) / tma_ctas - 1024;
@@ -310,28 +320,30 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
 // Plans are cached per (device, mode, shape, path): planning queries the
 // occupancy calculator, which costs microseconds per call.
 struct PlanKey {
-  int dev, mode, nr, nc, G, vec, tma, warps, ctas;
+  int dev, mode, nr, nc, G, vec, tma, warps, ctas, ctype;
   bool operator==(const PlanKey& o) const {
     return dev == o.dev && mode == o.mode && nr == o.nr && nc == o.nc && G == o.G &&
-           vec == o.vec && tma == o.tma && warps == o.warps && ctas == o.ctas;
+           vec == o.vec && tma == o.tma && warps == o.warps && ctas == o.ctas &&
+           ctype == o.ctype;
   }
 };
 
 static std::mutex g_plan_mu;
 static std::vector<std::pair<PlanKey, Plan>> g_plans;
 
-static int make_plan(int mode, int nr, int nc, int G, int vec, bool tma, Plan& pl) {
+static int make_plan(int mode, int nr, int nc, int G, int vec, bool tma, Plan& pl,
+                     int ctype = DROT_C_F32) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return DROT_ERR_CUDA;
   const PlanKey key = {dev, mode, nr, nc, mode == MODE_GL ? G : 0, vec, tma ? 1 : 0,
                        tma ? tma_warps() : reg_warps(),
-                       tma && getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1};
+                       tma && getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1, ctype};
   {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     for (auto& e : g_plans)
       if (e.first == key) { pl = e.second; return DROT_OK; }
   }
-  const int rc = make_plan_uncached(mode, nr, nc, G, vec, tma, pl);
+  const int rc = make_plan_uncached(mode, nr, nc, G, vec, tma, ctype, pl);
   if (rc == DROT_OK) {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     if (g_plans.size() >= 64) g_plans.erase(g_plans.begin());
@@ -354,13 +366,14 @@ static int path_override() {
 // part the fused update is bound by per-warp instruction latency, and two
 // 8-warp CTAs per SM with register-resident segments beat one 16-warp CTA
 // fed by the shared-memory TMA ring.  DROT_PATH=tma selects the ring.
-static int choose_plan(int mode, int nr, int nc, int G, bool aligned4, Plan& pl) {
+static int choose_plan(int mode, int nr, int nc, int G, bool aligned4, Plan& pl,
+                       int ctype = DROT_C_F32) {
   const int ov = path_override();
-  if (ov == 2) {
+  if (ov == 2 && ctype == DROT_C_F32) {
     if (!aligned4) return DROT_ERR_UNSUPPORTED;
     return make_plan(mode, nr, nc, G, 4, true, pl);
   }
-  return make_plan(mode, nr, nc, G, aligned4 ? 4 : 1, false, pl);
+  return make_plan(mode, nr, nc, G, aligned4 ? 4 : 1, false, pl, ctype);
 }
 
 static size_t scratch_bytes(int mode, int nr, int nc, int G) {
@@ -385,7 +398,9 @@ static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
 struct SolveArgs {
   int mode;
-  const float *c, *p, *q;
+  const void* c;
+  int ctype;
+  const float *p, *q;
   int nr, nc, G;
   float s, kappa, lambda;
   int max_iters;
@@ -418,10 +433,12 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
     return DROT_ERR_INVALID_ARG;
   if (A.nr <= 0 || A.nc <= 0 || A.max_iters < 0) return DROT_ERR_INVALID_ARG;
   if (((uintptr_t)A.ws & (kAlign - 1)) != 0) return DROT_ERR_WORKSPACE;
+  if (A.ctype != DROT_C_F32 && A.ctype != DROT_C_BF16) return DROT_ERR_INVALID_ARG;
   const long long ld = A.nr;
-  const bool aligned4 = ld % 4 == 0 && aligned16(A.x) && aligned16(A.c);
+  const bool c_aligned = A.ctype == DROT_C_F32 ? aligned16(A.c) : (((uintptr_t)A.c & 7u) == 0);
+  const bool aligned4 = ld % 4 == 0 && aligned16(A.x) && c_aligned;
   Plan pl;
-  int rc = choose_plan(A.mode, A.nr, A.nc, A.G, aligned4, pl);
+  int rc = choose_plan(A.mode, A.nr, A.nc, A.G, aligned4, pl, A.ctype);
   if (rc != DROT_OK) return rc;
   if (A.ws_bytes < pl.total) return DROT_ERR_WORKSPACE;
 
@@ -457,7 +474,7 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
   prm.timeout_ns = barrier_timeout_ns();
 
   if (cudaMemsetAsync(ws, 0, 512, A.stream) != cudaSuccess) return DROT_ERR_CUDA;
-  SolveFn fn = kernel_for(A.mode, pl.vec, pl.kv, pl.tma);
+  SolveFn fn = kernel_for(A.mode, pl.vec, pl.kv, pl.tma, pl.ctype);
   if (pl.smem > 48 * 1024 &&
       cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)pl.smem) != cudaSuccess)
@@ -587,14 +604,35 @@ size_t drot_gl_workspace_bytes(int n_rows, int n_cols, int n_groups) {
   return scratch_bytes(MODE_GL, n_rows, n_cols, n_groups);
 }
 
+int drot_qr_solve_ex(const void* c, int c_dtype, const float* p, const float* q, int n_rows,
+                     int n_cols, float step_size, float scale, int max_iters, float eps,
+                     float* x, float* a, float* b, float* phi1, float* phi2, float* alpha,
+                     void* workspace, size_t workspace_bytes, drot_result* result,
+                     drot_stream_t stream) {
+  SolveArgs A = {MODE_QR, c, c_dtype, p, q, n_rows, n_cols, 0, step_size, scale, 0.0f,
+                 max_iters, eps, x, a, b, phi1, phi2, alpha, workspace, workspace_bytes,
+                 (cudaStream_t)stream};
+  if (!(scale > 0.0f)) return DROT_ERR_INVALID_ARG;
+  return run_solve(A, result);
+}
+
 int drot_qr_solve(const float* c, const float* p, const float* q, int n_rows, int n_cols,
                   float step_size, float scale, int max_iters, float eps, float* x, float* a,
                   float* b, float* phi1, float* phi2, float* alpha, void* workspace,
                   size_t workspace_bytes, drot_result* result, drot_stream_t stream) {
-  SolveArgs A = {MODE_QR, c, p, q, n_rows, n_cols, 0, step_size, scale, 0.0f, max_iters,
-                 eps, x, a, b, phi1, phi2, alpha, workspace, workspace_bytes,
+  return drot_qr_solve_ex(c, DROT_C_F32, p, q, n_rows, n_cols, step_size, scale, max_iters, eps,
+                          x, a, b, phi1, phi2, alpha, workspace, workspace_bytes, result, stream);
+}
+
+int drot_gl_solve_ex(const void* c, int c_dtype, const float* p, const float* q, int n_rows,
+                     int n_cols, int n_groups, float step_size, float lambda, int max_iters,
+                     float eps, float* x, float* a, float* b, float* phi1, float* phi2,
+                     float* alpha, void* workspace, size_t workspace_bytes, drot_result* result,
+                     drot_stream_t stream) {
+  if (n_groups <= 0) return DROT_ERR_INVALID_ARG;
+  SolveArgs A = {MODE_GL, c, c_dtype, p, q, n_rows, n_cols, n_groups, step_size, 1.0f, lambda,
+                 max_iters, eps, x, a, b, phi1, phi2, alpha, workspace, workspace_bytes,
                  (cudaStream_t)stream};
-  if (!(scale > 0.0f)) return DROT_ERR_INVALID_ARG;
   return run_solve(A, result);
 }
 
@@ -603,11 +641,9 @@ int drot_gl_solve(const float* c, const float* p, const float* q, int n_rows, in
                   float* x, float* a, float* b, float* phi1, float* phi2, float* alpha,
                   void* workspace, size_t workspace_bytes, drot_result* result,
                   drot_stream_t stream) {
-  if (n_groups <= 0) return DROT_ERR_INVALID_ARG;
-  SolveArgs A = {MODE_GL, c, p, q, n_rows, n_cols, n_groups, step_size, 1.0f, lambda,
-                 max_iters, eps, x, a, b, phi1, phi2, alpha, workspace, workspace_bytes,
-                 (cudaStream_t)stream};
-  return run_solve(A, result);
+  return drot_gl_solve_ex(c, DROT_C_F32, p, q, n_rows, n_cols, n_groups, step_size, lambda,
+                          max_iters, eps, x, a, b, phi1, phi2, alpha, workspace, workspace_bytes,
+                          result, stream);
 }
 
 int drot_read_result(const void* workspace, drot_result* result, drot_stream_t stream) {
@@ -627,10 +663,10 @@ size_t drot_group_lasso_drot_workspace_bytes(int n_rows, int n_cols, int n_class
   return state_layout(sc, n_rows, n_cols).total;
 }
 
-int drot_quadratic_drot(const float* c, const float* p, const float* q, int n_rows, int n_cols,
-                        float rho, float r_weight, int max_iters, float eps, float* x,
-                        void* workspace, size_t workspace_bytes, drot_result* result,
-                        drot_stream_t stream) {
+int drot_quadratic_drot_ex(const void* c, int c_dtype, const float* p, const float* q,
+                           int n_rows, int n_cols, float rho, float r_weight, int max_iters,
+                           float eps, float* x, void* workspace, size_t workspace_bytes,
+                           drot_result* result, drot_stream_t stream) {
   if (n_rows <= 0 || n_cols <= 0 || !workspace) return DROT_ERR_INVALID_ARG;
   const size_t sc = scratch_bytes(MODE_QR, n_rows, n_cols, 0);
   if (sc == 0) return DROT_ERR_UNSUPPORTED;
@@ -648,14 +684,22 @@ int drot_quadratic_drot(const float* c, const float* p, const float* q, int n_ro
   int rc = init_state(n_rows, n_cols, s, 1, p, q, x, a, b, phi1, phi2, alpha,
                       (cudaStream_t)stream);
   if (rc != DROT_OK) return rc;
-  return drot_qr_solve(c, p, q, n_rows, n_cols, s, kappa, max_iters, eps, x, a, b, phi1, phi2,
-                       alpha, workspace, sc, result, stream);
+  return drot_qr_solve_ex(c, c_dtype, p, q, n_rows, n_cols, s, kappa, max_iters, eps, x, a, b,
+                          phi1, phi2, alpha, workspace, sc, result, stream);
 }
 
-int drot_group_lasso_drot(const float* c, const float* p, const float* q, int n_rows,
-                          int n_cols, int n_class, float rho, float r_weight, int max_iters,
-                          float eps, float* x, void* workspace, size_t workspace_bytes,
-                          drot_result* result, drot_stream_t stream) {
+int drot_quadratic_drot(const float* c, const float* p, const float* q, int n_rows, int n_cols,
+                        float rho, float r_weight, int max_iters, float eps, float* x,
+                        void* workspace, size_t workspace_bytes, drot_result* result,
+                        drot_stream_t stream) {
+  return drot_quadratic_drot_ex(c, DROT_C_F32, p, q, n_rows, n_cols, rho, r_weight, max_iters,
+                                eps, x, workspace, workspace_bytes, result, stream);
+}
+
+int drot_group_lasso_drot_ex(const void* c, int c_dtype, const float* p, const float* q,
+                             int n_rows, int n_cols, int n_class, float rho, float r_weight,
+                             int max_iters, float eps, float* x, void* workspace,
+                             size_t workspace_bytes, drot_result* result, drot_stream_t stream) {
   if (n_rows <= 0 || n_cols <= 0 || n_class <= 0 || !workspace) return DROT_ERR_INVALID_ARG;
   const size_t sc = scratch_bytes(MODE_GL, n_rows, n_cols, n_class);
   if (sc == 0) return DROT_ERR_UNSUPPORTED;
@@ -671,8 +715,16 @@ int drot_group_lasso_drot(const float* c, const float* p, const float* q, int n_
   int rc = init_state(n_rows, n_cols, s, 1, p, q, x, a, b, phi1, phi2, alpha,
                       (cudaStream_t)stream);
   if (rc != DROT_OK) return rc;
-  return drot_gl_solve(c, p, q, n_rows, n_cols, n_class, s, lambda, max_iters, eps, x, a, b,
-                       phi1, phi2, alpha, workspace, sc, result, stream);
+  return drot_gl_solve_ex(c, c_dtype, p, q, n_rows, n_cols, n_class, s, lambda, max_iters, eps,
+                          x, a, b, phi1, phi2, alpha, workspace, sc, result, stream);
+}
+
+int drot_group_lasso_drot(const float* c, const float* p, const float* q, int n_rows,
+                          int n_cols, int n_class, float rho, float r_weight, int max_iters,
+                          float eps, float* x, void* workspace, size_t workspace_bytes,
+                          drot_result* result, drot_stream_t stream) {
+  return drot_group_lasso_drot_ex(c, DROT_C_F32, p, q, n_rows, n_cols, n_class, rho, r_weight,
+                                  max_iters, eps, x, workspace, workspace_bytes, result, stream);
 }
 
 // Host-buffer wrappers ------------------------------------------------------

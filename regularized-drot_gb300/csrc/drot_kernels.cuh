@@ -38,6 +38,7 @@
 // leaves its loop, and the host reads DROT_ERR_BARRIER_TIMEOUT.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -70,7 +71,7 @@ struct DeviceStats {
 };
 
 struct SolveParams {
-  const float* c;
+  const void* c;       // float or __nv_bfloat16 (the kernel's CT)
   const float* p;
   const float* q;
   float* x;
@@ -294,6 +295,24 @@ __device__ __forceinline__ void load_vec_nc(const float* ptr, float (&v)[VEC]) {
   }
 }
 
+// Cost loads: float, or bfloat16 widened exactly to float (a bf16 value is
+// the top 16 bits of the float with the same value).
+template <int VEC, typename CT>
+__device__ __forceinline__ void load_c(const CT* ptr, float (&v)[VEC]) {
+  if constexpr (std::is_same<CT, float>::value) {
+    load_vec_nc<VEC>(ptr, v);
+  } else if constexpr (VEC == 4) {
+    const uint2 t = __ldg(reinterpret_cast<const uint2*>(ptr));
+    v[0] = __uint_as_float(t.x << 16);
+    v[1] = __uint_as_float(t.x & 0xffff0000u);
+    v[2] = __uint_as_float(t.y << 16);
+    v[3] = __uint_as_float(t.y & 0xffff0000u);
+  } else {
+    const unsigned short t = __ldg(reinterpret_cast<const unsigned short*>(ptr));
+    v[0] = __uint_as_float((unsigned)t << 16);
+  }
+}
+
 template <int VEC>
 __device__ __forceinline__ void store_vec(float* ptr, const float (&v)[VEC]) {
   if constexpr (VEC == 4) {
@@ -367,10 +386,12 @@ __host__ __device__ constexpr size_t solve_smem_bytes(int warps, int wt, int S, 
 // The solve kernel
 // ---------------------------------------------------------------------------
 
-template <int MODE, int VEC, int KV, bool TMA>
+template <int MODE, int VEC, int KV, bool TMA, typename CT = float>
 __global__ void __launch_bounds__(512, 1)
 drot_solve_kernel(const SolveParams P) {
   static_assert(!TMA || VEC == 4, "the TMA path moves 16-byte vectors");
+  static_assert(!TMA || std::is_same<CT, float>::value, "the TMA path streams float costs");
+  const CT* const cbase = reinterpret_cast<const CT*>(P.c);
   constexpr int SV = 32 * VEC;        // rows per vector slot of a warp
   constexpr int S = SV * KV;          // rows per sub-band (one warp)
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -548,19 +569,19 @@ drot_solve_kernel(const SolveParams P) {
         float* dx = wring + (size_t)st * 2 * S;
         mbar_arrive_expect_tx(wbar + st, tx_bytes);
         bulk_g2s(dx, P.x + (long long)jn * ld + seg_lo, seg_bytes, wbar + st);
-        if constexpr (WITH_C) bulk_g2s(dx + S, P.c + (long long)jn * ld + seg_lo, seg_bytes, wbar + st);
+        if constexpr (WITH_C) bulk_g2s(dx + S, cbase + (long long)jn * ld + seg_lo, seg_bytes, wbar + st);
         ++issued;
       };
 
       // Register path: the warp's segment of column j straight into registers.
       auto load_reg = [&](int j, float (&xv)[KV][VEC], float (&cv)[KV][VEC]) {
         const float* xcol = P.x + (long long)j * ld;
-        const float* ccol = P.c + (long long)j * ld;
+        const CT* ccol = cbase + (long long)j * ld;
 #pragma unroll
         for (int v = 0; v < KV; ++v) {
           if (FULL || vanyf(v)) {
             load_vec<VEC>(xcol + row0f(v), xv[v]);
-            if constexpr (WITH_C) load_vec_nc<VEC>(ccol + row0f(v), cv[v]);
+            if constexpr (WITH_C) load_c<VEC, CT>(ccol + row0f(v), cv[v]);
             else {
 #pragma unroll
               for (int e = 0; e < VEC; ++e) cv[v][e] = 0.0f;
@@ -911,13 +932,13 @@ drot_solve_kernel(const SolveParams P) {
     // fix_x (kernel_qr.hpp:469-482): undo the fold of the last even step.
     for (int j = c0 + team; j < c1; j += nteams) {
       float* xcol = P.x + (long long)j * ld;
-      const float* ccol = P.c + (long long)j * ld;
+      const CT* ccol = cbase + (long long)j * ld;
 #pragma unroll
       for (int v = 0; v < KV; ++v) {
         if (!vanyf(v)) continue;
         float xv[VEC], cv[VEC];
         load_vec<VEC>(xcol + row0f(v), xv);
-        load_vec_nc<VEC>(ccol + row0f(v), cv);
+        load_c<VEC, CT>(ccol + row0f(v), cv);
 #pragma unroll
         for (int e = 0; e < VEC; ++e) xv[e] = fmaxf(fmaf(s, cv[e], xv[e]), 0.0f);
         if (vallf(v)) store_vec<VEC>(xcol + row0f(v), xv);

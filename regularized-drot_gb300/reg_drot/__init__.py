@@ -27,13 +27,16 @@ __all__ = ["quadratic_drot", "group_lasso_drot", "solve_qr", "solve_gl", "DrotEr
            "group_bounds", "workspace_bytes"]
 
 
-def _check_input(t, name):
+C_F32, C_BF16 = 0, 1  # DROT_C_F32 / DROT_C_BF16 of drot_gb300.h
+
+
+def _check_input(t, name, allow_bf16=False):
     # CHECK_CUDA / CHECK_CONTIGUOUS of pytorch/src/drot_cuda.cpp:22-24
     if not isinstance(t, torch.Tensor) or not t.is_cuda:
         raise RuntimeError(f"{name} must be a CUDA tensor")
     if not t.is_contiguous():
         raise RuntimeError(f"{name} must be contiguous")
-    if t.dtype != torch.float32:
+    if t.dtype != torch.float32 and not (allow_bf16 and t.dtype == torch.bfloat16):
         raise RuntimeError(f"expected scalar type Float but found {t.dtype} for {name}")
 
 
@@ -75,7 +78,7 @@ def _alloc(kind, c, n_rows, n_cols, n_class, out, workspace):
     ptr = workspace.data_ptr()
     pad = (-ptr) % 256
     if out is None:
-        out = torch.empty_like(c)
+        out = torch.empty(c.shape, dtype=torch.float32, device=c.device)
     else:
         _check_input(out, "out")
         if out.shape != c.shape or out.device != c.device:
@@ -90,16 +93,19 @@ def solve_qr(c, p, q, rho, r_weight, max_iters, eps, *, out=None, workspace=None
     ``info`` is the solve record (n_iter, iters_run, converged, status,
     objective, objective_f64, residual).  With ``sync=False`` the call
     returns right after enqueueing the solve on ``stream`` and ``info`` is
-    None; read the record later with ``read_result(workspace)``.
+    None; read the record later with ``read_result(workspace)``.  ``c`` may
+    be float32 or bfloat16 (BF16-stored cost, FP32 iterates; x is float32).
     """
-    for t, n in ((c, "c"), (p, "p"), (q, "q")):
+    _check_input(c, "c", allow_bf16=True)
+    for t, n in ((p, "p"), (q, "q")):
         _check_input(t, n)
     n_rows, n_cols = _check_shapes(c, p, q)
     x, ws, wptr, wbytes = _alloc("qr", c, n_rows, n_cols, 1, out, workspace)
     res = DrotResult()
     with torch.cuda.device(c.device):
-        rc = lib().drot_quadratic_drot(
-            c.data_ptr(), p.data_ptr(), q.data_ptr(), n_rows, n_cols, float(rho),
+        rc = lib().drot_quadratic_drot_ex(
+            c.data_ptr(), C_BF16 if c.dtype == torch.bfloat16 else C_F32,
+            p.data_ptr(), q.data_ptr(), n_rows, n_cols, float(rho),
             float(r_weight), int(max_iters), float(eps), x.data_ptr(), wptr, wbytes,
             ctypes_byref(res) if sync else None, _stream_handle(c.device, stream))
     check(rc, "quadratic_drot")
@@ -108,8 +114,10 @@ def solve_qr(c, p, q, rho, r_weight, max_iters, eps, *, out=None, workspace=None
 
 def solve_gl(c, p, q, n_class, rho, r_weight, max_iters, eps, *, out=None, workspace=None,
              stream=None, sync=True):
-    """Group-lasso-regularised DROT; returns (x, info, workspace)."""
-    for t, n in ((c, "c"), (p, "p"), (q, "q")):
+    """Group-lasso-regularised DROT; returns (x, info, workspace).  ``c`` may
+    be float32 or bfloat16."""
+    _check_input(c, "c", allow_bf16=True)
+    for t, n in ((p, "p"), (q, "q")):
         _check_input(t, n)
     n_rows, n_cols = _check_shapes(c, p, q)
     if int(n_class) <= 0:
@@ -117,8 +125,9 @@ def solve_gl(c, p, q, n_class, rho, r_weight, max_iters, eps, *, out=None, works
     x, ws, wptr, wbytes = _alloc("gl", c, n_rows, n_cols, int(n_class), out, workspace)
     res = DrotResult()
     with torch.cuda.device(c.device):
-        rc = lib().drot_group_lasso_drot(
-            c.data_ptr(), p.data_ptr(), q.data_ptr(), n_rows, n_cols, int(n_class), float(rho),
+        rc = lib().drot_group_lasso_drot_ex(
+            c.data_ptr(), C_BF16 if c.dtype == torch.bfloat16 else C_F32,
+            p.data_ptr(), q.data_ptr(), n_rows, n_cols, int(n_class), float(rho),
             float(r_weight), int(max_iters), float(eps), x.data_ptr(), wptr, wbytes,
             ctypes_byref(res) if sync else None, _stream_handle(c.device, stream))
     check(rc, "group_lasso_drot")
@@ -137,12 +146,14 @@ def read_result(workspace, stream=None):
 
 def quadratic_drot(c, p, q, rho, r_weight, max_iters, eps):
     """Transport plan of the quadratic-regularised OT problem (reference signature)."""
+    _check_input(c, "c")
     x, _, _ = solve_qr(c, p, q, rho, r_weight, max_iters, eps)
     return x
 
 
 def group_lasso_drot(c, p, q, n_class, rho, r_weight, max_iters, eps):
     """Transport plan of the group-lasso-regularised OT problem (reference signature)."""
+    _check_input(c, "c")
     x, _, _ = solve_gl(c, p, q, n_class, rho, r_weight, max_iters, eps)
     return x
 

@@ -54,6 +54,18 @@ SIGNATURES = {
                                _c_int, _c_float, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _c_size,
                                _RP, _vp]),
     "drot_read_result": (_c_int, [_vp, _RP, _vp]),
+    "drot_qr_solve_ex": (_c_int, [_vp, _c_int, _vp, _vp, _c_int, _c_int, _c_float, _c_float,
+                                  _c_int, _c_float, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _c_size,
+                                  _RP, _vp]),
+    "drot_gl_solve_ex": (_c_int, [_vp, _c_int, _vp, _vp, _c_int, _c_int, _c_int, _c_float,
+                                  _c_float, _c_int, _c_float, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                  _c_size, _RP, _vp]),
+    "drot_quadratic_drot_ex": (_c_int, [_vp, _c_int, _vp, _vp, _c_int, _c_int, _c_float,
+                                        _c_float, _c_int, _c_float, _vp, _vp, _c_size, _RP,
+                                        _vp]),
+    "drot_group_lasso_drot_ex": (_c_int, [_vp, _c_int, _vp, _vp, _c_int, _c_int, _c_int,
+                                          _c_float, _c_float, _c_int, _c_float, _vp, _vp,
+                                          _c_size, _RP, _vp]),
     "drot_quadratic_drot_workspace_bytes": (_c_size, [_c_int, _c_int]),
     "drot_quadratic_drot": (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_float, _c_float, _c_int,
                                      _c_float, _vp, _vp, _c_size, _RP, _vp]),
