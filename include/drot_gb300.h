@@ -244,6 +244,67 @@ int drot_quadratic_drot_noalloc(const float *c, const float *p, const float *q,
                                 int max_iters, float eps, float *x,
                                 drot_result *result, drot_stream_t stream);
 
+/* ---------------------------------------------------------------------------
+ * Batched quadratic-regularised solves
+ *
+ * No counterpart in the reference, whose callers solve many instances one at
+ * a time (core/multiexp_qr.cu:47-49 calls the wrapper once per repetition;
+ * benchmark/utils/compute_w2_dist.py:86 calls reg_drot.quadratic_drot once
+ * per problem).  Here many independent instances of different shapes run in
+ * ONE persistent cooperative launch: per instance the same iteration, warm
+ * start, stop test and n_iter as drot_quadratic_drot, each instance stopping
+ * on its own.
+ *
+ * Flow: drot_batch_plan_create (host, once per set of shapes) ->
+ * drot_batch_upload (copies the plan's descriptors into the workspace, once
+ * per workspace) -> drot_qr_batch_launch (device work only: no allocation,
+ * no host synchronisation, so it can be captured in a CUDA graph and
+ * replayed) -> drot_batch_results.
+ * ------------------------------------------------------------------------- */
+
+/* One instance.  Its C and X are n_rows x n_cols column-major blocks with
+ * leading dimension ld (ld >= n_rows, a multiple of 4), starting at element
+ * c_offset of the batch's C buffer and x_offset of its X buffer (multiples of
+ * 4); X must hold ld * n_cols elements (the rows past n_rows are zeroed).
+ * p and q start at p_offset / q_offset of the batch's p and q buffers.
+ * rho, r_weight, eps as in drot_quadratic_drot. */
+typedef struct {
+  int n_rows, n_cols, ld, pad;
+  long long c_offset, x_offset, p_offset, q_offset;
+  float rho, r_weight, eps, pad2;
+} drot_batch_instance;
+
+/* Per-instance outcome; fields as in drot_result. */
+typedef struct {
+  int n_iter, iters_run, converged, objective_valid;
+  double objective, residual;
+} drot_batch_result;
+
+typedef struct drot_batch_plan_s *drot_batch_plan;
+
+/* Builds the tile list of n_inst instances on the current device: tiles of
+ * 512 rows x cols_per_tile columns (<= 0: 128), plus the launch shape. */
+int drot_batch_plan_create(int n_inst, const drot_batch_instance *inst,
+                           int cols_per_tile, drot_batch_plan *plan);
+void drot_batch_plan_destroy(drot_batch_plan plan);
+/* Workspace bytes of a plan (device memory, 256-byte aligned). */
+size_t drot_batch_plan_workspace_bytes(drot_batch_plan plan);
+/* Number of tiles (work units of one iteration). */
+int drot_batch_plan_tiles(drot_batch_plan plan);
+/* Copies the plan's descriptors into the workspace; synchronises `stream`. */
+int drot_batch_upload(drot_batch_plan plan, void *workspace,
+                      size_t workspace_bytes, drot_stream_t stream);
+/* Warm start + solve of every instance (one init kernel, one cooperative
+ * launch).  c: DROT_C_F32 or DROT_C_BF16 elements.  Asynchronous. */
+int drot_qr_batch_launch(drot_batch_plan plan, const void *c, int c_dtype,
+                         const float *p, const float *q, float *x,
+                         int max_iters, void *workspace, size_t workspace_bytes,
+                         drot_stream_t stream);
+/* Copies the per-instance outcomes to out[n_inst]; synchronises `stream`.
+ * Returns DROT_ERR_BARRIER_TIMEOUT when the launch gave up on a barrier. */
+int drot_batch_results(drot_batch_plan plan, const void *workspace,
+                       drot_batch_result *out, drot_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

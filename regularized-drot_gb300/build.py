@@ -1,7 +1,8 @@
 """Build recipe of the solver library (libdrot_gb300.so) for sm_103a.
 
-One nvcc invocation compiles csrc/drot_api.cu (which includes the kernels)
-into reg_drot/libdrot_gb300.so, in tree.  Device code is compiled with
+nvcc compiles the translation units csrc/drot_api.cu (single-instance
+solver and C ABI) and csrc/drot_batch.cu (batched solver) in parallel and
+links them into reg_drot/libdrot_gb300.so, in tree.  Device code is compiled with
 --fmad=false: the kernels spell out every fused multiply-add they need
 (the ones the reference's kernels compile to), so nothing else is contracted.
 Host code is compiled with -ffp-contract=off so the parameter mapping rounds
@@ -18,7 +19,7 @@ REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 OUT = os.path.join(PKG, "reg_drot", "libdrot_gb300.so")
-SOURCES = [os.path.join(CSRC, "drot_api.cu")]
+SOURCES = [os.path.join(CSRC, "drot_api.cu"), os.path.join(CSRC, "drot_batch.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))] + \
     [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
 
@@ -26,7 +27,6 @@ NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-lineinfo", "-O3", "-std=c++17", "--fmad=false",
     "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
-    "-shared",
 ]
 
 
@@ -41,10 +41,23 @@ def build(force=False, verbose=False, extra=()):
     newest = max(os.path.getmtime(f) for f in DEPS)
     if not force and os.path.exists(OUT) and os.path.getmtime(OUT) >= newest:
         return OUT
-    cmd = [nvcc(), *NVCC_FLAGS, *extra, "-I", INCLUDE, "-I", CSRC, "-o", OUT + ".tmp", *SOURCES]
+    objs, procs = [], []
+    for src in SOURCES:
+        obj = os.path.join(os.path.dirname(OUT), os.path.basename(src) + ".o")
+        cmd = [nvcc(), *NVCC_FLAGS, *extra, "-I", INCLUDE, "-I", CSRC, "-c", "-o", obj, src]
+        if verbose:
+            print(" ".join(cmd), flush=True)
+        procs.append((subprocess.Popen(cmd), cmd))
+        objs.append(obj)
+    for proc, cmd in procs:
+        if proc.wait() != 0:
+            raise subprocess.CalledProcessError(proc.returncode, cmd)
+    cmd = [nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-o", OUT + ".tmp", *objs]
     if verbose:
         print(" ".join(cmd), flush=True)
     subprocess.check_call(cmd)
+    for obj in objs:
+        os.remove(obj)
     os.replace(OUT + ".tmp", OUT)
     return OUT
 

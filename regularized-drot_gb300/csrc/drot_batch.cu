@@ -1,0 +1,658 @@
+// drot_batch.cu -- batched quadratic-regularised DROT: many independent
+// instances of uneven shape solved in one persistent cooperative launch.
+//
+// Work units are tiles (instance, row band, column chunk).  In the fused
+// update every CTA takes tiles from a per-iteration atomic counter until the
+// list is exhausted (instances of very different sizes balance out), and
+// every tile writes its own partial-sum slots, so the sums do not depend on
+// which CTA ran which tile (results are deterministic).  The dual update,
+// the stop test and the bookkeeping of an instance belong to one CTA
+// (instance k -> CTA k mod grid).  Converged instances drop out of the tile
+// list; the launch ends when every instance has converged or max_iters is
+// reached.  Per instance the iteration map, fold, stop rule and counts are
+// those of the single-instance solver (core/drot_qr.hpp:159-234).
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <type_traits>
+#include <vector>
+
+#include "drot_gb300.h"
+#include "drot_kernels.cuh"
+
+namespace drot {
+
+struct BatchInst {
+  long long c_off, x_off, p_off, q_off;  // element offsets into the caller's buffers
+  long long ld;                          // leading dimension of its C and X
+  long long rp_off;                      // row partials [P][nr] (floats)
+  long long cp_off;                      // column partials [nbands][nc] (floats)
+  int nr, nc;
+  int nbands, band_h, P;
+  int tile0, ntiles;
+  int row_off, col_off;                  // its rows / columns in the packed state arrays
+  float s, kappa, kappa_rcp, eps, nc_rcp, nr_rcp;
+  float w_phi1, w_phi2, w_a, w_b, w_alpha;  // warm-start constants
+  int pad;
+};
+
+struct BatchTile {
+  int inst, band, chunk, lo, hi, c0, c1, pad;
+};
+
+struct BatchStat {
+  int n_iter, iters_run, converged, objective_valid;
+  double objective, residual;
+};
+
+struct BatchParams {
+  const void* c;
+  const float* p;
+  const float* q;
+  float* x;
+  const BatchInst* inst;
+  const BatchTile* tiles;
+  int n_inst, n_tiles, max_iters, pad;
+  float *a, *b, *phi1, *phi2, *alpha;  // packed state
+  float *rowpart, *colpart;
+  double *tile_sum, *tile_obj;
+  int* conv;
+  BatchStat* stats;
+  unsigned* counters;  // [0], [1]: tile counters of even / odd iterations; [2]: converged count
+  unsigned* bar;
+  int* abort_flag;
+  long long timeout_ns;
+};
+
+constexpr int kBatchKV = 4;
+constexpr int kBatchS = 32 * 4 * kBatchKV;  // rows per band (one warp covers a band)
+
+// Warm start of every instance (core/drot_qr.hpp:321-346): X = 0 over its
+// ld x nc block, constant phi1, phi2, a, b, alpha.
+__global__ void batch_init_kernel(const BatchParams P) {
+  const int k = blockIdx.y;
+  if (k >= P.n_inst) return;
+  const BatchInst I = P.inst[k];
+  const long long nx = I.ld * I.nc;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nx;
+       t += (long long)gridDim.x * blockDim.x)
+    P.x[I.x_off + t] = 0.0f;
+  if (blockIdx.x == 0) {
+    for (int i = threadIdx.x; i < I.nr; i += blockDim.x) {
+      P.a[I.row_off + i] = I.w_a;
+      P.phi1[I.row_off + i] = I.w_phi1;
+    }
+    for (int j = threadIdx.x; j < I.nc; j += blockDim.x) {
+      P.b[I.col_off + j] = I.w_b;
+      P.phi2[I.col_off + j] = I.w_phi2;
+    }
+    if (threadIdx.x == 0) {
+      P.alpha[k] = I.w_alpha;
+      P.conv[k] = 0;
+      BatchStat st = {0, 0, 0, 0, 0.0, -1.0};
+      P.stats[k] = st;
+    }
+  }
+}
+
+template <typename CT>
+__global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P) {
+  constexpr int VEC = 4, KV = kBatchKV, SV = 128, S = kBatchS;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int W = blockDim.x >> 5;
+  float* red = reinterpret_cast<float*>(smem_raw);  // [W][S]
+  float* f1s = red + (size_t)W * S;                 // [S]
+  double* dscr = reinterpret_cast<double*>(f1s + S);  // [W + 1]
+  double* oscr = dscr + W + 1;                        // [W]
+  __shared__ int s_flag, s_tile;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int G = gridDim.x;
+  const CT* const cbase = reinterpret_cast<const CT*>(P.c);
+  unsigned epoch = 0;
+  bool aborted = false;
+  int it = 0;
+
+  for (; it < P.max_iters; ++it) {
+    const bool even = (it & 1) == 0;
+    unsigned* counter = P.counters + (it & 1);
+
+    // ---------------------------------------------------------- fused update
+    for (;;) {
+      __syncthreads();
+      if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
+      __syncthreads();
+      const int t = s_tile;
+      if (t >= P.n_tiles) break;
+      const BatchTile T = P.tiles[t];
+      if (__ldcg(P.conv + T.inst)) continue;
+      const BatchInst I = P.inst[T.inst];
+      const int lo = T.lo, hi = T.hi;
+      for (int idx = threadIdx.x; idx < S; idx += blockDim.x) {
+        const int r = lo + idx;
+        f1s[idx] = r < hi ? __ldcg(P.phi1 + I.row_off + r) : 0.0f;
+      }
+      __syncthreads();
+      const int lrow = lo + lane * VEC;
+      float acc[KV][VEC];
+#pragma unroll
+      for (int v = 0; v < KV; ++v)
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) acc[v][e] = 0.0f;
+      float ms_hi = 0.0f, ms_lo = 0.0f, ob_hi = 0.0f, ob_lo = 0.0f;
+      const float s = I.s, kappa = I.kappa, krcp = I.kappa_rcp;
+      // The column loop of one tile; EV: even iteration (reads C, stores the
+      // folded X - sC), else odd (reads X only).  Same arithmetic as the
+      // single-instance kernel.
+      auto tile_columns = [&](auto even_tag) {
+        constexpr bool EV = decltype(even_tag)::value;
+        for (int j = T.c0 + warp; j < T.c1; j += W) {
+          float* xcol = P.x + I.x_off + (long long)j * I.ld;
+          const CT* ccol = cbase + I.c_off + (long long)j * I.ld;
+          const float f2 = __ldcg(P.phi2 + I.col_off + j);
+          float xv[KV][VEC], cv[KV][VEC];
+#pragma unroll
+          for (int v = 0; v < KV; ++v) {
+            const int r = lrow + v * SV;
+            if (r < hi) {
+              load_vec<VEC>(xcol + r, xv[v]);
+              if constexpr (EV) load_c<VEC, CT>(ccol + r, cv[v]);
+              else {
+#pragma unroll
+                for (int e = 0; e < VEC; ++e) cv[v][e] = 0.0f;
+              }
+              if (r + VEC > hi) {
+                // Rows between n_rows and ld belong to the caller: zero them
+                // so that they add exact zeros.
+#pragma unroll
+                for (int e = 0; e < VEC; ++e)
+                  if (r + e >= hi) { xv[v][e] = 0.0f; cv[v][e] = 0.0f; }
+              }
+            } else {
+#pragma unroll
+              for (int e = 0; e < VEC; ++e) { xv[v][e] = 0.0f; cv[v][e] = 0.0f; }
+            }
+          }
+          unsigned tmin = 0xffffffffu;
+#pragma unroll
+          for (int v = 0; v < KV; ++v) {
+            const float4 f1 = *reinterpret_cast<const float4*>(f1s + v * SV + lane * VEC);
+            const float f1a[VEC] = {f1.x, f1.y, f1.z, f1.w};
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) {
+              float tt = (xv[v][e] + f1a[e]) + f2;
+              if constexpr (EV) tt = fmaf(-s, cv[v][e], tt);
+              xv[v][e] = tt;
+              tmin = min(tmin, (unsigned)__float_as_int(tt) - 1u);
+            }
+          }
+          const bool slow = __any_sync(0xffffffffu, tmin < kDivTinyBitsM1);
+          float colp = 0.0f, objp = 0.0f;
+          auto body = [&](auto slow_tag) {
+            constexpr bool SLOW = decltype(slow_tag)::value;
+#pragma unroll
+            for (int v = 0; v < KV; ++v)
+#pragma unroll
+              for (int e = 0; e < VEC; ++e) {
+                const float a0 = fmaxf(xv[v][e], 0.0f);
+                float y = SLOW ? a0 / kappa : div_rn_by_fma(a0, kappa, krcp);
+                y = (lrow + v * SV + e < hi) ? y : 0.0f;
+                if constexpr (EV) {
+                  xv[v][e] = fmaf(-s, cv[v][e], y);
+                  objp = fmaf(y, cv[v][e], objp);
+                } else {
+                  xv[v][e] = y;
+                }
+                acc[v][e] += y;
+                colp += y;
+              }
+          };
+          if (slow) body(std::true_type());
+          else body(std::false_type());
+#pragma unroll
+          for (int v = 0; v < KV; ++v) {
+            const int r = lrow + v * SV;
+            if (r + VEC <= hi) {
+              store_vec<VEC>(xcol + r, xv[v]);
+            } else if (r < hi) {
+#pragma unroll
+              for (int e = 0; e < VEC; ++e)
+                if (r + e < hi) xcol[r + e] = xv[v][e];
+            }
+          }
+          float e1;
+          two_sum(ms_hi, colp, ms_hi, e1);
+          ms_lo += e1;
+          if constexpr (EV) {
+            two_sum(ob_hi, objp, ob_hi, e1);
+            ob_lo += e1;
+          }
+          colp = warp_sum(colp);
+          if (lane == 0) P.colpart[I.cp_off + (long long)T.band * I.nc + j] = colp;
+        }
+      };
+      if (even) tile_columns(std::true_type());
+      else tile_columns(std::false_type());
+      // Tile partials: rows (fixed warp order), mass and objective (FP64).
+      const double wsum = warp_sum_d((double)ms_hi + (double)ms_lo);
+      const double wobj = even ? warp_sum_d((double)ob_hi + (double)ob_lo) : 0.0;
+#pragma unroll
+      for (int v = 0; v < KV; ++v)
+        *reinterpret_cast<float4*>(red + (size_t)warp * S + v * SV + lane * VEC) =
+            make_float4(acc[v][0], acc[v][1], acc[v][2], acc[v][3]);
+      if (lane == 0) {
+        dscr[warp] = wsum;
+        oscr[warp] = wobj;
+      }
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < S; idx += blockDim.x) {
+        const int r = lo + idx;
+        if (r < hi) {
+          float tsum = 0.0f;
+          for (int w = 0; w < W; ++w) tsum += red[(size_t)w * S + idx];
+          P.rowpart[I.rp_off + (long long)T.chunk * I.nr + r] = tsum;
+        }
+      }
+      if (warp == 0) {
+        double a1 = lane < W ? dscr[lane] : 0.0;
+        double a2 = lane < W ? oscr[lane] : 0.0;
+        a1 = warp_sum_d(a1);
+        a2 = warp_sum_d(a2);
+        if (lane == 0) {
+          P.tile_sum[t] = a1;
+          if (even) P.tile_obj[t] = a2;
+        }
+      }
+    }
+
+    if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag)) {
+      aborted = true;
+      break;
+    }
+
+    // ---------------------------------------------------------- dual update
+    if (blockIdx.x == 0 && threadIdx.x == 0) P.counters[(it + 1) & 1] = 0u;
+    for (int k = blockIdx.x; k < P.n_inst; k += G) {
+      if (__ldcg(P.conv + k)) continue;
+      const BatchInst I = P.inst[k];
+      double sg = 0.0, og = 0.0;
+      for (int i = threadIdx.x; i < I.ntiles; i += blockDim.x) {
+        sg += __ldcg(P.tile_sum + I.tile0 + i);
+        if (even) og += __ldcg(P.tile_obj + I.tile0 + i);
+      }
+      sg = block_sum_d(sg, dscr);
+      if (even) og = block_sum_d(og, dscr);
+      const float sigma = (float)sg;
+      const float alpha = P.alpha[k];
+      const float gamma =
+          (float)((2.0 * ((double)sigma - 1.0) - (double)alpha) / (double)(I.nr + I.nc));
+      __syncthreads();
+      if (threadIdx.x == 0) P.alpha[k] = (float)(((double)alpha + 1.0) - (double)sigma);
+      double res = 0.0;
+      const float ncf = (float)I.nc, nrf = (float)I.nr;
+      for (int i = threadIdx.x; i < I.nr; i += blockDim.x) {
+        const float* rp = P.rowpart + I.rp_off + i;
+        float r = 0.0f;
+#pragma unroll 8
+        for (int c = 0; c < I.P; ++c) r += __ldcg(rp + (long long)c * I.nr);
+        const float rs = r - __ldg(P.p + I.p_off + i);
+        const float ab = P.a[I.row_off + i] - rs;
+        P.phi1[I.row_off + i] = div_rn_by((ab - rs) + gamma, ncf, I.nc_rcp);
+        P.a[I.row_off + i] = ab;
+        res = fma((double)rs, (double)rs, res);
+      }
+      for (int j = threadIdx.x; j < I.nc; j += blockDim.x) {
+        const float* cp = P.colpart + I.cp_off + j;
+        float cs_ = 0.0f;
+#pragma unroll 4
+        for (int bnd = 0; bnd < I.nbands; ++bnd) cs_ += __ldcg(cp + (long long)bnd * I.nc);
+        const float cs = cs_ - __ldg(P.q + I.q_off + j);
+        const float ab = P.b[I.col_off + j] - cs;
+        P.phi2[I.col_off + j] = div_rn_by((ab - cs) + gamma, nrf, I.nr_rcp);
+        P.b[I.col_off + j] = ab;
+        res = fma((double)cs, (double)cs, res);
+      }
+      res = block_sum_d(res, dscr);
+      if (threadIdx.x == 0) {
+        BatchStat st = P.stats[k];
+        if (even) {
+          st.objective = og;
+          st.objective_valid = 1;
+          st.residual = sqrt(res);
+          if (st.residual < (double)I.eps) {
+            // Converged at iteration it: the instance keeps its folded X
+            // until the unfold pass at the end of the launch.
+            st.converged = 1;
+            st.n_iter = it + 1;
+            st.iters_run = it + 1;
+            P.conv[k] = 1;
+            atomicAdd(P.counters + 2, 1u);
+          }
+        }
+        P.stats[k] = st;
+      }
+      __syncthreads();
+    }
+
+    if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag)) {
+      aborted = true;
+      break;
+    }
+    if (__ldcg(P.counters + 2) >= (unsigned)P.n_inst) {
+      ++it;
+      break;
+    }
+  }
+
+  // ------------------------------------------------------------ epilogue
+  // Unfold the X of converged instances (fix_x, kernel_qr.hpp:469-482);
+  // static tile assignment (the last barrier ordered every earlier write).
+  if (!aborted) {
+    for (int t = blockIdx.x; t < P.n_tiles; t += G) {
+      const BatchTile T = P.tiles[t];
+      if (!__ldcg(P.conv + T.inst)) continue;
+      const BatchInst I = P.inst[T.inst];
+      for (int j = T.c0 + warp; j < T.c1; j += W) {
+        float* xcol = P.x + I.x_off + (long long)j * I.ld;
+        const CT* ccol = cbase + I.c_off + (long long)j * I.ld;
+#pragma unroll
+        for (int v = 0; v < KV; ++v) {
+          const int r = T.lo + lane * VEC + v * SV;
+          if (r >= T.hi) continue;
+          float xv[VEC], cv[VEC];
+          load_vec<VEC>(xcol + r, xv);
+          load_c<VEC, CT>(ccol + r, cv);
+#pragma unroll
+          for (int e = 0; e < VEC; ++e) xv[e] = fmaxf(fmaf(I.s, cv[e], xv[e]), 0.0f);
+          if (r + VEC <= T.hi) store_vec<VEC>(xcol + r, xv);
+          else {
+#pragma unroll
+            for (int e = 0; e < VEC; ++e)
+              if (r + e < T.hi) xcol[r + e] = xv[e];
+          }
+        }
+      }
+    }
+  }
+  for (int k = blockIdx.x; k < P.n_inst; k += G) {
+    if (threadIdx.x == 0) {
+      BatchStat st = P.stats[k];
+      if (!st.converged) {
+        st.n_iter = P.max_iters + 1;  // drot_qr.hpp:233 without convergence
+        st.iters_run = aborted ? it : P.max_iters;
+      }
+      P.stats[k] = st;
+    }
+  }
+  if (aborted && blockIdx.x == 0 && threadIdx.x == 0) atomicExch(P.abort_flag, 1);
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+static const size_t kAl = 256;
+static inline size_t al(size_t v) { return (v + kAl - 1) / kAl * kAl; }
+
+struct BatchPlanImpl {
+  int n_inst = 0, n_tiles = 0, grid = 0, threads = 256, cols_per_tile = 0;
+  size_t smem = 0;
+  long long rows = 0, cols = 0, rowpart = 0, colpart = 0;
+  std::vector<BatchInst> inst;
+  std::vector<BatchTile> tiles;
+  // workspace layout
+  size_t off_ctrl = 0, off_inst = 0, off_tiles = 0, off_a = 0, off_b = 0, off_phi1 = 0,
+         off_phi2 = 0, off_alpha = 0, off_rp = 0, off_cp = 0, off_tsum = 0, off_tobj = 0,
+         off_conv = 0, off_stats = 0, total = 0;
+  bool uploaded_any = false;
+};
+
+static size_t batch_smem(int warps) {
+  return sizeof(float) * ((size_t)warps * kBatchS + kBatchS) + sizeof(double) * (2 * warps + 1);
+}
+
+}  // namespace drot
+
+using namespace drot;
+
+struct drot_batch_plan_s {
+  BatchPlanImpl p;
+};
+
+extern "C" {
+
+int drot_batch_plan_create(int n_inst, const drot_batch_instance* desc, int cols_per_tile,
+                           drot_batch_plan* out) {
+  if (!out || n_inst <= 0 || n_inst > 65535 || !desc) return DROT_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (cols_per_tile <= 0) cols_per_tile = 128;
+  BatchPlanImpl P;
+  P.n_inst = n_inst;
+  P.cols_per_tile = cols_per_tile;
+  P.inst.resize(n_inst);
+  long long rows = 0, cols = 0, rp = 0, cpp = 0;
+  for (int k = 0; k < n_inst; ++k) {
+    const drot_batch_instance& d = desc[k];
+    if (d.n_rows <= 0 || d.n_cols <= 0 || d.ld < d.n_rows || (d.ld & 3) != 0 ||
+        (long long)d.ld * d.n_cols > (1LL << 40) ||
+        (d.c_offset & 3) != 0 || (d.x_offset & 3) != 0 || d.c_offset < 0 || d.x_offset < 0 ||
+        d.p_offset < 0 || d.q_offset < 0 || !(d.rho > 0.0f) || !(d.r_weight >= 0.0f))
+      return DROT_ERR_INVALID_ARG;
+    BatchInst I;
+    memset(&I, 0, sizeof(I));
+    I.nr = d.n_rows;
+    I.nc = d.n_cols;
+    I.ld = d.ld;
+    I.c_off = d.c_offset;
+    I.x_off = d.x_offset;
+    I.p_off = d.p_offset;
+    I.q_off = d.q_offset;
+    I.nbands = (d.n_rows + kBatchS - 1) / kBatchS;
+    I.band_h = (((d.n_rows + I.nbands - 1) / I.nbands) + 3) & ~3;
+    I.nbands = (d.n_rows + I.band_h - 1) / I.band_h;
+    I.P = (d.n_cols + cols_per_tile - 1) / cols_per_tile;
+    I.tile0 = (int)P.tiles.size();
+    for (int b = 0; b < I.nbands; ++b)
+      for (int c = 0; c < I.P; ++c) {
+        BatchTile T;
+        T.inst = k;
+        T.band = b;
+        T.chunk = c;
+        T.lo = b * I.band_h;
+        T.hi = std::min(T.lo + I.band_h, d.n_rows);
+        T.c0 = (int)(((long long)d.n_cols * c) / I.P);
+        T.c1 = (int)(((long long)d.n_cols * (c + 1)) / I.P);
+        T.pad = 0;
+        P.tiles.push_back(T);
+      }
+    I.ntiles = (int)P.tiles.size() - I.tile0;
+    I.row_off = (int)rows;
+    I.col_off = (int)cols;
+    I.rp_off = rp;
+    I.cp_off = cpp;
+    rows += d.n_rows;
+    cols += d.n_cols;
+    rp += (long long)I.P * d.n_rows;
+    cpp += (long long)I.nbands * d.n_cols;
+    // Operator parameters (pytorch/src/qr_drot_cuda_kernel.cu:100-102) and
+    // the warm start (core/drot_qr.hpp:321-331), in float as the reference.
+    const float s = d.rho / ((float)d.n_rows + (float)d.n_cols);
+    float t = s * d.r_weight;
+    t = t * (float)(d.n_rows + d.n_cols);
+    I.s = s;
+    I.kappa = 1.0f + t;
+    I.kappa_rcp = (float)(1.0 / (double)I.kappa);
+    I.eps = d.eps;
+    I.nc_rcp = (float)(1.0 / (double)(float)d.n_cols);
+    I.nr_rcp = (float)(1.0 / (double)(float)d.n_rows);
+    const float n = (float)d.n_rows, m = (float)d.n_cols;
+    float kk = 1.0f * s;
+    kk = kk * n;
+    kk = kk * m;
+    kk = kk - 2.0f;
+    float tt = (kk + 2.0f) / n;
+    I.w_phi1 = tt / (m + n);
+    tt = (kk + 2.0f) / m;
+    I.w_phi2 = tt / (m + n);
+    I.w_a = (kk + 1.0f) / n;
+    I.w_b = (kk + 1.0f) / m;
+    I.w_alpha = kk + 1.0f;
+    P.inst[k] = I;
+  }
+  P.n_tiles = (int)P.tiles.size();
+  P.rows = rows;
+  P.cols = cols;
+  P.rowpart = rp;
+  P.colpart = cpp;
+  if (rows > INT32_MAX || cols > INT32_MAX) return DROT_ERR_UNSUPPORTED;
+
+  int dev = 0, sms = 0, coop = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
+    return DROT_ERR_CUDA;
+  P.threads = 256;
+  P.smem = batch_smem(P.threads / 32);
+  int occ_f = 0, occ_b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, (const void*)batch_solve_kernel<float>,
+                                                    P.threads, P.smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &occ_b, (const void*)batch_solve_kernel<__nv_bfloat16>, P.threads, P.smem) !=
+          cudaSuccess)
+    return DROT_ERR_CUDA;
+  const int occ = std::min(occ_f, occ_b);
+  if (occ <= 0) return DROT_ERR_CUDA;
+  P.grid = occ * sms;
+
+  size_t off = 0;
+  P.off_ctrl = off;  off = al(off + 512);
+  P.off_inst = off;  off = al(off + sizeof(BatchInst) * n_inst);
+  P.off_tiles = off; off = al(off + sizeof(BatchTile) * P.n_tiles);
+  P.off_a = off;     off = al(off + sizeof(float) * rows);
+  P.off_phi1 = off;  off = al(off + sizeof(float) * rows);
+  P.off_b = off;     off = al(off + sizeof(float) * cols);
+  P.off_phi2 = off;  off = al(off + sizeof(float) * cols);
+  P.off_alpha = off; off = al(off + sizeof(float) * n_inst);
+  P.off_rp = off;    off = al(off + sizeof(float) * rp);
+  P.off_cp = off;    off = al(off + sizeof(float) * cpp);
+  P.off_tsum = off;  off = al(off + sizeof(double) * P.n_tiles);
+  P.off_tobj = off;  off = al(off + sizeof(double) * P.n_tiles);
+  P.off_conv = off;  off = al(off + sizeof(int) * n_inst);
+  P.off_stats = off; off = al(off + sizeof(BatchStat) * n_inst);
+  P.total = off;
+
+  drot_batch_plan h = new (std::nothrow) drot_batch_plan_s;
+  if (!h) return DROT_ERR_CUDA;
+  h->p = std::move(P);
+  *out = h;
+  return DROT_OK;
+}
+
+void drot_batch_plan_destroy(drot_batch_plan plan) { delete plan; }
+
+size_t drot_batch_plan_workspace_bytes(drot_batch_plan plan) {
+  return plan ? plan->p.total : 0;
+}
+
+int drot_batch_plan_tiles(drot_batch_plan plan) { return plan ? plan->p.n_tiles : 0; }
+
+int drot_batch_upload(drot_batch_plan plan, void* workspace, size_t workspace_bytes,
+                      drot_stream_t stream) {
+  if (!plan || !workspace) return DROT_ERR_INVALID_ARG;
+  const BatchPlanImpl& P = plan->p;
+  if (workspace_bytes < P.total || ((uintptr_t)workspace & 255u)) return DROT_ERR_WORKSPACE;
+  char* ws = (char*)workspace;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(ws + P.off_inst, P.inst.data(), sizeof(BatchInst) * P.n_inst,
+                      cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(ws + P.off_tiles, P.tiles.data(), sizeof(BatchTile) * P.n_tiles,
+                      cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return DROT_ERR_CUDA;
+  return DROT_OK;
+}
+
+int drot_qr_batch_launch(drot_batch_plan plan, const void* c, int c_dtype, const float* p,
+                         const float* q, float* x, int max_iters, void* workspace,
+                         size_t workspace_bytes, drot_stream_t stream) {
+  if (!plan || !c || !p || !q || !x || !workspace || max_iters < 0) return DROT_ERR_INVALID_ARG;
+  if (c_dtype != DROT_C_F32 && c_dtype != DROT_C_BF16) return DROT_ERR_INVALID_ARG;
+  const BatchPlanImpl& P = plan->p;
+  if (workspace_bytes < P.total || ((uintptr_t)workspace & 255u)) return DROT_ERR_WORKSPACE;
+  if (((uintptr_t)x & 15u) || ((uintptr_t)c & (c_dtype == DROT_C_F32 ? 15u : 7u)))
+    return DROT_ERR_INVALID_ARG;
+  char* ws = (char*)workspace;
+  cudaStream_t st = (cudaStream_t)stream;
+  BatchParams B;
+  memset(&B, 0, sizeof(B));
+  B.c = c;
+  B.p = p;
+  B.q = q;
+  B.x = x;
+  B.inst = (const BatchInst*)(ws + P.off_inst);
+  B.tiles = (const BatchTile*)(ws + P.off_tiles);
+  B.n_inst = P.n_inst;
+  B.n_tiles = P.n_tiles;
+  B.max_iters = max_iters;
+  B.a = (float*)(ws + P.off_a);
+  B.b = (float*)(ws + P.off_b);
+  B.phi1 = (float*)(ws + P.off_phi1);
+  B.phi2 = (float*)(ws + P.off_phi2);
+  B.alpha = (float*)(ws + P.off_alpha);
+  B.rowpart = (float*)(ws + P.off_rp);
+  B.colpart = (float*)(ws + P.off_cp);
+  B.tile_sum = (double*)(ws + P.off_tsum);
+  B.tile_obj = (double*)(ws + P.off_tobj);
+  B.conv = (int*)(ws + P.off_conv);
+  B.stats = (BatchStat*)(ws + P.off_stats);
+  B.counters = (unsigned*)(ws + P.off_ctrl);
+  B.bar = (unsigned*)(ws + P.off_ctrl + 64);
+  B.abort_flag = (int*)(ws + P.off_ctrl + 128);
+  const char* e = getenv("DROT_BARRIER_TIMEOUT_MS");
+  const long long ms = (e && atoll(e) > 0) ? atoll(e) : 10000LL;
+  B.timeout_ns = ms * 1000000LL;
+  if (cudaMemsetAsync(ws + P.off_ctrl, 0, 512, st) != cudaSuccess) return DROT_ERR_CUDA;
+  batch_init_kernel<<<dim3(64, P.n_inst), 256, 0, st>>>(B);
+  if (cudaGetLastError() != cudaSuccess) return DROT_ERR_CUDA;
+  const void* fn = c_dtype == DROT_C_F32 ? (const void*)batch_solve_kernel<float>
+                                         : (const void*)batch_solve_kernel<__nv_bfloat16>;
+  void* args[] = {(void*)&B};
+  if (cudaLaunchCooperativeKernel(fn, dim3(P.grid), dim3(P.threads), args, P.smem, st) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return DROT_ERR_CUDA;
+  }
+  return DROT_OK;
+}
+
+int drot_batch_results(drot_batch_plan plan, const void* workspace, drot_batch_result* out,
+                       drot_stream_t stream) {
+  if (!plan || !workspace || !out) return DROT_ERR_INVALID_ARG;
+  const BatchPlanImpl& P = plan->p;
+  const char* ws = (const char*)workspace;
+  std::vector<BatchStat> st(P.n_inst);
+  int abort_flag = 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(st.data(), ws + P.off_stats, sizeof(BatchStat) * P.n_inst,
+                      cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaMemcpyAsync(&abort_flag, ws + P.off_ctrl + 128, sizeof(int), cudaMemcpyDeviceToHost,
+                      s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return DROT_ERR_CUDA;
+  for (int k = 0; k < P.n_inst; ++k) {
+    out[k].n_iter = st[k].n_iter;
+    out[k].iters_run = st[k].iters_run;
+    out[k].converged = st[k].converged;
+    out[k].objective_valid = st[k].objective_valid;
+    out[k].objective = st[k].objective;
+    out[k].residual = st[k].residual;
+  }
+  return abort_flag ? DROT_ERR_BARRIER_TIMEOUT : DROT_OK;
+}
+
+}  // extern "C"

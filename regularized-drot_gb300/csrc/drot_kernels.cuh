@@ -189,22 +189,22 @@ __device__ __forceinline__ double warp_sum_strided(const double* v, int n, int l
 
 // Grid barrier.  Returns false when the run was aborted (time limit hit here
 // or in another CTA).  `epoch` counts barriers passed by this CTA.
-__device__ __forceinline__ bool grid_barrier(const SolveParams& P, unsigned& epoch,
-                                             int* s_flag) {
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, int* abort_flag, long long timeout_ns,
+                                             unsigned& epoch, int* s_flag) {
   __syncthreads();
   if (threadIdx.x == 0) {
     epoch += 1u;
     const unsigned target = epoch * gridDim.x;
     __threadfence();
-    red_release_add_u32(P.bar, 1u);
+    red_release_add_u32(bar, 1u);
     int ok = 1;
     const unsigned long long t0 = globaltimer_ns();
     unsigned spins = 0;
-    while ((int)(ld_acquire_u32(P.bar) - target) < 0) {
+    while ((int)(ld_acquire_u32(bar) - target) < 0) {
       if ((++spins & 31u) == 0u) {
-        if (ld_volatile_i32(P.abort_flag)) { ok = 0; break; }
-        if ((long long)(globaltimer_ns() - t0) > P.timeout_ns) {
-          atomicExch(P.abort_flag, 1);
+        if (ld_volatile_i32(abort_flag)) { ok = 0; break; }
+        if ((long long)(globaltimer_ns() - t0) > timeout_ns) {
+          atomicExch(abort_flag, 1);
           ok = 0;
           break;
         }
@@ -215,6 +215,10 @@ __device__ __forceinline__ bool grid_barrier(const SolveParams& P, unsigned& epo
   }
   __syncthreads();
   return *s_flag != 0;
+}
+
+__device__ __forceinline__ bool grid_barrier(const SolveParams& P, unsigned& epoch, int* s_flag) {
+  return grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, s_flag);
 }
 
 // ---- shared-memory addresses, mbarriers and TMA bulk copies -------------

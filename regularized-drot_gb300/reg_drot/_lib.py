@@ -38,6 +38,29 @@ class DrotResult(ctypes.Structure):
 
 _RP = ctypes.POINTER(DrotResult)
 
+
+class DrotBatchInstance(ctypes.Structure):
+    _fields_ = [
+        ("n_rows", ctypes.c_int), ("n_cols", ctypes.c_int), ("ld", ctypes.c_int),
+        ("pad", ctypes.c_int),
+        ("c_offset", ctypes.c_longlong), ("x_offset", ctypes.c_longlong),
+        ("p_offset", ctypes.c_longlong), ("q_offset", ctypes.c_longlong),
+        ("rho", ctypes.c_float), ("r_weight", ctypes.c_float), ("eps", ctypes.c_float),
+        ("pad2", ctypes.c_float),
+    ]
+
+
+class DrotBatchResult(ctypes.Structure):
+    _fields_ = [
+        ("n_iter", ctypes.c_int), ("iters_run", ctypes.c_int), ("converged", ctypes.c_int),
+        ("objective_valid", ctypes.c_int), ("objective", ctypes.c_double),
+        ("residual", ctypes.c_double),
+    ]
+
+
+_BIP = ctypes.POINTER(DrotBatchInstance)
+_BRP = ctypes.POINTER(DrotBatchResult)
+
 SIGNATURES = {
     "drot_status_string": (ctypes.c_char_p, [_c_int]),
     "drot_last_status": (_c_int, []),
@@ -80,6 +103,14 @@ SIGNATURES = {
     "drot_free_host": (None, [_fp]),
     "drot_quadratic_drot_noalloc": (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_float, _c_float,
                                              _c_int, _c_float, _vp, _RP, _vp]),
+    "drot_batch_plan_create": (_c_int, [_c_int, _BIP, _c_int, ctypes.POINTER(_vp)]),
+    "drot_batch_plan_destroy": (None, [_vp]),
+    "drot_batch_plan_workspace_bytes": (_c_size, [_vp]),
+    "drot_batch_plan_tiles": (_c_int, [_vp]),
+    "drot_batch_upload": (_c_int, [_vp, _vp, _c_size, _vp]),
+    "drot_qr_batch_launch": (_c_int, [_vp, _vp, _c_int, _vp, _vp, _vp, _c_int, _vp, _c_size,
+                                      _vp]),
+    "drot_batch_results": (_c_int, [_vp, _vp, _BRP, _vp]),
 }
 
 _lib = None

@@ -1,0 +1,237 @@
+"""Batched quadratic-regularised DROT: many instances, one persistent launch.
+
+The reference solves one problem per call (pytorch/src/drot_cuda.cpp:26-44;
+its callers loop, e.g. benchmark/utils/compute_w2_dist.py:86).  ``QRBatch``
+solves a list of independent instances of different shapes together: per
+instance the iteration, warm start, stop test and iteration count of
+``reg_drot.quadratic_drot``, each instance stopping on its own.
+
+Instances are packed into flat buffers.  Instance k's cost ``c_k`` (a
+[n_cols, n_rows] tensor, the layout of the reference operator) occupies
+``n_cols`` columns of ``ld_k = n_rows`` rounded up to 4 elements, starting at
+a 32-element boundary of the packed C buffer; its plan X has the same place
+in the packed X buffer; p_k and q_k are concatenated.
+
+    B = QRBatch([(nr, nc), ...], rho=2.0, r_weight=1e-3, eps=1e-4)
+    c = B.pack_c(list_of_costs)            # float32 or bfloat16
+    p, q = B.pack_marginals(ps, qs)
+    x, info = B.solve(c, p, q, max_iters)  # info: list of per-instance dicts
+    plans = B.unpack(x)                    # [n_cols, n_rows] views
+
+``solve(..., sync=False)`` only enqueues device work (an init kernel and one
+cooperative launch), so it can be captured in a CUDA graph
+(``B.capture(c, p, q, x, max_iters)``).  ``cols_per_tile=None`` picks the tile
+width by timing short runs of each candidate on the caller's data.
+"""
+import ctypes
+
+import torch
+
+from ._lib import DrotBatchInstance, DrotBatchResult, DrotError, check, lib
+
+C_F32, C_BF16 = 0, 1
+TILE_CANDIDATES = (32, 64, 128, 256)
+_ALIGN = 32  # elements between instance blocks (128 bytes of FP32)
+
+
+def _as_list(v, n, name):
+    if isinstance(v, (list, tuple)):
+        if len(v) != n:
+            raise RuntimeError(f"{name} needs one value per instance")
+        return [float(t) for t in v]
+    return [float(v)] * n
+
+
+class QRBatch:
+    """A fixed set of instance shapes and parameters, planned once."""
+
+    def __init__(self, shapes, rho, r_weight, eps, *, device=None, cols_per_tile=None):
+        shapes = [(int(a), int(b)) for a, b in shapes]
+        if not shapes:
+            raise RuntimeError("QRBatch needs at least one instance")
+        self.shapes = shapes
+        self.n = len(shapes)
+        device = torch.device("cuda" if device is None else device)
+        if device.type != "cuda":
+            raise RuntimeError("QRBatch runs on a CUDA device")
+        if device.index is None:
+            device = torch.device("cuda", torch.cuda.current_device())
+        self.device = device
+        rho = _as_list(rho, self.n, "rho")
+        r_weight = _as_list(r_weight, self.n, "r_weight")
+        eps = _as_list(eps, self.n, "eps")
+        desc = (DrotBatchInstance * self.n)()
+        off = prow = pcol = 0
+        self.offsets, self.lds = [], []
+        for k, (nr, nc) in enumerate(shapes):
+            if nr <= 0 or nc <= 0:
+                raise RuntimeError("instance shapes must be positive")
+            ld = (nr + 3) // 4 * 4
+            d = desc[k]
+            d.n_rows, d.n_cols, d.ld = nr, nc, ld
+            d.c_offset = d.x_offset = off
+            d.p_offset, d.q_offset = prow, pcol
+            d.rho, d.r_weight, d.eps = rho[k], r_weight[k], eps[k]
+            self.offsets.append(off)
+            self.lds.append(ld)
+            off += (ld * nc + _ALIGN - 1) // _ALIGN * _ALIGN
+            prow += nr
+            pcol += nc
+        self.total = off
+        self.total_rows, self.total_cols = prow, pcol
+        self._desc = desc
+        self._plans = {}
+        self._ws = None
+        self._ws_plan = None
+        self.cols_per_tile = cols_per_tile
+
+    # ------------------------------------------------------------------ packing
+    def pack_c(self, costs, dtype=torch.float32):
+        """Packed C buffer from [n_cols, n_rows] costs (padding rows zero)."""
+        buf = torch.zeros(self.total, dtype=dtype, device=self.device)
+        for k, c in enumerate(costs):
+            nr, nc = self.shapes[k]
+            if tuple(c.shape) != (nc, nr):
+                raise RuntimeError(f"cost {k} must have shape [{nc}, {nr}]")
+            self.view(buf, k).copy_(c)
+        return buf
+
+    def pack_marginals(self, ps, qs):
+        p = torch.cat([t.reshape(-1).float() for t in ps]).to(self.device).contiguous()
+        q = torch.cat([t.reshape(-1).float() for t in qs]).to(self.device).contiguous()
+        if p.numel() != self.total_rows or q.numel() != self.total_cols:
+            raise RuntimeError("marginal sizes do not match the instance shapes")
+        return p, q
+
+    def view(self, buf, k):
+        """[n_cols, n_rows] view of instance k inside a packed buffer."""
+        nr, nc = self.shapes[k]
+        ld, off = self.lds[k], self.offsets[k]
+        return buf[off:off + ld * nc].view(nc, ld)[:, :nr]
+
+    def unpack(self, buf):
+        return [self.view(buf, k) for k in range(self.n)]
+
+    def empty_x(self):
+        return torch.empty(self.total, dtype=torch.float32, device=self.device)
+
+    # ------------------------------------------------------------------ plans
+    def _plan(self, cols_per_tile):
+        cpt = int(cols_per_tile)
+        if cpt not in self._plans:
+            h = ctypes.c_void_p()
+            with torch.cuda.device(self.device):
+                check(lib().drot_batch_plan_create(self.n, self._desc, cpt, ctypes.byref(h)),
+                      "batch_plan_create")
+            self._plans[cpt] = h
+        return self._plans[cpt]
+
+    def workspace_for(self, cols_per_tile, stream=None):
+        """Workspace holding the plan's uploaded descriptors (reused while the
+        tile width stays the same)."""
+        h = self._plan(cols_per_tile)
+        nbytes = int(lib().drot_batch_plan_workspace_bytes(h))
+        if self._ws is None or self._ws.numel() < nbytes + 256:
+            self._ws = torch.empty(nbytes + 256, dtype=torch.uint8, device=self.device)
+            self._ws_plan = None
+        ptr = self._ws.data_ptr()
+        ptr += (-ptr) % 256
+        if self._ws_plan != cols_per_tile:
+            s = torch.cuda.current_stream(self.device) if stream is None else stream
+            check(lib().drot_batch_upload(h, ptr, nbytes, s.cuda_stream), "batch_upload")
+            self._ws_plan = cols_per_tile
+        return h, ptr, nbytes
+
+    def tiles(self, cols_per_tile):
+        return int(lib().drot_batch_plan_tiles(self._plan(cols_per_tile)))
+
+    # ------------------------------------------------------------------ solve
+    def _check(self, c, p, q, x):
+        if c.device != self.device or c.dim() != 1 or c.numel() != self.total or \
+                c.dtype not in (torch.float32, torch.bfloat16) or not c.is_contiguous():
+            raise RuntimeError("c must be the packed cost buffer (pack_c)")
+        if p.numel() != self.total_rows or q.numel() != self.total_cols or \
+                p.dtype != torch.float32 or q.dtype != torch.float32 or \
+                not p.is_contiguous() or not q.is_contiguous() or \
+                p.device != self.device or q.device != self.device:
+            raise RuntimeError("p, q must be the packed marginals (pack_marginals)")
+        if x.numel() != self.total or x.dtype != torch.float32 or x.device != self.device or \
+                not x.is_contiguous():
+            raise RuntimeError("x must be a packed float32 buffer (empty_x)")
+
+    def launch(self, c, p, q, x, max_iters, cols_per_tile=None, stream=None):
+        """Enqueue warm start + solve on ``stream``; device work only."""
+        cpt = cols_per_tile or self.cols_per_tile or 128
+        h, ptr, nbytes = self.workspace_for(cpt, stream)
+        s = torch.cuda.current_stream(self.device) if stream is None else stream
+        rc = lib().drot_qr_batch_launch(h, c.data_ptr(),
+                                        C_BF16 if c.dtype == torch.bfloat16 else C_F32,
+                                        p.data_ptr(), q.data_ptr(), x.data_ptr(), int(max_iters),
+                                        ptr, nbytes, s.cuda_stream)
+        check(rc, "qr_batch_launch")
+
+    def results(self, stream=None):
+        """Per-instance records of the last launch (waits for the stream)."""
+        out = (DrotBatchResult * self.n)()
+        h, ptr, _ = self.workspace_for(self._ws_plan or self.cols_per_tile or 128, stream)
+        s = torch.cuda.current_stream(self.device) if stream is None else stream
+        rc = lib().drot_batch_results(h, ptr, out, s.cuda_stream)
+        check(rc, "batch_results")
+        return [{name: getattr(r, name) for name, _ in r._fields_} for r in out]
+
+    def autotune(self, c, p, q, iters=40, candidates=TILE_CANDIDATES):
+        """Times ``iters`` iterations per tile width on the caller's data and
+        keeps the fastest (the candidates give identical results)."""
+        x = self.empty_x()
+        best = None
+        for cpt in candidates:
+            self.launch(c, p, q, x, iters, cpt)  # warm-up (plan upload, caches)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(2):
+                self.launch(c, p, q, x, iters, cpt)
+            e1.record()
+            e1.synchronize()
+            t = e0.elapsed_time(e1)
+            if best is None or t < best[0]:
+                best = (t, cpt)
+        self.cols_per_tile = best[1]
+        return best[1]
+
+    def solve(self, c, p, q, max_iters, *, out=None, stream=None, sync=True):
+        """Solve every instance; returns (x, info list or None)."""
+        x = self.empty_x() if out is None else out
+        self._check(c, p, q, x)
+        with torch.cuda.device(self.device):
+            if self.cols_per_tile is None:
+                self.autotune(c, p, q)
+            self.launch(c, p, q, x, max_iters, stream=stream)
+            info = self.results(stream) if sync else None
+        return x, info
+
+    def capture(self, c, p, q, x, max_iters, stream=None):
+        """A CUDA graph of the whole solve (warm start included); replay it
+        with ``g.replay()`` and read ``results()`` afterwards."""
+        self._check(c, p, q, x)
+        if self.cols_per_tile is None:
+            self.autotune(c, p, q)
+        cpt = self.cols_per_tile
+        self.workspace_for(cpt)  # upload outside the capture
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.launch(c, p, q, x, max_iters, cpt, torch.cuda.current_stream(self.device))
+        g.drot_workspace = self._ws  # the graph reads this workspace
+        return g
+
+    def __del__(self):
+        try:
+            for h in self._plans.values():
+                lib().drot_batch_plan_destroy(h)
+        except Exception:
+            pass
+        self._plans = {}
+
+
+__all__ = ["QRBatch", "DrotError", "TILE_CANDIDATES"]

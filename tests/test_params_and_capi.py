@@ -152,3 +152,27 @@ def test_operator_rejects_host_tensors():
         reg_drot.quadratic_drot(c, p, q, 2.0, 1e-2, 100, 1e-4)
     with pytest.raises(RuntimeError, match="must be a CUDA tensor"):
         reg_drot.group_lasso_drot(c, p, q, 2, 2.0, 1e-2, 100, 1e-4)
+
+
+def test_batch_plan_rejects_bad_descriptors_on_the_host(solver_lib):
+    from reg_drot._lib import DrotBatchInstance
+    h = ctypes.c_void_p()
+    good = dict(n_rows=100, n_cols=50, ld=100, c_offset=0, x_offset=0, p_offset=0, q_offset=0,
+                rho=2.0, r_weight=1e-3, eps=1e-4)
+    bad = [dict(ld=99), dict(ld=102), dict(n_rows=0), dict(n_cols=-1), dict(c_offset=2),
+           dict(x_offset=6), dict(rho=0.0), dict(r_weight=-1.0), dict(p_offset=-1)]
+    for change in bad:
+        arr = (DrotBatchInstance * 2)()
+        for d in arr:
+            for k, v in good.items():
+                setattr(d, k, v)
+        for k, v in change.items():
+            setattr(arr[1], k, v)
+        assert solver_lib.drot_batch_plan_create(2, arr, 128, ctypes.byref(h)) == 1, change
+        assert not h.value
+    assert solver_lib.drot_batch_plan_create(0, None, 128, ctypes.byref(h)) == 1
+    assert solver_lib.drot_batch_plan_workspace_bytes(None) == 0
+    assert solver_lib.drot_batch_plan_tiles(None) == 0
+    solver_lib.drot_batch_plan_destroy(None)
+    assert solver_lib.drot_qr_batch_launch(None, None, 0, None, None, None, 10, None, 0,
+                                           None) == 1
