@@ -299,6 +299,93 @@ def gl_da_point(dev):
             "published_v100_median_s": 0.0619}
 
 
+BATCH_INSTANCES = 256
+BATCH_MIN, BATCH_MAX = 64, 2048
+
+
+def make_batch_problem(dev, n_inst=BATCH_INSTANCES, seed=SEED):
+    """Batched workload: n_inst instances, m, n ~ U{64..2048} independent,
+    C = squared Euclidean distances of N(0, I_8) point clouds (max-normalised
+    per instance), uniform marginals; eps_k = REL_EPS * ||(p_k; q_k)||_2."""
+    import torch
+    rng = np.random.default_rng(seed)
+    shapes = [(int(a), int(b)) for a, b in rng.integers(BATCH_MIN, BATCH_MAX + 1, size=(n_inst, 2))]
+    g = torch.Generator(device=dev).manual_seed(seed)
+    costs, ps, qs, eps = [], [], [], []
+    for (m, n) in shapes:
+        xs = torch.randn(m, 8, generator=g, device=dev)
+        yt = torch.randn(n, 8, generator=g, device=dev)
+        c = (yt * yt).sum(1, keepdim=True) + (xs * xs).sum(1)[None, :] - 2.0 * (yt @ xs.T)
+        c = c.clamp_min_(0.0)
+        costs.append(c / c.max())                      # [n_cols = n, n_rows = m]
+        ps.append(torch.full((m,), 1.0 / m))
+        qs.append(torch.full((n,), 1.0 / n))
+        eps.append(REL_EPS * math.sqrt(1.0 / m + 1.0 / n))
+    return shapes, costs, ps, qs, eps
+
+
+def batched_point(dev, flush, single_sample=16):
+    """The batched solver on the 256-instance workload (FP32 and BF16-stored
+    C), one CUDA-graph replay per solve of the whole batch, against solving
+    the same instances one at a time with reg_drot.solve_qr."""
+    import torch
+    import reg_drot
+    from reg_drot.batch import QRBatch
+    shapes, costs, ps, qs, eps = make_batch_problem(dev)
+    elems = np.array([m * n for m, n in shapes], dtype=np.float64)
+    out = {"workload": (f"batched QR-DROT, {len(shapes)} instances, m,n ~ U{{{BATCH_MIN}..{BATCH_MAX}}}, "
+                        f"C = sq. Euclidean of N(0,I_8) clouds / max, uniform marginals, "
+                        f"alpha={ALPHA}, rho={RHO}, relative eps {REL_EPS}"),
+           "elements": int(elems.sum())}
+    peak, _ = measured_peak()
+    for name, dtype in (("fp32", torch.float32), ("bf16_c", torch.bfloat16)):
+        B = QRBatch(shapes, RHO, ALPHA, eps, device=dev)
+        c = B.pack_c(costs, dtype=dtype)
+        p, q = B.pack_marginals(ps, qs)
+        cpt = B.autotune(c, p, q, iters=200)
+        x = B.empty_x()
+        graph = B.capture(c, p, q, x, 10 ** 6)
+        graph.replay()
+        times = []
+        for _ in range(3):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            graph.replay()
+            b.record()
+            b.synchronize()
+            times.append(a.elapsed_time(b) / 1e3)
+        info = B.results()
+        it = np.array([r["n_iter"] for r in info], dtype=np.float64)
+        cb = 2 if dtype == torch.bfloat16 else 4
+        # even iterations read C (cb bytes) + X and write X, odd ones X only,
+        # plus the unfold pass (C + X read, X write).
+        nbytes = float((elems * ((8 + cb) * np.ceil(it / 2) + 8 * np.floor(it / 2) + 8 + cb)).sum())
+        t = statistics.median(times)
+        out[name] = {"solves_per_s": len(shapes) / t, "s_per_batch": t, "cols_per_tile": cpt,
+                     "converged": int(sum(r["converged"] for r in info)),
+                     "n_iter_min_median_max": [int(it.min()), float(np.median(it)), int(it.max())],
+                     "achieved_GBps": nbytes / t / 1e9, "frac_of_measured_hbm": nbytes / t / 1e9 / peak}
+        del B, c, x, graph
+    # The same instances one solve at a time (a sample, every 16th instance).
+    ks = list(range(0, len(shapes), max(1, len(shapes) // single_sample)))
+    t_sum = 0.0
+    for k in ks:
+        cd, pd, qd = costs[k].contiguous(), ps[k].to(dev), qs[k].to(dev)
+        xk, ik, ws = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, 10 ** 6, eps[k])
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        xk, ik, ws = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, 10 ** 6, eps[k], out=xk, workspace=ws)
+        b.record()
+        b.synchronize()
+        t_sum += a.elapsed_time(b) / 1e3
+    out["per_instance_solves_per_s"] = len(ks) / t_sum
+    out["per_instance_sample"] = f"{len(ks)} instances (every {len(shapes) // len(ks)}th), one solve each"
+    out["speedup_fp32_vs_per_instance"] = out["fp32"]["solves_per_s"] / out["per_instance_solves_per_s"]
+    return out
+
+
 def run_gpu(args):
     import torch
     import reg_drot
@@ -373,7 +460,8 @@ def run_gpu(args):
                          "the 10000^2 point in extra.hbm_point is the HBM-resident case")}
 
     e2e = e2e_wrapper(c, p, q, eps, args.steps)
-    extra = {"hbm_point": hbm_point(dev, flush), "gl_da": gl_da_point(dev)}
+    extra = {"hbm_point": hbm_point(dev, flush), "gl_da": gl_da_point(dev),
+             "batched": batched_point(dev, flush)}
     cpu = cpu_sample(budget_s=12.0) if world == 1 else None
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,

@@ -43,7 +43,8 @@ struct BatchInst {
 };
 
 struct BatchTile {
-  int inst, band, chunk, lo, hi, c0, c1, pad;
+  int inst, band, chunk, lo, hi, c0, c1;
+  int kvr;  // 128-row blocks per warp step: 1, 2 or 4 (band height <= 128 * kvr)
 };
 
 struct BatchStat {
@@ -101,9 +102,132 @@ __global__ void batch_init_kernel(const BatchParams P) {
   }
 }
 
+// The column loop of one tile.  A warp step covers 512 elements per lane
+// group: KVR row blocks of 128 rows (32 lanes x float4) times 4 / KVR columns,
+// so short bands (the last band of an instance, or instances under 512 rows)
+// still put 16 loads per lane in flight.  EV: even iteration (reads C, stores
+// the folded X - sC), else odd (reads X only).  FULL: the band is exactly
+// 128 * KVR rows (no row masks).  Element arithmetic as in the
+// single-instance kernel: t = (X + phi1) + phi2 (- sC), y = max(t, 0) / kappa.
+template <int KVR, bool EV, bool FULL, typename CT>
+__device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const BatchInst& I,
+                                                   const BatchTile& T, const float* f1s,
+                                                   float (&acc)[4][4], float& ms_hi,
+                                                   float& ms_lo, float& ob_hi, float& ob_lo,
+                                                   int lane, int warp, int W) {
+  constexpr int VEC = 4, SV = 128, NCOL = 4 / KVR;
+  const CT* const cbase = reinterpret_cast<const CT*>(P.c);
+  const int lo = T.lo, hi = T.hi, c1 = T.c1;
+  const float s = I.s, kappa = I.kappa, krcp = I.kappa_rcp;
+  for (int j0 = T.c0 + warp * NCOL; j0 < c1; j0 += W * NCOL) {
+    float xv[4][VEC], cv[4][VEC], f2[NCOL];
+    // All loads of the step first (nothing consumes them before the last
+    // one is issued).
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int jc = j0 + v / KVR;
+      const int r = lo + (v % KVR) * SV + lane * VEC;
+      if ((NCOL == 1 || jc < c1) && (FULL || r < hi)) {
+        load_vec<VEC>(P.x + I.x_off + (long long)jc * I.ld + r, xv[v]);
+        if constexpr (EV) load_c<VEC, CT>(cbase + I.c_off + (long long)jc * I.ld + r, cv[v]);
+        else {
+#pragma unroll
+          for (int e = 0; e < VEC; ++e) cv[v][e] = 0.0f;
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) { xv[v][e] = 0.0f; cv[v][e] = 0.0f; }
+      }
+    }
+#pragma unroll
+    for (int cc = 0; cc < NCOL; ++cc)
+      f2[cc] = (NCOL == 1 || j0 + cc < c1) ? __ldcg(P.phi2 + I.col_off + j0 + cc) : 0.0f;
+
+    auto valid = [&](int v, int e) -> bool {
+      if constexpr (FULL && NCOL == 1) return true;
+      const bool colok = (NCOL == 1) || (j0 + v / KVR < c1);
+      return colok && (FULL || lo + (v % KVR) * SV + lane * VEC + e < hi);
+    };
+    unsigned tmin = 0xffffffffu;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const float4 f1 = *reinterpret_cast<const float4*>(f1s + (v % KVR) * SV + lane * VEC);
+      const float f1a[VEC] = {f1.x, f1.y, f1.z, f1.w};
+#pragma unroll
+      for (int e = 0; e < VEC; ++e) {
+        float tt = (xv[v][e] + f1a[e]) + f2[v / KVR];
+        if constexpr (EV) tt = fmaf(-s, cv[v][e], tt);
+        xv[v][e] = tt;
+        const unsigned key = (unsigned)__float_as_int(tt) - 1u;
+        tmin = min(tmin, valid(v, e) ? key : 0xffffffffu);
+      }
+    }
+    // A nonzero t below 2^-90 anywhere in the step sends the whole step
+    // through the IEEE division (one warp vote).
+    const bool slow = __any_sync(0xffffffffu, tmin < kDivTinyBitsM1);
+    float colp[NCOL], objp = 0.0f;
+#pragma unroll
+    for (int cc = 0; cc < NCOL; ++cc) colp[cc] = 0.0f;
+    auto body = [&](auto slow_tag) {
+      constexpr bool SLOW = decltype(slow_tag)::value;
+#pragma unroll
+      for (int v = 0; v < 4; ++v)
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+          const bool ok = valid(v, e);
+          const float a0 = fmaxf(xv[v][e], 0.0f);
+          float y = SLOW ? a0 / kappa : div_rn_by_fma(a0, kappa, krcp);
+          y = ok ? y : 0.0f;
+          if constexpr (EV) {
+            const float c = ok ? cv[v][e] : 0.0f;  // the caller's padding may hold anything
+            xv[v][e] = fmaf(-s, c, y);
+            objp = fmaf(y, c, objp);
+          } else {
+            xv[v][e] = y;
+          }
+          acc[v % KVR][e] += y;
+          colp[v / KVR] += y;
+        }
+    };
+    if (slow) body(std::true_type());
+    else body(std::false_type());
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int jc = j0 + v / KVR;
+      const int r = lo + (v % KVR) * SV + lane * VEC;
+      if ((NCOL == 1 || jc < c1) && (FULL || r < hi)) {
+        float* xp = P.x + I.x_off + (long long)jc * I.ld + r;
+        if (FULL || r + VEC <= hi) {
+          store_vec<VEC>(xp, xv[v]);
+        } else {
+#pragma unroll
+          for (int e = 0; e < VEC; ++e)
+            if (r + e < hi) xp[e] = xv[v][e];
+        }
+      }
+    }
+    float e1;
+#pragma unroll
+    for (int cc = 0; cc < NCOL; ++cc) {
+      two_sum(ms_hi, colp[cc], ms_hi, e1);
+      ms_lo += e1;
+    }
+    if constexpr (EV) {
+      two_sum(ob_hi, objp, ob_hi, e1);
+      ob_lo += e1;
+    }
+#pragma unroll
+    for (int cc = 0; cc < NCOL; ++cc) {
+      const float cs = warp_sum(colp[cc]);
+      if (lane == 0 && (NCOL == 1 || j0 + cc < c1))
+        P.colpart[I.cp_off + (long long)T.band * I.nc + j0 + cc] = cs;
+    }
+  }
+}
+
 template <typename CT>
 __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P) {
-  constexpr int VEC = 4, KV = kBatchKV, SV = 128, S = kBatchS;
+  constexpr int VEC = 4, KV = kBatchKV, S = kBatchS;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int W = blockDim.x >> 5;
   float* red = reinterpret_cast<float*>(smem_raw);  // [W][S]
@@ -138,113 +262,42 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
         f1s[idx] = r < hi ? __ldcg(P.phi1 + I.row_off + r) : 0.0f;
       }
       __syncthreads();
-      const int lrow = lo + lane * VEC;
-      float acc[KV][VEC];
+      float acc[4][4];
 #pragma unroll
-      for (int v = 0; v < KV; ++v)
+      for (int v = 0; v < 4; ++v)
 #pragma unroll
-        for (int e = 0; e < VEC; ++e) acc[v][e] = 0.0f;
+        for (int e = 0; e < 4; ++e) acc[v][e] = 0.0f;
       float ms_hi = 0.0f, ms_lo = 0.0f, ob_hi = 0.0f, ob_lo = 0.0f;
-      const float s = I.s, kappa = I.kappa, krcp = I.kappa_rcp;
-      // The column loop of one tile; EV: even iteration (reads C, stores the
-      // folded X - sC), else odd (reads X only).  Same arithmetic as the
-      // single-instance kernel.
-      auto tile_columns = [&](auto even_tag) {
-        constexpr bool EV = decltype(even_tag)::value;
-        for (int j = T.c0 + warp; j < T.c1; j += W) {
-          float* xcol = P.x + I.x_off + (long long)j * I.ld;
-          const CT* ccol = cbase + I.c_off + (long long)j * I.ld;
-          const float f2 = __ldcg(P.phi2 + I.col_off + j);
-          float xv[KV][VEC], cv[KV][VEC];
-#pragma unroll
-          for (int v = 0; v < KV; ++v) {
-            const int r = lrow + v * SV;
-            if (r < hi) {
-              load_vec<VEC>(xcol + r, xv[v]);
-              if constexpr (EV) load_c<VEC, CT>(ccol + r, cv[v]);
-              else {
-#pragma unroll
-                for (int e = 0; e < VEC; ++e) cv[v][e] = 0.0f;
-              }
-              if (r + VEC > hi) {
-                // Rows between n_rows and ld belong to the caller: zero them
-                // so that they add exact zeros.
-#pragma unroll
-                for (int e = 0; e < VEC; ++e)
-                  if (r + e >= hi) { xv[v][e] = 0.0f; cv[v][e] = 0.0f; }
-              }
-            } else {
-#pragma unroll
-              for (int e = 0; e < VEC; ++e) { xv[v][e] = 0.0f; cv[v][e] = 0.0f; }
-            }
-          }
-          unsigned tmin = 0xffffffffu;
-#pragma unroll
-          for (int v = 0; v < KV; ++v) {
-            const float4 f1 = *reinterpret_cast<const float4*>(f1s + v * SV + lane * VEC);
-            const float f1a[VEC] = {f1.x, f1.y, f1.z, f1.w};
-#pragma unroll
-            for (int e = 0; e < VEC; ++e) {
-              float tt = (xv[v][e] + f1a[e]) + f2;
-              if constexpr (EV) tt = fmaf(-s, cv[v][e], tt);
-              xv[v][e] = tt;
-              tmin = min(tmin, (unsigned)__float_as_int(tt) - 1u);
-            }
-          }
-          const bool slow = __any_sync(0xffffffffu, tmin < kDivTinyBitsM1);
-          float colp = 0.0f, objp = 0.0f;
-          auto body = [&](auto slow_tag) {
-            constexpr bool SLOW = decltype(slow_tag)::value;
-#pragma unroll
-            for (int v = 0; v < KV; ++v)
-#pragma unroll
-              for (int e = 0; e < VEC; ++e) {
-                const float a0 = fmaxf(xv[v][e], 0.0f);
-                float y = SLOW ? a0 / kappa : div_rn_by_fma(a0, kappa, krcp);
-                y = (lrow + v * SV + e < hi) ? y : 0.0f;
-                if constexpr (EV) {
-                  xv[v][e] = fmaf(-s, cv[v][e], y);
-                  objp = fmaf(y, cv[v][e], objp);
-                } else {
-                  xv[v][e] = y;
-                }
-                acc[v][e] += y;
-                colp += y;
-              }
-          };
-          if (slow) body(std::true_type());
-          else body(std::false_type());
-#pragma unroll
-          for (int v = 0; v < KV; ++v) {
-            const int r = lrow + v * SV;
-            if (r + VEC <= hi) {
-              store_vec<VEC>(xcol + r, xv[v]);
-            } else if (r < hi) {
-#pragma unroll
-              for (int e = 0; e < VEC; ++e)
-                if (r + e < hi) xcol[r + e] = xv[v][e];
-            }
-          }
-          float e1;
-          two_sum(ms_hi, colp, ms_hi, e1);
-          ms_lo += e1;
-          if constexpr (EV) {
-            two_sum(ob_hi, objp, ob_hi, e1);
-            ob_lo += e1;
-          }
-          colp = warp_sum(colp);
-          if (lane == 0) P.colpart[I.cp_off + (long long)T.band * I.nc + j] = colp;
-        }
+      auto run = [&](auto kvr_tag, auto ev_tag) {
+        constexpr int KVR = decltype(kvr_tag)::value;
+        constexpr bool EV = decltype(ev_tag)::value;
+        if (hi - lo == 128 * KVR)
+          batch_tile_columns<KVR, EV, true, CT>(P, I, T, f1s, acc, ms_hi, ms_lo, ob_hi, ob_lo,
+                                                lane, warp, W);
+        else
+          batch_tile_columns<KVR, EV, false, CT>(P, I, T, f1s, acc, ms_hi, ms_lo, ob_hi, ob_lo,
+                                                 lane, warp, W);
       };
-      if (even) tile_columns(std::true_type());
-      else tile_columns(std::false_type());
+      using K1 = std::integral_constant<int, 1>;
+      using K2 = std::integral_constant<int, 2>;
+      using K4 = std::integral_constant<int, 4>;
+      if (even) {
+        if (T.kvr == 1) run(K1(), std::true_type());
+        else if (T.kvr == 2) run(K2(), std::true_type());
+        else run(K4(), std::true_type());
+      } else {
+        if (T.kvr == 1) run(K1(), std::false_type());
+        else if (T.kvr == 2) run(K2(), std::false_type());
+        else run(K4(), std::false_type());
+      }
       // Tile partials: rows (fixed warp order), mass and objective (FP64).
       const double wsum = warp_sum_d((double)ms_hi + (double)ms_lo);
       const double wobj = even ? warp_sum_d((double)ob_hi + (double)ob_lo) : 0.0;
 #pragma unroll
-      for (int v = 0; v < KV; ++v)
-        *reinterpret_cast<float4*>(red + (size_t)warp * S + v * SV + lane * VEC) =
-            make_float4(acc[v][0], acc[v][1], acc[v][2], acc[v][3]);
+      for (int v = 0; v < 4; ++v)
+        if (v < T.kvr)
+          *reinterpret_cast<float4*>(red + (size_t)warp * S + v * 128 + lane * 4) =
+              make_float4(acc[v][0], acc[v][1], acc[v][2], acc[v][3]);
       if (lane == 0) {
         dscr[warp] = wsum;
         oscr[warp] = wobj;
@@ -362,7 +415,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
         const CT* ccol = cbase + I.c_off + (long long)j * I.ld;
 #pragma unroll
         for (int v = 0; v < KV; ++v) {
-          const int r = T.lo + lane * VEC + v * SV;
+          const int r = T.lo + lane * VEC + v * 128;
           if (r >= T.hi) continue;
           float xv[VEC], cv[VEC];
           load_vec<VEC>(xcol + r, xv);
@@ -452,9 +505,10 @@ int drot_batch_plan_create(int n_inst, const drot_batch_instance* desc, int cols
     I.x_off = d.x_offset;
     I.p_off = d.p_offset;
     I.q_off = d.q_offset;
+    // Bands of 512 rows; the last one takes the remainder and the narrowest
+    // warp step (128, 256 or 512 rows x 4, 2 or 1 columns) that covers it.
+    I.band_h = kBatchS;
     I.nbands = (d.n_rows + kBatchS - 1) / kBatchS;
-    I.band_h = (((d.n_rows + I.nbands - 1) / I.nbands) + 3) & ~3;
-    I.nbands = (d.n_rows + I.band_h - 1) / I.band_h;
     I.P = (d.n_cols + cols_per_tile - 1) / cols_per_tile;
     I.tile0 = (int)P.tiles.size();
     for (int b = 0; b < I.nbands; ++b)
@@ -463,11 +517,12 @@ int drot_batch_plan_create(int n_inst, const drot_batch_instance* desc, int cols
         T.inst = k;
         T.band = b;
         T.chunk = c;
-        T.lo = b * I.band_h;
-        T.hi = std::min(T.lo + I.band_h, d.n_rows);
+        T.lo = b * kBatchS;
+        T.hi = std::min(T.lo + kBatchS, d.n_rows);
         T.c0 = (int)(((long long)d.n_cols * c) / I.P);
         T.c1 = (int)(((long long)d.n_cols * (c + 1)) / I.P);
-        T.pad = 0;
+        const int h = T.hi - T.lo;
+        T.kvr = h <= 128 ? 1 : (h <= 256 ? 2 : 4);
         P.tiles.push_back(T);
       }
     I.ntiles = (int)P.tiles.size() - I.tile0;
