@@ -304,6 +304,65 @@ int drot_qr_batch_launch(drot_batch_plan plan, const void *c, int c_dtype,
  * Returns DROT_ERR_BARRIER_TIMEOUT when the launch gave up on a barrier. */
 int drot_batch_results(drot_batch_plan plan, const void *workspace,
                        drot_batch_result *out, drot_stream_t stream);
+/* Device pointers of the final duals phi1 (all instances' rows, in instance
+ * order) and phi2 (all columns) inside a launched workspace; instance k's
+ * entries start at the sum of the earlier instances' n_rows / n_cols. */
+int drot_batch_state(drot_batch_plan plan, void *workspace, float **phi1,
+                     float **phi2);
+
+/* ---------------------------------------------------------------------------
+ * Implicit adjoint of the quadratic-regularised plan (autograd backward)
+ *
+ * No counterpart in the reference (its operators have no backward).  At
+ * the solution X of min <C,X> + (lambda/2)||X||^2 over the transport
+ * polytope, with support S = {X > 0} and mask M, the adjoint system is
+ *     [D_r M; M^T D_c] [a; b] = [rowsum(G o M); colsum(G o M)]
+ * (D_r, D_c: row / column support counts), and then
+ *     dL/dC = (a_i + b_j - G_ij) / lambda on S, 0 elsewhere;
+ *     dL/dp = a, dL/dq = b (up to a + t, b - t).
+ * The support is read off the duals of the solve: S = {phi1_i + phi2_j -
+ * s C_ij > 0} (at the fixed point of X = max(X + phi1 + phi2 - sC, 0)/kappa
+ * the plan is positive exactly there; a finite solve still holds tiny
+ * positive entries of X off S that decay towards 0).
+ *
+ * drot_qr_adjoint_prepare builds the bit-packed support masks (and,
+ * optionally, a byte mask in the layout of C for the caller's own
+ * right-hand side and gradient assembly); drot_qr_adjoint_solve then solves
+ * the system of every instance with Jacobi-preconditioned conjugate
+ * gradients in one persistent launch whose matvecs walk the mask bits.
+ * ------------------------------------------------------------------------- */
+
+/* One instance: C is n_rows x n_cols column-major with leading dimension ld
+ * at element c_offset of the C buffer; its phi1 (n_rows) and phi2 (n_cols)
+ * start at phi1_offset / phi2_offset of the phi buffers; step_size is the s
+ * of its solve; its right-hand side and solution [a (n_rows); b (n_cols)]
+ * start at element v_offset of rhs / z. */
+typedef struct {
+  int n_rows, n_cols, ld, pad;
+  long long c_offset, v_offset, phi1_offset, phi2_offset;
+  float step_size, pad2;
+} drot_adjoint_instance;
+
+/* Workspace of the prepare + solve pair (the same for both calls). */
+size_t drot_qr_adjoint_workspace_bytes(int n_inst, const drot_adjoint_instance *inst);
+
+/* Support masks of every instance into the workspace; mask (may be NULL)
+ * receives 1 / 0 bytes at the positions of C.  c: DROT_C_F32 or DROT_C_BF16.
+ * Synchronises `stream`. */
+int drot_qr_adjoint_prepare(int n_inst, const drot_adjoint_instance *inst,
+                            const void *c, int c_dtype, const float *phi1,
+                            const float *phi2, unsigned char *mask,
+                            void *workspace, size_t workspace_bytes,
+                            drot_stream_t stream);
+
+/* After drot_qr_adjoint_prepare on the same workspace and instances: solves
+ * until ||r|| <= tol * ||r_0|| per instance or max_iters; writes z and, when
+ * iters != NULL, the CG iterations of each instance (host array of n_inst).
+ * Synchronises `stream`. */
+int drot_qr_adjoint_solve(int n_inst, const drot_adjoint_instance *inst,
+                          const float *rhs, float *z, float tol, int max_iters,
+                          void *workspace, size_t workspace_bytes, int *iters,
+                          drot_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -1,8 +1,9 @@
 """Build recipe of the solver library (libdrot_gb300.so) for sm_103a.
 
 nvcc compiles the translation units csrc/drot_api.cu (single-instance
-solver and C ABI) and csrc/drot_batch.cu (batched solver) in parallel and
-links them into reg_drot/libdrot_gb300.so, in tree.  Device code is compiled with
+solver and C ABI), csrc/drot_batch.cu (batched solver) and
+csrc/drot_adjoint.cu (implicit adjoint for autograd) in parallel and links
+them into reg_drot/libdrot_gb300.so, in tree.  Device code is compiled with
 --fmad=false: the kernels spell out every fused multiply-add they need
 (the ones the reference's kernels compile to), so nothing else is contracted.
 Host code is compiled with -ffp-contract=off so the parameter mapping rounds
@@ -19,7 +20,7 @@ REPO = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 OUT = os.path.join(PKG, "reg_drot", "libdrot_gb300.so")
-SOURCES = [os.path.join(CSRC, "drot_api.cu"), os.path.join(CSRC, "drot_batch.cu")]
+SOURCES = [os.path.join(CSRC, f) for f in ("drot_api.cu", "drot_batch.cu", "drot_adjoint.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))] + \
     [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
 

@@ -685,6 +685,14 @@ int drot_qr_batch_launch(drot_batch_plan plan, const void* c, int c_dtype, const
   return DROT_OK;
 }
 
+int drot_batch_state(drot_batch_plan plan, void* workspace, float** phi1, float** phi2) {
+  if (!plan || !workspace || !phi1 || !phi2) return DROT_ERR_INVALID_ARG;
+  char* ws = (char*)workspace;
+  *phi1 = (float*)(ws + plan->p.off_phi1);
+  *phi2 = (float*)(ws + plan->p.off_phi2);
+  return DROT_OK;
+}
+
 int drot_batch_results(drot_batch_plan plan, const void* workspace, drot_batch_result* out,
                        drot_stream_t stream) {
   if (!plan || !workspace || !out) return DROT_ERR_INVALID_ARG;

@@ -58,6 +58,16 @@ class DrotBatchResult(ctypes.Structure):
     ]
 
 
+class DrotAdjointInstance(ctypes.Structure):
+    _fields_ = [
+        ("n_rows", ctypes.c_int), ("n_cols", ctypes.c_int), ("ld", ctypes.c_int),
+        ("pad", ctypes.c_int), ("c_offset", ctypes.c_longlong), ("v_offset", ctypes.c_longlong),
+        ("phi1_offset", ctypes.c_longlong), ("phi2_offset", ctypes.c_longlong),
+        ("step_size", ctypes.c_float), ("pad2", ctypes.c_float),
+    ]
+
+
+_AIP = ctypes.POINTER(DrotAdjointInstance)
 _BIP = ctypes.POINTER(DrotBatchInstance)
 _BRP = ctypes.POINTER(DrotBatchResult)
 
@@ -111,6 +121,12 @@ SIGNATURES = {
     "drot_qr_batch_launch": (_c_int, [_vp, _vp, _c_int, _vp, _vp, _vp, _c_int, _vp, _c_size,
                                       _vp]),
     "drot_batch_results": (_c_int, [_vp, _vp, _BRP, _vp]),
+    "drot_batch_state": (_c_int, [_vp, _vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
+    "drot_qr_adjoint_workspace_bytes": (_c_size, [_c_int, _AIP]),
+    "drot_qr_adjoint_prepare": (_c_int, [_c_int, _AIP, _vp, _c_int, _vp, _vp, _vp, _vp,
+                                         _c_size, _vp]),
+    "drot_qr_adjoint_solve": (_c_int, [_c_int, _AIP, _vp, _vp, _c_float, _c_int, _vp, _c_size,
+                                       _ip, _vp]),
 }
 
 _lib = None

@@ -1,0 +1,225 @@
+"""Differentiable DROT plans (torch.autograd).
+
+The reference's operators return plans without gradients
+(pytorch/src/drot_cuda.cpp:26-44: outputs have requires_grad=False).  Here:
+
+  quadratic_drot_fn(c, p, q, rho, r_weight, max_iters, eps)   -> x (differentiable)
+  batch_quadratic_drot_fn(batch, c, p, q, max_iters)          -> packed x (differentiable)
+
+Forward: the CUDA solver (single instance or QRBatch).  Backward: the
+implicit adjoint of the regularised problem
+    min <C, X> + (lambda / 2) ||X||_F^2  s.t.  X 1 = p, X^T 1 = q, X >= 0,
+lambda = (kappa - 1) / s (= r_weight * (n_rows + n_cols) with the operator's
+parameters, pytorch/src/qr_drot_cuda_kernel.cu:100-102): on the support S,
+    dL/dC = (a_i + b_j - G_ij) / lambda,  dL/dp = a,  dL/dq = b,
+where [a; b] solves the masked Laplacian system built from the support
+(drot_qr_adjoint_prepare / _solve: bit-packed masks, Jacobi-preconditioned
+CG in one persistent launch).  The support is S = {phi1_i + phi2_j - s C_ij
+> 0} from the solve's final duals: a finite solve leaves tiny, geometrically
+decaying positive entries of X off S, so X > 0 would overstate it.  a and b
+are unique up to a + t, b - t (the marginals' masses are tied) -- one such
+constant per connected component of the bipartite support graph; the
+returned pair has sum(a) = sum(b) overall.  The gradient is
+that of the exact solution on a locally fixed support, so it assumes the
+forward solve converged (a warning is raised otherwise) and r_weight > 0.
+"""
+import ctypes
+import warnings
+
+import numpy as np
+import torch
+
+from ._lib import DrotAdjointInstance, check, lib
+
+C_F32, C_BF16 = 0, 1
+CG_TOL = 1e-6
+CG_MAX_ITERS = 5000
+
+f32 = np.float32
+
+
+def qr_lambda(rho, r_weight, n_rows, n_cols):
+    """lambda = (kappa - 1) / s with the FP32 s and kappa of the operator."""
+    s = f32(rho) / (f32(n_rows) + f32(n_cols))
+    t = f32(s * f32(r_weight))
+    t = f32(t * f32(n_rows + n_cols))
+    kappa = f32(f32(1.0) + t)
+    return (float(kappa) - 1.0) / float(s)
+
+
+def step_and_kappa(rho, r_weight, n_rows, n_cols):
+    s = f32(rho) / (f32(n_rows) + f32(n_cols))
+    t = f32(s * f32(r_weight))
+    t = f32(t * f32(n_rows + n_cols))
+    return float(s), float(f32(f32(1.0) + t))
+
+
+class _Adjoint:
+    """Support masks + CG solve of one or more instances (drot_qr_adjoint_*)."""
+
+    def __init__(self, c, phi1, phi2, descs):
+        # descs: (n_rows, n_cols, ld, c_offset, v_offset, phi1_offset, phi2_offset, s)
+        n = len(descs)
+        self.n = n
+        self.arr = (DrotAdjointInstance * n)()
+        for k, (nr, nc, ld, co, vo, o1, o2, st) in enumerate(descs):
+            d = self.arr[k]
+            d.n_rows, d.n_cols, d.ld, d.c_offset, d.v_offset = nr, nc, ld, co, vo
+            d.phi1_offset, d.phi2_offset, d.step_size = o1, o2, st
+        self.device = c.device
+        with torch.cuda.device(c.device):
+            self.nbytes = int(lib().drot_qr_adjoint_workspace_bytes(n, self.arr))
+            if self.nbytes == 0:
+                raise RuntimeError("drot_qr_adjoint_workspace_bytes: unsupported shapes")
+            self.ws = torch.empty(self.nbytes + 256, dtype=torch.uint8, device=c.device)
+            self.ptr = self.ws.data_ptr() + (-self.ws.data_ptr()) % 256
+            self.mask = torch.zeros(c.shape, dtype=torch.uint8, device=c.device)
+            rc = lib().drot_qr_adjoint_prepare(
+                n, self.arr, c.data_ptr(), C_BF16 if c.dtype == torch.bfloat16 else C_F32,
+                phi1.data_ptr(), phi2.data_ptr(), self.mask.data_ptr(), self.ptr, self.nbytes,
+                torch.cuda.current_stream(c.device).cuda_stream)
+        check(rc, "qr_adjoint_prepare")
+        self.mask = self.mask.bool()
+
+    def solve(self, rhs, tol, max_iters):
+        z = torch.empty_like(rhs)
+        iters = (ctypes.c_int * self.n)()
+        with torch.cuda.device(self.device):
+            rc = lib().drot_qr_adjoint_solve(self.n, self.arr, rhs.data_ptr(), z.data_ptr(),
+                                             float(tol), int(max_iters), self.ptr, self.nbytes,
+                                             iters, torch.cuda.current_stream(self.device).cuda_stream)
+        check(rc, "qr_adjoint_solve")
+        return z, list(iters)
+
+
+def _grads_from_z(G, mask, a, b, lam):
+    """dL/dC (implicit part), dL/dp, dL/dq of one instance ([n_cols, n_rows] layout)."""
+    t = (b.sum() - a.sum()) / (a.numel() + b.numel())
+    a = a + t
+    b = b - t
+    gc = torch.where(mask, (a[None, :] + b[:, None] - G) / lam, torch.zeros((), device=G.device))
+    return gc, a, b
+
+
+class QuadraticDROTFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, c, p, q, rho, r_weight, max_iters, eps, cg_tol, cg_max_iters):
+        from . import _check_input, _check_shapes, DrotResult
+        _check_input(c, "c", allow_bf16=True)
+        for t, n in ((p, "p"), (q, "q")):
+            _check_input(t, n)
+        nr, nc = _check_shapes(c, p, q)
+        s, kappa = step_and_kappa(rho, r_weight, nr, nc)
+        dev = c.device
+        x = torch.empty(c.shape, dtype=torch.float32, device=dev)
+        a = torch.empty(nr, device=dev)
+        b = torch.empty(nc, device=dev)
+        phi1 = torch.empty(nr, device=dev)
+        phi2 = torch.empty(nc, device=dev)
+        alpha = torch.empty(1, device=dev)
+        res = DrotResult()
+        with torch.cuda.device(dev):
+            st = torch.cuda.current_stream(dev).cuda_stream
+            check(lib().drot_init_state(nr, nc, s, 1, p.data_ptr(), q.data_ptr(), x.data_ptr(),
+                                        a.data_ptr(), b.data_ptr(), phi1.data_ptr(),
+                                        phi2.data_ptr(), alpha.data_ptr(), st), "init_state")
+            nbytes = int(lib().drot_qr_workspace_bytes(nr, nc))
+            ws = torch.empty(nbytes + 256, dtype=torch.uint8, device=dev)
+            wptr = ws.data_ptr() + (-ws.data_ptr()) % 256
+            check(lib().drot_qr_solve_ex(c.data_ptr(), C_BF16 if c.dtype == torch.bfloat16 else C_F32,
+                                         p.data_ptr(), q.data_ptr(), nr, nc, s, kappa,
+                                         int(max_iters), float(eps), x.data_ptr(), a.data_ptr(),
+                                         b.data_ptr(), phi1.data_ptr(), phi2.data_ptr(),
+                                         alpha.data_ptr(), wptr, nbytes, ctypes.byref(res), st),
+                  "qr_solve")
+        info = res.as_dict()
+        if not info["converged"]:
+            warnings.warn("quadratic_drot_fn: the solve did not converge; the implicit "
+                          "gradient assumes the optimal plan")
+        ctx.save_for_backward(c, phi1, phi2)
+        ctx.meta = (nr, nc, s, (kappa - 1.0) / s)
+        ctx.cg = (cg_tol, cg_max_iters)
+        ctx.info = info
+        return x
+
+    @staticmethod
+    def backward(ctx, gx):
+        c, phi1, phi2 = ctx.saved_tensors
+        nr, nc, s, lam = ctx.meta
+        G = gx.detach().float().contiguous()
+        adj = _Adjoint(c.detach(), phi1, phi2, [(nr, nc, nr, 0, 0, 0, 0, s)])
+        Gm = G * adj.mask
+        rhs = torch.cat([Gm.sum(0), Gm.sum(1)]).contiguous()
+        z, iters = adj.solve(rhs, *ctx.cg)
+        ctx.cg_iters = iters
+        gc, a, b = _grads_from_z(G, adj.mask, z[:nr], z[nr:], lam)
+        return gc.to(c.dtype), a, b, None, None, None, None, None, None
+
+
+def quadratic_drot_fn(c, p, q, rho, r_weight, max_iters, eps, *, cg_tol=CG_TOL,
+                      cg_max_iters=CG_MAX_ITERS):
+    """reg_drot.quadratic_drot with a backward (implicit adjoint)."""
+    if not r_weight > 0:
+        raise RuntimeError("quadratic_drot_fn needs r_weight > 0 (the gradient divides by lambda)")
+    return QuadraticDROTFn.apply(c, p, q, float(rho), float(r_weight), int(max_iters), float(eps),
+                                 float(cg_tol), int(cg_max_iters))
+
+
+class BatchQuadraticDROTFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, c, p, q, batch, max_iters, cg_tol, cg_max_iters):
+        x, info = batch.solve(c.detach(), p.detach(), q.detach(), max_iters)
+        if not all(r["converged"] for r in info):
+            warnings.warn("batch_quadratic_drot_fn: some instances did not converge; the "
+                          "implicit gradient assumes optimal plans")
+        phi1, phi2 = batch.duals()
+        ctx.save_for_backward(c, phi1, phi2)
+        ctx.batch = batch
+        ctx.cg = (cg_tol, cg_max_iters)
+        ctx.info = info
+        return x
+
+    @staticmethod
+    def backward(ctx, gx):
+        c, phi1, phi2 = ctx.saved_tensors
+        B = ctx.batch
+        G = gx.detach().float().contiguous()
+        steps = B.step_sizes()
+        descs, vo, prow, pcol = [], 0, 0, 0
+        for k, (nr, nc) in enumerate(B.shapes):
+            descs.append((nr, nc, B.lds[k], B.offsets[k], vo, prow, pcol, steps[k]))
+            vo += nr + nc
+            prow += nr
+            pcol += nc
+        adj = _Adjoint(c.detach(), phi1, phi2, descs)
+        rhs_parts = []
+        for k in range(B.n):
+            Gm = B.view(G, k) * B.view(adj.mask, k)
+            rhs_parts += [Gm.sum(0), Gm.sum(1)]
+        rhs = torch.cat(rhs_parts).contiguous()
+        z, iters = adj.solve(rhs, *ctx.cg)
+        ctx.cg_iters = iters
+        gc = torch.zeros_like(G)
+        gp, gq = [], []
+        for k, (nr, nc) in enumerate(B.shapes):
+            vo = descs[k][4]
+            lam = (step_and_kappa(B.rho[k], B.r_weight[k], nr, nc)[1] - 1.0) / steps[k]
+            g, a, b = _grads_from_z(B.view(G, k), B.view(adj.mask, k), z[vo:vo + nr],
+                                    z[vo + nr:vo + nr + nc], lam)
+            B.view(gc, k).copy_(g)
+            gp.append(a)
+            gq.append(b)
+        return gc.to(c.dtype), torch.cat(gp), torch.cat(gq), None, None, None, None
+
+
+def batch_quadratic_drot_fn(batch, c, p, q, max_iters, *, cg_tol=CG_TOL,
+                            cg_max_iters=CG_MAX_ITERS):
+    """QRBatch.solve with a backward; c, p, q packed (QRBatch.pack_c /
+    pack_marginals), returns the packed plans (QRBatch.unpack gives views)."""
+    if not all(r > 0 for r in batch.r_weight):
+        raise RuntimeError("batch_quadratic_drot_fn needs r_weight > 0 for every instance")
+    return BatchQuadraticDROTFn.apply(c, p, q, batch, int(max_iters), float(cg_tol),
+                                      int(cg_max_iters))
+
+
+__all__ = ["quadratic_drot_fn", "batch_quadratic_drot_fn", "qr_lambda", "step_and_kappa"]

@@ -80,6 +80,7 @@ class QRBatch:
         self.total = off
         self.total_rows, self.total_cols = prow, pcol
         self._desc = desc
+        self.rho, self.r_weight, self.eps = rho, r_weight, eps
         self._plans = {}
         self._ws = None
         self._ws_plan = None
@@ -179,9 +180,28 @@ class QRBatch:
         check(rc, "batch_results")
         return [{name: getattr(r, name) for name, _ in r._fields_} for r in out]
 
+    def duals(self):
+        """(phi1, phi2) after the last launch: copies of the packed final duals
+        (instance k's rows / columns at its p / q offsets)."""
+        h, ptr, _ = self.workspace_for(self._ws_plan or self.cols_per_tile or 128)
+        f1, f2 = ctypes.c_void_p(), ctypes.c_void_p()
+        check(lib().drot_batch_state(h, ptr, ctypes.byref(f1), ctypes.byref(f2)), "batch_state")
+        base = self._ws.data_ptr()
+        o1, o2 = f1.value - base, f2.value - base
+        phi1 = self._ws[o1:o1 + 4 * self.total_rows].view(torch.float32).clone()
+        phi2 = self._ws[o2:o2 + 4 * self.total_cols].view(torch.float32).clone()
+        return phi1, phi2
+
+    def step_sizes(self):
+        """s = rho / (n_rows + n_cols) of every instance (FP32, as the solver)."""
+        import numpy as np
+        return [float(np.float32(r) / (np.float32(nr) + np.float32(nc)))
+                for r, (nr, nc) in zip(self.rho, self.shapes)]
+
     def autotune(self, c, p, q, iters=40, candidates=TILE_CANDIDATES):
         """Times ``iters`` iterations per tile width on the caller's data and
-        keeps the fastest (the candidates give identical results)."""
+        keeps the fastest (the widths differ only in the order of the FP32
+        partial sums)."""
         x = self.empty_x()
         best = None
         for cpt in candidates:
