@@ -364,6 +364,31 @@ int drot_qr_adjoint_solve(int n_inst, const drot_adjoint_instance *inst,
                           void *workspace, size_t workspace_bytes, int *iters,
                           drot_stream_t stream);
 
+/* ---------------------------------------------------------------------------
+ * Cost matrices of point clouds (tensor cores)
+ *
+ * No counterpart in the reference, whose callers build C on the host
+ * (benchmark/utils/compute_w2_dist.py:68-94).  For each instance, points
+ * x (m x dim) and y (n x dim), row-major float32:
+ *     C[c_offset + j*ld + i] = scale * max(|x_i|^2 + |y_j|^2 - 2 <x_i, y_j>, 0)
+ * (no max when clamp == 0): the column-major m x n cost the solvers read.
+ * The Gram term runs on the tcgen05 tensor cores in split TF32 ("3xTF32",
+ * FP32-level accuracy); norms are FP32.  dim: 8, 16, 24 or 32.
+ * ------------------------------------------------------------------------- */
+
+/* x_offset / y_offset: index of the instance's first point in x / y;
+ * c_offset: element offset of its C block (leading dimension ld >= m). */
+typedef struct {
+  int m, n, ld, pad;
+  long long x_offset, y_offset, c_offset;
+} drot_cost_instance;
+
+/* Up to 256 instances per call (x, y 16-byte aligned).  Synchronises
+ * `stream` (it reads back the kernel's error flag). */
+int drot_sqeuclidean_cost(int n_inst, const drot_cost_instance *inst,
+                          const float *x, const float *y, int dim, float scale,
+                          int clamp, float *c, drot_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

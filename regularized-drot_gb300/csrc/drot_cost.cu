@@ -1,0 +1,307 @@
+// drot_cost.cu -- squared-Euclidean cost matrices of point clouds on the
+// 5th-generation tensor cores (tcgen05.mma kind::tf32, accumulator in TMEM).
+//
+// No counterpart in the reference, whose callers build C on the host
+// (benchmark/utils/compute_w2_dist.py:68-94) and hand it to the solver.  For
+// point clouds x (m x d) and y (n x d), row-major:
+//     C[j*ld + i] = scale * max(||x_i||^2 + ||y_j||^2 - 2 <x_i, y_j>, 0)
+// i.e. the column-major m x n cost the solver reads (the reference's PyTorch
+// layout [n, m]).  The Gram term is one GEMM with K = d, done in "3xTF32":
+// x = x_hi + x_lo with x_hi = RN_tf32(x), x_lo = RN_tf32(x - x_hi) (same
+// for y), <x, y> ~ x_hi.y_hi + x_hi.y_lo + x_lo.y_hi accumulated in FP32 --
+// the split-precision scheme that gives FP32-level accuracy on TF32 tensor
+// cores (the dropped x_lo.y_lo term is below 2^-22 relative).  Norms are
+// FP32 FMA sums in k order.
+//
+// One CTA per 128 x 256 tile: 4 warps stage the hi / lo operand tiles in
+// shared memory (K-major, no swizzle: 8-row x 16-byte core matrices), one
+// thread issues 3 * d/8 MMAs into a 128-lane x 256-column TMEM accumulator,
+// a tcgen05.commit arrives on an mbarrier, then each warp reads its 32 TMEM
+// lanes (tcgen05.ld 32x32b) and writes its rows of every column (128 bytes
+// per warp store).  The kernel is bound by the C stores (4 bytes per element).
+#include <cuda_runtime.h>
+
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "drot_gb300.h"
+#include "drot_kernels.cuh"
+
+namespace drot {
+
+constexpr int kCostM = 128;        // tile rows (x points) = TMEM lanes
+constexpr int kCostN = 256;        // tile columns (y points) = TMEM columns
+constexpr int kCostMaxInst = 256;  // instances per launch (descriptors travel in the parameters)
+constexpr int kCostThreads = 128;
+
+struct CostInst {
+  long long x_off, y_off, c_off;  // element offsets: x (m x d), y (n x d), C (ld x n)
+  int m, n, ld, tiles_m, tiles;
+  int pad;
+};
+
+struct CostParams {
+  const float* x;
+  const float* y;
+  float* c;
+  int* err;
+  long long timeout_ns;
+  int dim, n_inst, clamp, pad;
+  float scale, pad2;
+  CostInst inst[kCostMaxInst];
+};
+
+__device__ __forceinline__ uint32_t to_tf32(float v) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+  return r;
+}
+
+// Shared-memory matrix descriptor (tcgen05): start address, leading byte
+// offset (between core matrices along K), stride byte offset (between 8-row
+// groups), descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// Instruction descriptor of kind::tf32: D F32, A and B TF32, both K-major,
+// N >> 3 at bit 17, M >> 4 at bit 24.
+constexpr uint32_t kCostIdesc = (1u << 4) | (2u << 7) | (2u << 10) |
+                                ((uint32_t)(kCostN >> 3) << 17) | ((uint32_t)(kCostM >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+      :: "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kCostIdesc), "r"(accumulate) : "memory");
+}
+
+// Byte offset of element (r, k) of a K-major tile with kc = d / 4 core
+// matrices per 8-row group.
+__device__ __forceinline__ uint32_t kmaj_off(int r, int k, int kc) {
+  return (uint32_t)((((r >> 3) * kc + (k >> 2)) << 7) + ((r & 7) << 4) + ((k & 3) << 2));
+}
+
+__global__ void __launch_bounds__(kCostThreads) cost_sqeuclid_kernel(const __grid_constant__ CostParams P) {
+  const int k = blockIdx.y;
+  if (k >= P.n_inst) return;
+  const CostInst& I = P.inst[k];
+  const int t = blockIdx.x;
+  if (t >= I.tiles) return;
+  const int i0 = (t % I.tiles_m) * kCostM;
+  const int j0 = (t / I.tiles_m) * kCostN;
+  const int d = P.dim, kc = d >> 2;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const uint32_t a_bytes = (uint32_t)kCostM * d * 4, b_bytes = (uint32_t)kCostN * d * 4;
+  unsigned char* a_hi = smem;
+  unsigned char* a_lo = a_hi + a_bytes;
+  unsigned char* b_hi = a_lo + a_bytes;
+  unsigned char* b_lo = b_hi + b_bytes;
+  float* xn = reinterpret_cast<float*>(b_lo + b_bytes);
+  float* yn = xn + kCostM;
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t s_tmem;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 :: "r"(smem_u32(&s_tmem)), "r"((uint32_t)kCostN) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    mbar_init(&mbar, 1);
+    fence_mbar_init();
+  }
+
+  // Stage x rows (one per thread) and y rows (two per thread): hi / lo TF32
+  // parts in the K-major layout, FP32 norms.
+  {
+    const int r = tid;
+    const int i = i0 + r;
+    float nrm = 0.0f;
+    for (int c4 = 0; c4 < kc; ++c4) {
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (i < I.m) v = __ldg(reinterpret_cast<const float4*>(P.x + I.x_off + (long long)i * d) + c4);
+      const float e[4] = {v.x, v.y, v.z, v.w};
+      uint32_t hi[4], lo[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        hi[q] = to_tf32(e[q]);
+        lo[q] = to_tf32(e[q] - __uint_as_float(hi[q]));
+        nrm = fmaf(e[q], e[q], nrm);
+      }
+      const uint32_t off = kmaj_off(r, c4 * 4, kc);
+      *reinterpret_cast<uint4*>(a_hi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+      *reinterpret_cast<uint4*>(a_lo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    }
+    xn[r] = nrm;
+  }
+  for (int r = tid; r < kCostN; r += kCostThreads) {
+    const int j = j0 + r;
+    float nrm = 0.0f;
+    for (int c4 = 0; c4 < kc; ++c4) {
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (j < I.n) v = __ldg(reinterpret_cast<const float4*>(P.y + I.y_off + (long long)j * d) + c4);
+      const float e[4] = {v.x, v.y, v.z, v.w};
+      uint32_t hi[4], lo[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        hi[q] = to_tf32(e[q]);
+        lo[q] = to_tf32(e[q] - __uint_as_float(hi[q]));
+        nrm = fmaf(e[q], e[q], nrm);
+      }
+      const uint32_t off = kmaj_off(r, c4 * 4, kc);
+      *reinterpret_cast<uint4*>(b_hi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+      *reinterpret_cast<uint4*>(b_lo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    }
+    yn[r] = nrm;
+  }
+  fence_proxy_async_shared();  // generic-proxy smem writes -> visible to the tensor core
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = s_tmem;
+
+  if (tid == 0) {
+    const uint32_t sbo = (uint32_t)kc * 128u;
+    const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
+    const uint32_t bh = smem_u32(b_hi), bl = smem_u32(b_lo);
+    const int ks_n = d >> 3;  // K = 8 per kind::tf32 MMA = 2 core matrices
+    for (int ks = 0; ks < ks_n; ++ks)
+      mma_tf32(tmem, smem_desc(ah + ks * 256, 128, sbo), smem_desc(bh + ks * 256, 128, sbo),
+               ks > 0 ? 1u : 0u);
+    for (int ks = 0; ks < ks_n; ++ks)
+      mma_tf32(tmem, smem_desc(ah + ks * 256, 128, sbo), smem_desc(bl + ks * 256, 128, sbo), 1u);
+    for (int ks = 0; ks < ks_n; ++ks)
+      mma_tf32(tmem, smem_desc(al + ks * 256, 128, sbo), smem_desc(bh + ks * 256, 128, sbo), 1u);
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 :: "r"(smem_u32(&mbar)) : "memory");
+  }
+  bool ok = mbar_wait(&mbar, 0, P.timeout_ns);
+  if (!ok) {
+    atomicExch(P.err, 1);
+    ok = false;
+    mbar_wait(&mbar, 0, P.timeout_ns);  // give the MMAs a second bounded chance to land
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+  // Epilogue: warp w owns TMEM lanes 32w..32w+31 = rows i0 + 32w + lane.
+  const int i = i0 + warp * 32 + lane;
+  const float xi = xn[warp * 32 + lane];
+  float* crow = P.c + I.c_off + i;
+  for (int cb = 0; cb < kCostN; cb += 32) {
+    uint32_t r[32];
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+          "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+          "=r"(r[31])
+        : "r"(taddr) : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    if (ok && i < I.m) {
+#pragma unroll
+      for (int e = 0; e < 32; ++e) {
+        const int j = j0 + cb + e;
+        if (j < I.n) {
+          float v = fmaf(-2.0f, __uint_as_float(r[e]), xi + yn[cb + e]);
+          if (P.clamp) v = fmaxf(v, 0.0f);
+          crow[(long long)j * I.ld] = v * P.scale;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                 :: "r"(tmem), "r"((uint32_t)kCostN) : "memory");
+}
+
+static size_t cost_smem_bytes(int dim) {
+  return (size_t)(kCostM + kCostN) * dim * 4 * 2 + sizeof(float) * (kCostM + kCostN);
+}
+
+}  // namespace drot
+
+using namespace drot;
+
+extern "C" {
+
+int drot_sqeuclidean_cost(int n_inst, const drot_cost_instance* inst, const float* x,
+                          const float* y, int dim, float scale, int clamp, float* c,
+                          drot_stream_t stream) {
+  if (n_inst <= 0 || n_inst > kCostMaxInst || !inst || !x || !y || !c) return DROT_ERR_INVALID_ARG;
+  if (dim <= 0 || dim > 32 || (dim & 7) != 0) return DROT_ERR_UNSUPPORTED;
+  if (((uintptr_t)x & 15u) || ((uintptr_t)y & 15u)) return DROT_ERR_INVALID_ARG;
+  // The parameter block (descriptors included) is about 12 KB: kept off the
+  // stack, filled and launched under a lock (launch copies it).
+  static CostParams P;
+  static int* err_flag[64] = {};
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return DROT_ERR_CUDA;
+  if (!err_flag[dev] && cudaMalloc(&err_flag[dev], sizeof(int)) != cudaSuccess) return DROT_ERR_CUDA;
+  int* err = err_flag[dev];
+  memset(&P, 0, sizeof(P));
+  int max_tiles = 0;
+  for (int k = 0; k < n_inst; ++k) {
+    const drot_cost_instance& a = inst[k];
+    if (a.m <= 0 || a.n <= 0 || a.ld < a.m || a.x_offset < 0 || a.y_offset < 0 ||
+        a.c_offset < 0 || ((a.x_offset * dim) & 3) || ((a.y_offset * dim) & 3))
+      return DROT_ERR_INVALID_ARG;
+    CostInst& I = P.inst[k];
+    I.x_off = a.x_offset * dim;
+    I.y_off = a.y_offset * dim;
+    I.c_off = a.c_offset;
+    I.m = a.m;
+    I.n = a.n;
+    I.ld = a.ld;
+    I.tiles_m = (a.m + kCostM - 1) / kCostM;
+    const long long tiles = (long long)I.tiles_m * ((a.n + kCostN - 1) / kCostN);
+    if (tiles > 65535LL * 1024) return DROT_ERR_UNSUPPORTED;
+    I.tiles = (int)tiles;
+    max_tiles = std::max(max_tiles, I.tiles);
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  P.x = x;
+  P.y = y;
+  P.c = c;
+  P.err = err;
+  P.timeout_ns = 2000000000LL;
+  P.dim = dim;
+  P.n_inst = n_inst;
+  P.clamp = clamp ? 1 : 0;
+  P.scale = scale;
+  const size_t smem = cost_smem_bytes(dim);
+  if (cudaFuncSetAttribute((const void*)cost_sqeuclid_kernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return DROT_ERR_CUDA;
+  if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) return DROT_ERR_CUDA;
+  cost_sqeuclid_kernel<<<dim3(max_tiles, n_inst), kCostThreads, smem, st>>>(P);
+  if (cudaGetLastError() != cudaSuccess) return DROT_ERR_CUDA;
+  int h_err = 0;
+  if (cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return DROT_ERR_CUDA;
+  return h_err ? DROT_ERR_BARRIER_TIMEOUT : DROT_OK;
+}
+
+}  // extern "C"

@@ -68,6 +68,17 @@ class DrotAdjointInstance(ctypes.Structure):
 
 
 _AIP = ctypes.POINTER(DrotAdjointInstance)
+
+
+class DrotCostInstance(ctypes.Structure):
+    _fields_ = [
+        ("m", ctypes.c_int), ("n", ctypes.c_int), ("ld", ctypes.c_int), ("pad", ctypes.c_int),
+        ("x_offset", ctypes.c_longlong), ("y_offset", ctypes.c_longlong),
+        ("c_offset", ctypes.c_longlong),
+    ]
+
+
+_CIP = ctypes.POINTER(DrotCostInstance)
 _BIP = ctypes.POINTER(DrotBatchInstance)
 _BRP = ctypes.POINTER(DrotBatchResult)
 
@@ -127,6 +138,8 @@ SIGNATURES = {
                                          _c_size, _vp]),
     "drot_qr_adjoint_solve": (_c_int, [_c_int, _AIP, _vp, _vp, _c_float, _c_int, _vp, _c_size,
                                        _ip, _vp]),
+    "drot_sqeuclidean_cost": (_c_int, [_c_int, _CIP, _vp, _vp, _c_int, _c_float, _c_int, _vp,
+                                       _vp]),
 }
 
 _lib = None

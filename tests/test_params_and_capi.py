@@ -176,3 +176,16 @@ def test_batch_plan_rejects_bad_descriptors_on_the_host(solver_lib):
     solver_lib.drot_batch_plan_destroy(None)
     assert solver_lib.drot_qr_batch_launch(None, None, 0, None, None, None, 10, None, 0,
                                            None) == 1
+
+
+def test_cost_and_adjoint_reject_bad_arguments_on_the_host(solver_lib):
+    from reg_drot._lib import DrotAdjointInstance, DrotCostInstance
+    arr = (DrotCostInstance * 1)()
+    arr[0].m, arr[0].n, arr[0].ld = 10, 10, 10
+    assert solver_lib.drot_sqeuclidean_cost(0, arr, None, None, 16, 1.0, 1, None, None) == 1
+    assert solver_lib.drot_sqeuclidean_cost(1, arr, 4, 16, 16, 1.0, 1, 16, None) == 1  # x misaligned
+    assert solver_lib.drot_sqeuclidean_cost(1, arr, 16, 16, 12, 1.0, 1, 16, None) == 4  # dim 12
+    adj = (DrotAdjointInstance * 1)()
+    adj[0].n_rows, adj[0].n_cols, adj[0].ld, adj[0].step_size = 10, 10, 9, 0.1
+    assert solver_lib.drot_qr_adjoint_workspace_bytes(1, adj) == 0  # ld < n_rows
+    assert solver_lib.drot_qr_adjoint_solve(1, adj, None, None, 1e-6, 10, None, 0, None, None) == 1
