@@ -386,6 +386,119 @@ def batched_point(dev, flush, single_sample=16):
     return out
 
 
+DIFF_INSTANCES = 64
+DIFF_MIN, DIFF_MAX = 512, 4096
+DIFF_DIM = 16
+DIFF_SCALE = 1.0 / (4 * DIFF_DIM)  # C = |x - y|^2 / 64: mean cost 0.5 for N(0, I_16) clouds
+
+
+def differentiable_point(dev, n_inst=DIFF_INSTANCES, gl_inst=4, single_sample=8, gl_iters=500):
+    """Differentiable OT loss: point clouds x_k (m x 16), y_k (n x 16) ~ N(0, 1),
+    m, n ~ U{512..4096}; C_k = |x - y|^2 / 64 on the tensor cores; loss =
+    sum_k <C_k, X_k*> + w ||X_k*||_F^2 (w fixed random); one step = cost +
+    batched QR solve (relative eps 1e-4, alpha 1e-3) + backward (implicit
+    adjoint + cost chain rule) for all instances.  GL part: the same loss with
+    the group-lasso plan (2 classes, lambda weight 1e-3) and the checkpointed
+    unrolled adjoint on the first `gl_inst` instances, `gl_iters` iterations
+    each (the GL solve does not reach the relative 1e-4 stop on these clouds
+    within 20000 iterations; the adjoint's cost is linear in the iterations)."""
+    import torch
+    import reg_drot
+    from reg_drot.autograd import batch_quadratic_drot_fn, group_lasso_drot_fn
+    from reg_drot.batch import QRBatch
+    from reg_drot.cost import packed_sqeuclidean_cost, sqeuclidean_cost
+    rng = np.random.default_rng(SEED + 5)
+    shapes = [(int(a), int(b)) for a, b in rng.integers(DIFF_MIN, DIFF_MAX + 1, size=(n_inst, 2))]
+    g = torch.Generator(device=dev).manual_seed(SEED + 5)
+    x_cat = torch.randn(sum(m for m, _ in shapes), DIFF_DIM, generator=g, device=dev,
+                        requires_grad=True)
+    y_cat = torch.randn(sum(n for _, n in shapes), DIFF_DIM, generator=g, device=dev,
+                        requires_grad=True)
+    w = float(torch.rand(1, generator=torch.Generator().manual_seed(SEED)).item())
+    eps = [REL_EPS * math.sqrt(1.0 / m + 1.0 / n) for m, n in shapes]
+    B = QRBatch(shapes, RHO, ALPHA, eps, device=dev)
+    p, q = B.pack_marginals([torch.full((m,), 1.0 / m) for m, _ in shapes],
+                            [torch.full((n,), 1.0 / n) for _, n in shapes])
+    with torch.no_grad():
+        B.autotune(packed_sqeuclidean_cost(B, x_cat, y_cat, DIFF_SCALE), p, q, iters=100)
+
+    def ev():
+        e = torch.cuda.Event(enable_timing=True)
+        e.record()
+        return e
+
+    def step():
+        x_cat.grad = None
+        y_cat.grad = None
+        e0 = ev()
+        c = packed_sqeuclidean_cost(B, x_cat, y_cat, DIFF_SCALE)
+        e1 = ev()
+        X = batch_quadratic_drot_fn(B, c, p, q, 10 ** 6)
+        e2 = ev()
+        loss = (c * X).sum() + w * (X * X).sum()
+        loss.backward()
+        e3 = ev()
+        e3.synchronize()
+        return (e0.elapsed_time(e1) / 1e3, e1.elapsed_time(e2) / 1e3, e2.elapsed_time(e3) / 1e3,
+                X.grad_fn, float(loss.detach()))
+
+    step()  # warm-up
+    t_cost, t_fwd, t_bwd, fn, loss = step()
+    it = np.array([r["n_iter"] for r in fn.info])
+    total = t_cost + t_fwd + t_bwd
+    out = {"workload": (f"differentiable QR-DROT loss, {n_inst} instances, m,n ~ U{{{DIFF_MIN}..{DIFF_MAX}}}, "
+                        f"x,y ~ N(0,I_{DIFF_DIM}), C = |x-y|^2/64 (tcgen05 split-TF32 GEMM), "
+                        f"alpha={ALPHA}, relative eps {REL_EPS}, loss = sum <C,X*> + w|X*|^2"),
+           "elements": int(sum(m * n for m, n in shapes)),
+           "qr": {"s_per_step": total, "solves_with_grad_per_s": n_inst / total,
+                  "cost_s": t_cost, "forward_s": t_fwd, "backward_s": t_bwd,
+                  "converged": int(sum(r["converged"] for r in fn.info)),
+                  "n_iter_min_median_max": [int(it.min()), float(np.median(it)), int(it.max())],
+                  "cg_iters_min_median_max": [int(min(fn.cg_iters)), float(np.median(fn.cg_iters)),
+                                              int(max(fn.cg_iters))],
+                  "loss": loss}}
+    # plain per-instance FP32 solves, forward only (sample)
+    ks = list(range(0, n_inst, max(1, n_inst // single_sample)))
+    t_single = 0.0
+    with torch.no_grad():
+        for k in ks:
+            m, n = shapes[k]
+            xo = sum(a for a, _ in shapes[:k])
+            yo = sum(b for _, b in shapes[:k])
+            ck = sqeuclidean_cost(x_cat[xo:xo + m].detach(), y_cat[yo:yo + n].detach(), DIFF_SCALE)
+            pk, qk = torch.full((m,), 1.0 / m, device=dev), torch.full((n,), 1.0 / n, device=dev)
+            xk, _, ws = reg_drot.solve_qr(ck, pk, qk, RHO, ALPHA, 10 ** 6, eps[k])
+            e0 = ev()
+            reg_drot.solve_qr(ck, pk, qk, RHO, ALPHA, 10 ** 6, eps[k], out=xk, workspace=ws)
+            e1 = ev()
+            e1.synchronize()
+            t_single += e0.elapsed_time(e1) / 1e3
+    out["per_instance_forward_only_solves_per_s"] = len(ks) / t_single
+    out["per_instance_sample"] = f"{len(ks)} instances, reg_drot.solve_qr forward only"
+    # GL with the unrolled adjoint, one instance at a time
+    gl_times, gl_iters_run = [], []
+    for k in range(gl_inst):
+        m, n = shapes[k]
+        xo = sum(a for a, _ in shapes[:k])
+        yo = sum(b for _, b in shapes[:k])
+        xk = x_cat[xo:xo + m].detach().clone().requires_grad_(True)
+        yk = y_cat[yo:yo + n].detach().clone().requires_grad_(True)
+        pk, qk = torch.full((m,), 1.0 / m, device=dev), torch.full((n,), 1.0 / n, device=dev)
+        for rep in range(2):
+            e0 = ev()
+            ck = sqeuclidean_cost(xk, yk, DIFF_SCALE)
+            Xk = group_lasso_drot_fn(ck, pk, qk, 2, RHO, ALPHA, gl_iters, eps[k])
+            ((ck * Xk).sum() + w * (Xk * Xk).sum()).backward()
+            e1 = ev()
+            e1.synchronize()
+        gl_times.append(e0.elapsed_time(e1) / 1e3)
+        gl_iters_run.append(Xk.grad_fn.info["n_iter"])
+    out["gl"] = {"instances": gl_inst, "s_per_instance_with_grad": statistics.mean(gl_times),
+                 "iterations": gl_iters_run, "segment": 32,
+                 "ms_per_iteration_with_grad": 1e3 * sum(gl_times) / sum(gl_iters_run)}
+    return out
+
+
 def run_gpu(args):
     import torch
     import reg_drot
@@ -461,7 +574,7 @@ def run_gpu(args):
 
     e2e = e2e_wrapper(c, p, q, eps, args.steps)
     extra = {"hbm_point": hbm_point(dev, flush), "gl_da": gl_da_point(dev),
-             "batched": batched_point(dev, flush)}
+             "batched": batched_point(dev, flush), "differentiable": differentiable_point(dev)}
     cpu = cpu_sample(budget_s=12.0) if world == 1 else None
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,

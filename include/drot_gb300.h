@@ -365,6 +365,29 @@ int drot_qr_adjoint_solve(int n_inst, const drot_adjoint_instance *inst,
                           drot_stream_t stream);
 
 /* ---------------------------------------------------------------------------
+ * Unrolled adjoint of the group-lasso iteration (autograd backward)
+ *
+ * No counterpart in the reference.  One GL iteration (core/drot_glr.hpp:
+ * 242-355) maps s_k = (X, phi1, phi2, a, b, alpha) to s_{k+1};
+ * drot_gl_adjoint_step applies the transposed Jacobian of that map: given
+ * X, phi1, phi2 of s_k (recomputed from a checkpoint) and the adjoint of
+ * s_{k+1} in xbar (n_rows x n_cols) and vbar ([phi1bar | phi2bar | abar |
+ * bbar | alphabar], 2*(n_rows + n_cols) + 1 floats), it overwrites them with
+ * the adjoint of s_k and adds the step's terms to cbar, pbar, qbar.
+ * step_size / lambda are the solve's s and group threshold (the lambda of
+ * drot_gl_solve).  Asynchronous (four kernels on `stream`).
+ * ------------------------------------------------------------------------- */
+
+size_t drot_gl_adjoint_workspace_bytes(int n_rows, int n_cols, int n_groups);
+
+int drot_gl_adjoint_step(const void *c, int c_dtype, int n_rows, int n_cols,
+                         int n_groups, float step_size, float lambda,
+                         const float *x, const float *phi1, const float *phi2,
+                         float *xbar, float *vbar, float *cbar, float *pbar,
+                         float *qbar, void *workspace, size_t workspace_bytes,
+                         drot_stream_t stream);
+
+/* ---------------------------------------------------------------------------
  * Cost matrices of point clouds (tensor cores)
  *
  * No counterpart in the reference, whose callers build C on the host

@@ -91,3 +91,46 @@ def point_grads(xs, yt, gc):
     gx = 2.0 * (xs * gc.sum(0)[:, None] - gc.T @ yt)
     gy = 2.0 * (yt * gc.sum(1)[:, None] - gc @ xs)
     return gx, gy
+
+
+def gl_unrolled(c, p, q, n_class, rho, r_weight, iters, norm_eps=1e-9):
+    """X after `iters` GL iterations from the warm start, in FP64 torch (CPU)
+    so that autograd gives the exact gradient of the unrolled map.  Restates
+    the oracle's GL loop (oracle_gl_solve: core/drot_glr.hpp:242-355,
+    kernel_glr.hpp:59-161, 461-526) with the operator's parameters
+    (pytorch/src/glr_drot_cuda_kernel.cu:255-257).  c, p, q: torch float64
+    tensors ([n_cols, n_rows], [n_rows], [n_cols])."""
+    import torch
+    nc, nr = c.shape
+    s = O.step_size(rho, nr, nc)
+    lam = O.gl_lambda(r_weight, nr, n_class, "torch")
+    w = O.warm_start(s, nr, nc)
+    bounds = [int(v) for v in O.group_bounds(nr, n_class)]
+    f64 = dict(dtype=torch.float64)
+    X = torch.zeros(nc, nr, **f64)
+    phi1 = torch.full((nr,), float(w["phi1"]), **f64)
+    phi2 = torch.full((nc,), float(w["phi2"]), **f64)
+    a = torch.full((nr,), float(w["a"]), **f64)
+    b = torch.full((nc,), float(w["b"]), **f64)
+    alpha = torch.tensor(float(w["alpha"]), **f64)
+    for _ in range(iters):
+        y = (X + phi1[None, :] + phi2[:, None] - s * c).clamp_min(0.0)
+        parts = []
+        for g in range(n_class):
+            yg = y[:, bounds[g]:bounds[g + 1]]
+            n2 = (yg * yg).sum(1)
+            pos = n2 > 0
+            n = torch.sqrt(torch.where(pos, n2, torch.ones_like(n2))) * pos
+            sig = (1.0 - lam / (n + norm_eps)).clamp_min(0.0)
+            parts.append(sig[:, None] * yg)
+        X = torch.cat(parts, 1)
+        r, cs_, sigma = X.sum(0), X.sum(1), X.sum()
+        gamma = (2.0 * (sigma - 1.0) - alpha) / (nr + nc)
+        rs = r - p
+        a = a - rs
+        phi1 = (a - rs + gamma) / nc
+        cs = cs_ - q
+        b = b - cs
+        phi2 = (b - cs + gamma) / nr
+        alpha = alpha + 1.0 - sigma
+    return X

@@ -2,8 +2,9 @@
 
 nvcc compiles the translation units csrc/drot_api.cu (single-instance
 solver and C ABI), csrc/drot_batch.cu (batched solver) and
-csrc/drot_adjoint.cu (implicit adjoint for autograd) and csrc/drot_cost.cu
-(tensor-core cost matrices) in parallel and links them into
+csrc/drot_adjoint.cu (implicit QR adjoint), csrc/drot_gl_adjoint.cu
+(unrolled GL adjoint) and csrc/drot_cost.cu (tensor-core cost matrices) in
+parallel and links them into
 reg_drot/libdrot_gb300.so, in tree.  Device code is compiled with
 --fmad=false: the kernels spell out every fused multiply-add they need
 (the ones the reference's kernels compile to), so nothing else is contracted.
@@ -22,7 +23,8 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 OUT = os.path.join(PKG, "reg_drot", "libdrot_gb300.so")
 SOURCES = [os.path.join(CSRC, f)
-           for f in ("drot_api.cu", "drot_batch.cu", "drot_adjoint.cu", "drot_cost.cu")]
+           for f in ("drot_api.cu", "drot_batch.cu", "drot_adjoint.cu", "drot_gl_adjoint.cu",
+                     "drot_cost.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))] + \
     [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
 

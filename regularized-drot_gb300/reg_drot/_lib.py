@@ -138,6 +138,9 @@ SIGNATURES = {
                                          _c_size, _vp]),
     "drot_qr_adjoint_solve": (_c_int, [_c_int, _AIP, _vp, _vp, _c_float, _c_int, _vp, _c_size,
                                        _ip, _vp]),
+    "drot_gl_adjoint_workspace_bytes": (_c_size, [_c_int, _c_int, _c_int]),
+    "drot_gl_adjoint_step": (_c_int, [_vp, _c_int, _c_int, _c_int, _c_int, _c_float, _c_float,
+                                      _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _c_size, _vp]),
     "drot_sqeuclidean_cost": (_c_int, [_c_int, _CIP, _vp, _vp, _c_int, _c_float, _c_int, _vp,
                                        _vp]),
 }

@@ -5,6 +5,11 @@ The reference's operators return plans without gradients
 
   quadratic_drot_fn(c, p, q, rho, r_weight, max_iters, eps)   -> x (differentiable)
   batch_quadratic_drot_fn(batch, c, p, q, max_iters)          -> packed x (differentiable)
+  group_lasso_drot_fn(c, p, q, n_class, rho, r_weight, max_iters, eps) -> x (differentiable)
+
+Group lasso: the gradient is the unrolled adjoint of the iterations the
+solve ran (drot_gl_adjoint_step, one reverse step per iteration), with the
+states recomputed segment by segment from checkpoints of the forward.
 
 Forward: the CUDA solver (single instance or QRBatch).  Backward: the
 implicit adjoint of the regularised problem
@@ -222,4 +227,135 @@ def batch_quadratic_drot_fn(batch, c, p, q, max_iters, *, cg_tol=CG_TOL,
                                       int(cg_max_iters))
 
 
-__all__ = ["quadratic_drot_fn", "batch_quadratic_drot_fn", "qr_lambda", "step_and_kappa"]
+def gl_step_and_lambda(rho, r_weight, n_rows, n_cols, n_class):
+    """s and the group threshold of the GL operator (glr_drot_cuda_kernel.cu:255-257)."""
+    import math
+    s = f32(rho) / (f32(n_rows) + f32(n_cols))
+    lam = f32(float(f32(r_weight)) * math.sqrt(n_rows // n_class))
+    return float(s), float(lam)
+
+
+class _GLState:
+    """Solver state (X, a, b, phi1, phi2, alpha) on the device and the
+    one-call GL solve from it (drot_gl_solve_ex: state in / state out)."""
+
+    def __init__(self, c, p, q, n_class, s, lam):
+        self.c, self.p, self.q, self.G, self.s, self.lam = c, p, q, n_class, s, lam
+        self.nc, self.nr = c.shape
+        dev = c.device
+        self.t = {"x": torch.empty(c.shape, dtype=torch.float32, device=dev),
+                  "a": torch.empty(self.nr, device=dev), "b": torch.empty(self.nc, device=dev),
+                  "phi1": torch.empty(self.nr, device=dev),
+                  "phi2": torch.empty(self.nc, device=dev),
+                  "alpha": torch.empty(1, device=dev)}
+        with torch.cuda.device(dev):
+            self.nbytes = int(lib().drot_gl_workspace_bytes(self.nr, self.nc, n_class))
+        if self.nbytes == 0:
+            raise RuntimeError("group_lasso_drot_fn: unsupported shape")
+        self.ws = torch.empty(self.nbytes + 256, dtype=torch.uint8, device=dev)
+        self.wptr = self.ws.data_ptr() + (-self.ws.data_ptr()) % 256
+
+    def stream(self):
+        return torch.cuda.current_stream(self.c.device).cuda_stream
+
+    def warm_start(self):
+        t = self.t
+        with torch.cuda.device(self.c.device):
+            check(lib().drot_init_state(self.nr, self.nc, self.s, 1, self.p.data_ptr(),
+                                        self.q.data_ptr(), t["x"].data_ptr(), t["a"].data_ptr(),
+                                        t["b"].data_ptr(), t["phi1"].data_ptr(),
+                                        t["phi2"].data_ptr(), t["alpha"].data_ptr(),
+                                        self.stream()), "init_state")
+
+    def run(self, iters, eps):
+        from . import DrotResult
+        t = self.t
+        res = DrotResult()
+        with torch.cuda.device(self.c.device):
+            check(lib().drot_gl_solve_ex(
+                self.c.data_ptr(), C_BF16 if self.c.dtype == torch.bfloat16 else C_F32,
+                self.p.data_ptr(), self.q.data_ptr(), self.nr, self.nc, self.G, self.s, self.lam,
+                int(iters), float(eps), t["x"].data_ptr(), t["a"].data_ptr(), t["b"].data_ptr(),
+                t["phi1"].data_ptr(), t["phi2"].data_ptr(), t["alpha"].data_ptr(), self.wptr,
+                self.nbytes, ctypes.byref(res), self.stream()), "gl_solve")
+        return res.as_dict()
+
+    def snapshot(self):
+        return {k: v.clone() for k, v in self.t.items()}
+
+    def restore(self, snap):
+        for k, v in snap.items():
+            self.t[k].copy_(v)
+
+
+class GroupLassoDROTFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, c, p, q, n_class, rho, r_weight, max_iters, eps, segment):
+        from . import _check_input, _check_shapes
+        _check_input(c, "c", allow_bf16=True)
+        for t, n in ((p, "p"), (q, "q")):
+            _check_input(t, n)
+        nr, nc = _check_shapes(c, p, q)
+        s, lam = gl_step_and_lambda(rho, r_weight, nr, nc, n_class)
+        st = _GLState(c.detach(), p.detach(), q.detach(), n_class, s, lam)
+        st.warm_start()
+        checkpoints, T, info = [], 0, None
+        while T < max_iters:
+            checkpoints.append(st.snapshot())
+            info = st.run(min(segment, max_iters - T), eps)
+            T += info["iters_run"]
+            if info["converged"] or info["iters_run"] == 0:
+                break
+        ctx.save_for_backward(c, p, q)
+        ctx.meta = (nr, nc, int(n_class), s, lam, int(segment), T)
+        ctx.checkpoints = checkpoints
+        ctx.info = dict(info, n_iter=T, iters_run=T)  # totals over the segments
+        return st.t["x"].clone()
+
+    @staticmethod
+    def backward(ctx, gx):
+        c, p, q = ctx.saved_tensors
+        nr, nc, G, s, lam, seg, T = ctx.meta
+        dev = c.device
+        st = _GLState(c.detach(), p.detach(), q.detach(), G, s, lam)
+        xbar = gx.detach().float().contiguous().clone()
+        vbar = torch.zeros(2 * (nr + nc) + 1, device=dev)
+        cbar = torch.zeros(c.shape, dtype=torch.float32, device=dev)
+        pbar = torch.zeros(nr, device=dev)
+        qbar = torch.zeros(nc, device=dev)
+        with torch.cuda.device(dev):
+            abytes = int(lib().drot_gl_adjoint_workspace_bytes(nr, nc, G))
+        if abytes == 0:
+            raise RuntimeError("group_lasso_drot_fn: shape unsupported by the adjoint")
+        aws = torch.empty(abytes + 256, dtype=torch.uint8, device=dev)
+        aptr = aws.data_ptr() + (-aws.data_ptr()) % 256
+        cdt = C_BF16 if c.dtype == torch.bfloat16 else C_F32
+        for si in reversed(range(len(ctx.checkpoints))):
+            k0 = si * seg
+            k1 = min(k0 + seg, T)
+            st.restore(ctx.checkpoints[si])
+            saved = []
+            for _ in range(k0, k1):  # recompute the segment's states
+                saved.append((st.t["x"].clone(), st.t["phi1"].clone(), st.t["phi2"].clone()))
+                st.run(1, -1.0)
+            for xk, f1k, f2k in reversed(saved):
+                with torch.cuda.device(dev):
+                    rc = lib().drot_gl_adjoint_step(
+                        c.data_ptr(), cdt, nr, nc, G, s, lam, xk.data_ptr(), f1k.data_ptr(),
+                        f2k.data_ptr(), xbar.data_ptr(), vbar.data_ptr(), cbar.data_ptr(),
+                        pbar.data_ptr(), qbar.data_ptr(), aptr, abytes, st.stream())
+                check(rc, "gl_adjoint_step")
+        return cbar.to(c.dtype), pbar, qbar, None, None, None, None, None, None
+
+
+def group_lasso_drot_fn(c, p, q, n_class, rho, r_weight, max_iters, eps, *, segment=32):
+    """reg_drot.group_lasso_drot with a backward: the unrolled adjoint of the
+    iterations the solve ran, recomputed from checkpoints taken every
+    ``segment`` iterations (memory: one state per segment plus ``segment``
+    plans during the backward)."""
+    return GroupLassoDROTFn.apply(c, p, q, int(n_class), float(rho), float(r_weight),
+                                  int(max_iters), float(eps), int(segment))
+
+
+__all__ = ["quadratic_drot_fn", "batch_quadratic_drot_fn", "group_lasso_drot_fn", "qr_lambda",
+           "step_and_kappa", "gl_step_and_lambda"]
