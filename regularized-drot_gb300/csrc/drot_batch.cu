@@ -225,6 +225,37 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
   }
 }
 
+// Line sums of `n` partial vectors of length `len` (partial c of line l at
+// base[c * len + l]) for lines threadIdx.x + k * blockDim.x.  A thread takes
+// 4 lines and issues the loads of 8 partials of each before adding any (one
+// L2 round trip per 32 loads instead of one per line); per line the
+// partials are added in index order.  use(l, sum) consumes each line.
+template <typename F>
+__device__ __forceinline__ void reduce_lines(const float* base, int len, int n, F&& use) {
+  const int nt = blockDim.x;
+  for (int l0 = threadIdx.x; l0 < len; l0 += 4 * nt) {
+    float s[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (int c0 = 0; c0 < n; c0 += 8) {
+      float v[4][8];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) {
+          const int l = l0 + u * nt, c = c0 + cc;
+          v[u][cc] = (l < len && c < n) ? __ldcg(base + (long long)c * len + l) : 0.0f;
+        }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc)
+          if (c0 + cc < n) s[u] += v[u][cc];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (l0 + u * nt < len) use(l0 + u * nt, s[u]);
+  }
+}
+
 template <typename CT>
 __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P) {
   constexpr int VEC = 4, KV = kBatchKV, S = kBatchS;
@@ -348,28 +379,20 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       if (threadIdx.x == 0) P.alpha[k] = (float)(((double)alpha + 1.0) - (double)sigma);
       double res = 0.0;
       const float ncf = (float)I.nc, nrf = (float)I.nr;
-      for (int i = threadIdx.x; i < I.nr; i += blockDim.x) {
-        const float* rp = P.rowpart + I.rp_off + i;
-        float r = 0.0f;
-#pragma unroll 8
-        for (int c = 0; c < I.P; ++c) r += __ldcg(rp + (long long)c * I.nr);
+      reduce_lines(P.rowpart + I.rp_off, I.nr, I.P, [&](int i, float r) {
         const float rs = r - __ldg(P.p + I.p_off + i);
         const float ab = P.a[I.row_off + i] - rs;
         P.phi1[I.row_off + i] = div_rn_by((ab - rs) + gamma, ncf, I.nc_rcp);
         P.a[I.row_off + i] = ab;
         res = fma((double)rs, (double)rs, res);
-      }
-      for (int j = threadIdx.x; j < I.nc; j += blockDim.x) {
-        const float* cp = P.colpart + I.cp_off + j;
-        float cs_ = 0.0f;
-#pragma unroll 4
-        for (int bnd = 0; bnd < I.nbands; ++bnd) cs_ += __ldcg(cp + (long long)bnd * I.nc);
+      });
+      reduce_lines(P.colpart + I.cp_off, I.nc, I.nbands, [&](int j, float cs_) {
         const float cs = cs_ - __ldg(P.q + I.q_off + j);
         const float ab = P.b[I.col_off + j] - cs;
         P.phi2[I.col_off + j] = div_rn_by((ab - cs) + gamma, nrf, I.nr_rcp);
         P.b[I.col_off + j] = ab;
         res = fma((double)cs, (double)cs, res);
-      }
+      });
       res = block_sum_d(res, dscr);
       if (threadIdx.x == 0) {
         BatchStat st = P.stats[k];
