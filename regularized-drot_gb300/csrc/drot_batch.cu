@@ -5,11 +5,15 @@
 // update every CTA takes tiles from a per-iteration atomic counter until the
 // list is exhausted (instances of very different sizes balance out), and
 // every tile writes its own partial-sum slots, so the sums do not depend on
-// which CTA ran which tile (results are deterministic).  The dual update,
-// the stop test and the bookkeeping of an instance belong to one CTA
-// (instance k -> CTA k mod grid).  Converged instances drop out of the tile
-// list; the launch ends when every instance has converged or max_iters is
-// reached.  Per instance the iteration map, fold, stop rule and counts are
+// which CTA ran which tile (results are deterministic).  The dual update is
+// split into items of at most 1024 lines (rows or columns) of one instance,
+// spread over the CTAs; the stop test and the bookkeeping of an instance
+// belong to the CTA of its first item and run after a third grid barrier on
+// the iterations that test (even ones).  Converged instances drop out of
+// the tile list; once fewer coarse tiles stay active than half the CTAs the
+// solve moves to a list of 128-column tiles, so the last large instances
+// still spread over more of the GPU.  The launch ends when every instance has
+// converged or max_iters is reached.  Per instance the iteration map, fold, stop rule and counts are
 // those of the single-instance solver (core/drot_qr.hpp:159-234).
 #include <cuda_runtime.h>
 
@@ -34,8 +38,10 @@ struct BatchInst {
   long long rp_off;                      // row partials [P][nr] (floats)
   long long cp_off;                      // column partials [nbands][nc] (floats)
   int nr, nc;
-  int nbands, band_h, P;
-  int tile0, ntiles;
+  int nbands, band_h;
+  int tile0, ntiles, P;                  // coarse tiles (global indices), column chunks
+  int tile0f, ntilesf, Pf;               // fine tiles (global indices), column chunks
+  int item0, nitems;                     // dual-update items (contiguous)
   int row_off, col_off;                  // its rows / columns in the packed state arrays
   float s, kappa, kappa_rcp, eps, nc_rcp, nr_rcp;
   float w_phi1, w_phi2, w_a, w_b, w_alpha;  // warm-start constants
@@ -45,6 +51,10 @@ struct BatchInst {
 struct BatchTile {
   int inst, band, chunk, lo, hi, c0, c1;
   int kvr;  // 128-row blocks per warp step: 1, 2 or 4 (band height <= 128 * kvr)
+};
+
+struct BatchItem {
+  int inst, l0, l1, pad;  // lines [l0, l1) of instance inst: row l < nr, column l - nr
 };
 
 struct BatchStat {
@@ -59,13 +69,19 @@ struct BatchParams {
   float* x;
   const BatchInst* inst;
   const BatchTile* tiles;
-  int n_inst, n_tiles, max_iters, pad;
-  float *a, *b, *phi1, *phi2, *alpha;  // packed state
+  const BatchItem* items;
+  int n_inst, n_tiles, max_iters, n_items;
+  int n_tiles_f;       // fine tiles, stored after the n_tiles coarse ones
+  int fine_threshold;  // fine list once fewer active coarse tiles remain
+  float *a, *b, *phi1, *phi2;  // packed state
+  float* alpha;                // [2][n_inst], by iteration parity
+  double *res_slot, *obj_slot; // per item: squared residual; per instance: objective
   float *rowpart, *colpart;
   double *tile_sum, *tile_obj;
   int* conv;
   BatchStat* stats;
-  unsigned* counters;  // [0], [1]: tile counters of even / odd iterations; [2]: converged count
+  unsigned* counters;  // [0], [1]: tile counters of even / odd iterations; [2]: converged
+                       // instances; [3]: coarse tiles of unconverged instances
   unsigned* bar;
   int* abort_flag;
   long long timeout_ns;
@@ -94,6 +110,7 @@ __global__ void batch_init_kernel(const BatchParams P) {
       P.phi2[I.col_off + j] = I.w_phi2;
     }
     if (threadIdx.x == 0) {
+      if (k == 0) P.counters[3] = (unsigned)P.n_tiles;
       P.alpha[k] = I.w_alpha;
       P.conv[k] = 0;
       BatchStat st = {0, 0, 0, 0, 0.0, -1.0};
@@ -225,15 +242,16 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
   }
 }
 
-// Line sums of `n` partial vectors of length `len` (partial c of line l at
-// base[c * len + l]) for lines threadIdx.x + k * blockDim.x.  A thread takes
+// Line sums of `n` partial vectors (partial c of line l at base[c * stride
+// + l]) for lines lo + threadIdx.x + k * blockDim.x below hi.  A thread takes
 // 4 lines and issues the loads of 8 partials of each before adding any (one
 // L2 round trip per 32 loads instead of one per line); per line the
 // partials are added in index order.  use(l, sum) consumes each line.
 template <typename F>
-__device__ __forceinline__ void reduce_lines(const float* base, int len, int n, F&& use) {
+__device__ __forceinline__ void reduce_lines(const float* base, int stride, int lo, int hi, int n,
+                                             F&& use) {
   const int nt = blockDim.x;
-  for (int l0 = threadIdx.x; l0 < len; l0 += 4 * nt) {
+  for (int l0 = lo + threadIdx.x; l0 < hi; l0 += 4 * nt) {
     float s[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     for (int c0 = 0; c0 < n; c0 += 8) {
       float v[4][8];
@@ -242,7 +260,7 @@ __device__ __forceinline__ void reduce_lines(const float* base, int len, int n, 
 #pragma unroll
         for (int cc = 0; cc < 8; ++cc) {
           const int l = l0 + u * nt, c = c0 + cc;
-          v[u][cc] = (l < len && c < n) ? __ldcg(base + (long long)c * len + l) : 0.0f;
+          v[u][cc] = (l < hi && c < n) ? __ldcg(base + (long long)c * stride + l) : 0.0f;
         }
 #pragma unroll
       for (int u = 0; u < 4; ++u)
@@ -252,7 +270,7 @@ __device__ __forceinline__ void reduce_lines(const float* base, int len, int n, 
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u)
-      if (l0 + u * nt < len) use(l0 + u * nt, s[u]);
+      if (l0 + u * nt < hi) use(l0 + u * nt, s[u]);
   }
 }
 
@@ -272,18 +290,25 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
   unsigned epoch = 0;
   bool aborted = false;
   int it = 0;
+  // Tile list of the iteration: the coarse one while enough tiles remain to
+  // keep every CTA busy, then the fine one.  The switch is read from the
+  // active-tile count after the decision barrier, so every CTA switches at
+  // the same iteration.
+  bool fine = P.n_tiles_f > 0 && P.n_tiles < P.fine_threshold;
 
   for (; it < P.max_iters; ++it) {
     const bool even = (it & 1) == 0;
     unsigned* counter = P.counters + (it & 1);
+    const int n_list = fine ? P.n_tiles_f : P.n_tiles;
+    const int list0 = fine ? P.n_tiles : 0;
 
     // ---------------------------------------------------------- fused update
     for (;;) {
       __syncthreads();
       if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
       __syncthreads();
-      const int t = s_tile;
-      if (t >= P.n_tiles) break;
+      if (s_tile >= n_list) break;
+      const int t = list0 + s_tile;
       const BatchTile T = P.tiles[t];
       if (__ldcg(P.conv + T.inst)) continue;
       const BatchInst I = P.inst[T.inst];
@@ -360,33 +385,45 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
     }
 
     // ---------------------------------------------------------- dual update
+    // Item q: lines [l0, l1) of one instance (kernel_qr.hpp:405-467).  Every
+    // item of the instance recomputes sigma from the tile sums; alpha is
+    // read from this iteration's parity and written (by the first item) to
+    // the other one.
     if (blockIdx.x == 0 && threadIdx.x == 0) P.counters[(it + 1) & 1] = 0u;
-    for (int k = blockIdx.x; k < P.n_inst; k += G) {
+    for (int qi = blockIdx.x; qi < P.n_items; qi += G) {
+      const BatchItem Q = P.items[qi];
+      const int k = Q.inst;
       if (__ldcg(P.conv + k)) continue;
       const BatchInst I = P.inst[k];
+      const bool first = qi == I.item0;
+      const int t0 = fine ? I.tile0f : I.tile0;
+      const int ntl = fine ? I.ntilesf : I.ntiles;
+      const int nchunks = fine ? I.Pf : I.P;
       double sg = 0.0, og = 0.0;
-      for (int i = threadIdx.x; i < I.ntiles; i += blockDim.x) {
-        sg += __ldcg(P.tile_sum + I.tile0 + i);
-        if (even) og += __ldcg(P.tile_obj + I.tile0 + i);
+      for (int i = threadIdx.x; i < ntl; i += blockDim.x) {
+        sg += __ldcg(P.tile_sum + t0 + i);
+        if (even && first) og += __ldcg(P.tile_obj + t0 + i);
       }
       sg = block_sum_d(sg, dscr);
-      if (even) og = block_sum_d(og, dscr);
+      if (even && first) og = block_sum_d(og, dscr);
       const float sigma = (float)sg;
-      const float alpha = P.alpha[k];
+      const float alpha = __ldcg(P.alpha + (size_t)(it & 1) * P.n_inst + k);
       const float gamma =
           (float)((2.0 * ((double)sigma - 1.0) - (double)alpha) / (double)(I.nr + I.nc));
-      __syncthreads();
-      if (threadIdx.x == 0) P.alpha[k] = (float)(((double)alpha + 1.0) - (double)sigma);
+      if (first && threadIdx.x == 0)
+        P.alpha[(size_t)((it + 1) & 1) * P.n_inst + k] =
+            (float)(((double)alpha + 1.0) - (double)sigma);
       double res = 0.0;
       const float ncf = (float)I.nc, nrf = (float)I.nr;
-      reduce_lines(P.rowpart + I.rp_off, I.nr, I.P, [&](int i, float r) {
+      reduce_lines(P.rowpart + I.rp_off, I.nr, Q.l0, min(Q.l1, I.nr), nchunks, [&](int i, float r) {
         const float rs = r - __ldg(P.p + I.p_off + i);
         const float ab = P.a[I.row_off + i] - rs;
         P.phi1[I.row_off + i] = div_rn_by((ab - rs) + gamma, ncf, I.nc_rcp);
         P.a[I.row_off + i] = ab;
         res = fma((double)rs, (double)rs, res);
       });
-      reduce_lines(P.colpart + I.cp_off, I.nc, I.nbands, [&](int j, float cs_) {
+      reduce_lines(P.colpart + I.cp_off, I.nc, max(Q.l0 - I.nr, 0), Q.l1 - I.nr, I.nbands,
+                   [&](int j, float cs_) {
         const float cs = cs_ - __ldg(P.q + I.q_off + j);
         const float ab = P.b[I.col_off + j] - cs;
         P.phi2[I.col_off + j] = div_rn_by((ab - cs) + gamma, nrf, I.nr_rcp);
@@ -395,22 +432,8 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       });
       res = block_sum_d(res, dscr);
       if (threadIdx.x == 0) {
-        BatchStat st = P.stats[k];
-        if (even) {
-          st.objective = og;
-          st.objective_valid = 1;
-          st.residual = sqrt(res);
-          if (st.residual < (double)I.eps) {
-            // Converged at iteration it: the instance keeps its folded X
-            // until the unfold pass at the end of the launch.
-            st.converged = 1;
-            st.n_iter = it + 1;
-            st.iters_run = it + 1;
-            P.conv[k] = 1;
-            atomicAdd(P.counters + 2, 1u);
-          }
-        }
-        P.stats[k] = st;
+        P.res_slot[qi] = res;
+        if (even && first) P.obj_slot[k] = og;
       }
       __syncthreads();
     }
@@ -419,9 +442,44 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       aborted = true;
       break;
     }
-    if (__ldcg(P.counters + 2) >= (unsigned)P.n_inst) {
-      ++it;
-      break;
+
+    if (even) {
+      // Stop test (drot_qr.hpp:219-229: even iterations, residual < eps), by
+      // the CTA of each instance's first item, then one more barrier so the
+      // next fused update sees every decision.
+      if (threadIdx.x == 0) {
+        for (int qi = blockIdx.x; qi < P.n_items; qi += G) {
+          const int k = P.items[qi].inst;
+          const BatchInst& I = P.inst[k];
+          if (qi != I.item0 || __ldcg(P.conv + k)) continue;
+          double r2 = 0.0;
+          for (int t = 0; t < I.nitems; ++t) r2 += __ldcg(P.res_slot + I.item0 + t);
+          BatchStat st = P.stats[k];
+          st.objective = __ldcg(P.obj_slot + k);
+          st.objective_valid = 1;
+          st.residual = sqrt(r2);
+          if (st.residual < (double)I.eps) {
+            // Converged at iteration it: the instance keeps its folded X
+            // until the unfold pass at the end of the launch.
+            st.converged = 1;
+            st.n_iter = it + 1;
+            st.iters_run = it + 1;
+            P.conv[k] = 1;
+            atomicAdd(P.counters + 2, 1u);
+            atomicSub(P.counters + 3, (unsigned)I.ntiles);
+          }
+          P.stats[k] = st;
+        }
+      }
+      if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag)) {
+        aborted = true;
+        break;
+      }
+      if (__ldcg(P.counters + 2) >= (unsigned)P.n_inst) {
+        ++it;
+        break;
+      }
+      if (!fine && P.n_tiles_f > 0 && (int)__ldcg(P.counters + 3) < P.fine_threshold) fine = true;
     }
   }
 
@@ -476,17 +534,60 @@ static const size_t kAl = 256;
 static inline size_t al(size_t v) { return (v + kAl - 1) / kAl * kAl; }
 
 struct BatchPlanImpl {
-  int n_inst = 0, n_tiles = 0, grid = 0, threads = 256, cols_per_tile = 0;
+  int n_inst = 0, n_tiles = 0, n_tiles_f = 0, grid = 0, threads = 256, cols_per_tile = 0;
   size_t smem = 0;
   long long rows = 0, cols = 0, rowpart = 0, colpart = 0;
   std::vector<BatchInst> inst;
-  std::vector<BatchTile> tiles;
+  std::vector<BatchTile> tiles;  // coarse tiles, then fine tiles
+  std::vector<BatchItem> items;
   // workspace layout
-  size_t off_ctrl = 0, off_inst = 0, off_tiles = 0, off_a = 0, off_b = 0, off_phi1 = 0,
-         off_phi2 = 0, off_alpha = 0, off_rp = 0, off_cp = 0, off_tsum = 0, off_tobj = 0,
-         off_conv = 0, off_stats = 0, total = 0;
+  size_t off_ctrl = 0, off_inst = 0, off_tiles = 0, off_items = 0, off_a = 0, off_b = 0,
+         off_phi1 = 0, off_phi2 = 0, off_alpha = 0, off_rp = 0, off_cp = 0, off_tsum = 0,
+         off_tobj = 0, off_res = 0, off_obj = 0, off_conv = 0, off_stats = 0, total = 0;
   bool uploaded_any = false;
 };
+
+// Fine-list shape: columns per fine tile and the switch point (fewer active
+// coarse tiles than grid / divisor).  Measured on 256 instances of
+// U{64..2048}^2 with 256-column coarse tiles: 128 columns, grid / 2 and
+// 1024-line dual-update items gave 3.20 s against 3.45 s without the fine
+// list (32-column fine tiles: 3.45-3.85 s; their per-tile overhead and the
+// longer row-partial sums cost more than the parallelism gains).
+// DROT_BATCH_FINE_COLS and DROT_BATCH_FINE_DIV override them (0 as divisor
+// disables the fine list).
+static int fine_cols() {
+  const char* e = getenv("DROT_BATCH_FINE_COLS");
+  const int v = e ? atoi(e) : 0;
+  return v > 0 ? v : 128;
+}
+static int fine_divisor() {
+  const char* e = getenv("DROT_BATCH_FINE_DIV");
+  const int v = e ? atoi(e) : -1;
+  return v >= 0 ? (v == 0 ? 1 << 30 : v) : 2;
+}
+static int item_lines() {  // lines per dual-update item (DROT_BATCH_ITEM_LINES overrides)
+  const char* e = getenv("DROT_BATCH_ITEM_LINES");
+  const int v = e ? atoi(e) : 0;
+  return v > 0 ? v : 1024;
+}
+
+// Tiles of one instance: every 512-row band x `chunks` column chunks.
+static void add_tiles(std::vector<BatchTile>& tiles, int k, const BatchInst& I, int chunks) {
+  for (int b = 0; b < I.nbands; ++b)
+    for (int c = 0; c < chunks; ++c) {
+      BatchTile T;
+      T.inst = k;
+      T.band = b;
+      T.chunk = c;
+      T.lo = b * kBatchS;
+      T.hi = std::min(T.lo + kBatchS, I.nr);
+      T.c0 = (int)(((long long)I.nc * c) / chunks);
+      T.c1 = (int)(((long long)I.nc * (c + 1)) / chunks);
+      const int h = T.hi - T.lo;
+      T.kvr = h <= 128 ? 1 : (h <= 256 ? 2 : 4);
+      tiles.push_back(T);
+    }
+}
 
 static size_t batch_smem(int warps) {
   return sizeof(float) * ((size_t)warps * kBatchS + kBatchS) + sizeof(double) * (2 * warps + 1);
@@ -533,21 +634,9 @@ int drot_batch_plan_create(int n_inst, const drot_batch_instance* desc, int cols
     I.band_h = kBatchS;
     I.nbands = (d.n_rows + kBatchS - 1) / kBatchS;
     I.P = (d.n_cols + cols_per_tile - 1) / cols_per_tile;
+    I.Pf = (d.n_cols + fine_cols() - 1) / fine_cols();
     I.tile0 = (int)P.tiles.size();
-    for (int b = 0; b < I.nbands; ++b)
-      for (int c = 0; c < I.P; ++c) {
-        BatchTile T;
-        T.inst = k;
-        T.band = b;
-        T.chunk = c;
-        T.lo = b * kBatchS;
-        T.hi = std::min(T.lo + kBatchS, d.n_rows);
-        T.c0 = (int)(((long long)d.n_cols * c) / I.P);
-        T.c1 = (int)(((long long)d.n_cols * (c + 1)) / I.P);
-        const int h = T.hi - T.lo;
-        T.kvr = h <= 128 ? 1 : (h <= 256 ? 2 : 4);
-        P.tiles.push_back(T);
-      }
+    add_tiles(P.tiles, k, I, I.P);
     I.ntiles = (int)P.tiles.size() - I.tile0;
     I.row_off = (int)rows;
     I.col_off = (int)cols;
@@ -555,7 +644,18 @@ int drot_batch_plan_create(int n_inst, const drot_batch_instance* desc, int cols
     I.cp_off = cpp;
     rows += d.n_rows;
     cols += d.n_cols;
-    rp += (long long)I.P * d.n_rows;
+    rp += (long long)std::max(I.P, I.Pf) * d.n_rows;
+    I.item0 = (int)P.items.size();
+    const int ilines = item_lines();
+    for (int l = 0; l < d.n_rows + d.n_cols; l += ilines) {
+      BatchItem Q;
+      Q.inst = k;
+      Q.l0 = l;
+      Q.l1 = std::min(l + ilines, d.n_rows + d.n_cols);
+      Q.pad = 0;
+      P.items.push_back(Q);
+    }
+    I.nitems = (int)P.items.size() - I.item0;
     cpp += (long long)I.nbands * d.n_cols;
     // Operator parameters (pytorch/src/qr_drot_cuda_kernel.cu:100-102) and
     // the warm start (core/drot_qr.hpp:321-331), in float as the reference.
@@ -583,6 +683,15 @@ int drot_batch_plan_create(int n_inst, const drot_batch_instance* desc, int cols
     P.inst[k] = I;
   }
   P.n_tiles = (int)P.tiles.size();
+  // The fine list (fine_cols()-column chunks) after the coarse one; unused when the
+  // coarse tiles are no wider.
+  for (int k = 0; k < n_inst; ++k) {
+    BatchInst& I = P.inst[k];
+    I.tile0f = (int)P.tiles.size();
+    add_tiles(P.tiles, k, I, I.Pf);
+    I.ntilesf = (int)P.tiles.size() - I.tile0f;
+  }
+  P.n_tiles_f = fine_cols() < cols_per_tile ? (int)P.tiles.size() - P.n_tiles : 0;
   P.rows = rows;
   P.cols = cols;
   P.rowpart = rp;
@@ -610,16 +719,19 @@ int drot_batch_plan_create(int n_inst, const drot_batch_instance* desc, int cols
   size_t off = 0;
   P.off_ctrl = off;  off = al(off + 512);
   P.off_inst = off;  off = al(off + sizeof(BatchInst) * n_inst);
-  P.off_tiles = off; off = al(off + sizeof(BatchTile) * P.n_tiles);
+  P.off_tiles = off; off = al(off + sizeof(BatchTile) * P.tiles.size());
+  P.off_items = off; off = al(off + sizeof(BatchItem) * P.items.size());
   P.off_a = off;     off = al(off + sizeof(float) * rows);
   P.off_phi1 = off;  off = al(off + sizeof(float) * rows);
   P.off_b = off;     off = al(off + sizeof(float) * cols);
   P.off_phi2 = off;  off = al(off + sizeof(float) * cols);
-  P.off_alpha = off; off = al(off + sizeof(float) * n_inst);
+  P.off_alpha = off; off = al(off + sizeof(float) * 2 * n_inst);
   P.off_rp = off;    off = al(off + sizeof(float) * rp);
   P.off_cp = off;    off = al(off + sizeof(float) * cpp);
-  P.off_tsum = off;  off = al(off + sizeof(double) * P.n_tiles);
-  P.off_tobj = off;  off = al(off + sizeof(double) * P.n_tiles);
+  P.off_tsum = off;  off = al(off + sizeof(double) * P.tiles.size());
+  P.off_tobj = off;  off = al(off + sizeof(double) * P.tiles.size());
+  P.off_res = off;   off = al(off + sizeof(double) * P.items.size());
+  P.off_obj = off;   off = al(off + sizeof(double) * n_inst);
   P.off_conv = off;  off = al(off + sizeof(int) * n_inst);
   P.off_stats = off; off = al(off + sizeof(BatchStat) * n_inst);
   P.total = off;
@@ -648,7 +760,9 @@ int drot_batch_upload(drot_batch_plan plan, void* workspace, size_t workspace_by
   cudaStream_t st = (cudaStream_t)stream;
   if (cudaMemcpyAsync(ws + P.off_inst, P.inst.data(), sizeof(BatchInst) * P.n_inst,
                       cudaMemcpyHostToDevice, st) != cudaSuccess ||
-      cudaMemcpyAsync(ws + P.off_tiles, P.tiles.data(), sizeof(BatchTile) * P.n_tiles,
+      cudaMemcpyAsync(ws + P.off_tiles, P.tiles.data(), sizeof(BatchTile) * P.tiles.size(),
+                      cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(ws + P.off_items, P.items.data(), sizeof(BatchItem) * P.items.size(),
                       cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return DROT_ERR_CUDA;
@@ -676,6 +790,12 @@ int drot_qr_batch_launch(drot_batch_plan plan, const void* c, int c_dtype, const
   B.tiles = (const BatchTile*)(ws + P.off_tiles);
   B.n_inst = P.n_inst;
   B.n_tiles = P.n_tiles;
+  B.n_tiles_f = P.n_tiles_f;
+  B.fine_threshold = P.grid / fine_divisor();
+  B.items = (const BatchItem*)(ws + P.off_items);
+  B.n_items = (int)P.items.size();
+  B.res_slot = (double*)(ws + P.off_res);
+  B.obj_slot = (double*)(ws + P.off_obj);
   B.max_iters = max_iters;
   B.a = (float*)(ws + P.off_a);
   B.b = (float*)(ws + P.off_b);
