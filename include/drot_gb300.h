@@ -387,6 +387,21 @@ int drot_gl_adjoint_step(const void *c, int c_dtype, int n_rows, int n_cols,
                          float *qbar, void *workspace, size_t workspace_bytes,
                          drot_stream_t stream);
 
+/* One checkpoint segment of the backward in one call: from the state at the
+ * segment start (x, a, b, phi1, phi2, alpha; advanced in place) it runs
+ * n_steps GL iterations with drot_gl_solve_ex (solve_ws: its workspace),
+ * keeping X, phi1, phi2 before each in `states` (n_steps * (n_rows*n_cols +
+ * n_rows + n_cols) floats), then applies drot_gl_adjoint_step for those
+ * iterations in reverse order.  Asynchronous. */
+int drot_gl_adjoint_segment(const void *c, int c_dtype, const float *p,
+                            const float *q, int n_rows, int n_cols, int n_groups,
+                            float step_size, float lambda, float *x, float *a,
+                            float *b, float *phi1, float *phi2, float *alpha,
+                            int n_steps, float *states, void *solve_ws,
+                            size_t solve_ws_bytes, float *xbar, float *vbar,
+                            float *cbar, float *pbar, float *qbar, void *adj_ws,
+                            size_t adj_ws_bytes, drot_stream_t stream);
+
 /* ---------------------------------------------------------------------------
  * Cost matrices of point clouds (tensor cores)
  *

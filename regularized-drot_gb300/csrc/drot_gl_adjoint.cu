@@ -25,10 +25,11 @@
 //                   tbar = [t > 0] ybar,  Xbar = tbar,  Cbar -= s tbar,
 //                   phi1bar = tbar 1,  phi2bar = tbar^T 1.
 // Kernels: gl_adj_vec (one CTA), gl_adj_groups (one warp per group column:
-// norms, shrink factors and <Xt, y>), gl_adj_elems (one CTA per 32-column
-// chunk: tbar, Xbar, Cbar, column sums, per-chunk row partials in shared
-// memory), gl_adj_rows (row partials -> phi1bar).  All sums are in a fixed
-// order (deterministic).
+// norms, shrink factors and <Xt, y>), gl_adj_elems (one CTA per 16 columns x
+// 1024 rows: tbar, Xbar, Cbar, row partials in shared memory, column
+// partials per row block), gl_adj_rows (partials -> phi1bar, phi2bar).  All
+// sums are in a fixed order (deterministic).  drot_gl_adjoint_segment runs a
+// whole checkpoint segment (recompute + reverse steps) in one call.
 #include <cuda_runtime.h>
 
 #include <math.h>
@@ -42,7 +43,8 @@
 
 namespace drot {
 
-constexpr int kGlaChunk = 32;     // columns per CTA in gl_adj_elems
+constexpr int kGlaChunk = 16;     // columns per CTA in gl_adj_elems
+constexpr int kGlaRows = 1024;    // rows per CTA in gl_adj_elems
 constexpr int kGlaThreads = 256;
 constexpr double kGlaNormEps = 1e-9;
 
@@ -54,8 +56,7 @@ struct GlaParams {
   const float *x, *phi1, *phi2;
   float *xbar, *vbar, *cbar, *pbar, *qbar;
   // workspace
-  float *rbar, *cbarv, *sbar, *sig, *coef, *rowpart;
-  int* gid;
+  float *rbar, *cbarv, *sbar, *sig, *coef, *rowpart, *colpart;
   int bounds[kMaxGroups + 1];  // group row boundaries (travel in the parameters)
 };
 
@@ -65,6 +66,9 @@ __device__ __forceinline__ float load_cost(const GlaParams& A, long long e) {
 }
 
 // vbar layout: [phi1bar (nr) | phi2bar (nc) | abar (nr) | bbar (nc) | alphabar (1)]
+// Grid over the n_rows + n_cols lines; every CTA first forms gbar from all
+// of phi1bar', phi2bar' (8 loads in flight per thread, FP64 across the
+// block), then updates its own lines; CTA 0 writes sigbar and alphabar.
 __global__ void gl_adj_vec(const GlaParams A) {
   __shared__ double red[kGlaThreads / 32 + 1];
   const int nr = A.nr, nc = A.nc;
@@ -73,21 +77,34 @@ __global__ void gl_adj_vec(const GlaParams A) {
   float* ab = f2 + nc;
   float* bb = ab + nr;
   float* alb = bb + nc;
-  double g = 0.0;
-  for (int i = threadIdx.x; i < nr; i += blockDim.x) g += (double)f1[i] / (double)nc;
-  for (int j = threadIdx.x; j < nc; j += blockDim.x) g += (double)f2[j] / (double)nr;
-  g = block_sum_d(g, red);
-  const double mn = (double)nr + (double)nc;
-  const float al = *alb;
-  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
-    const float F = f1[i] / (float)nc;
-    const float A1 = ab[i];
-    const float rs = -A1 - 2.0f * F;
-    A.rbar[i] = rs;
-    ab[i] = A1 + F;
-    A.pbar[i] -= rs;
+  float s1 = 0.0f, s2 = 0.0f;
+  for (int i0 = threadIdx.x; i0 < nr + nc; i0 += 8 * blockDim.x) {
+    float v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int l = i0 + u * blockDim.x;
+      v[u] = l < nr + nc ? f1[l] : 0.0f;  // f2 follows f1
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int l = i0 + u * blockDim.x;
+      if (l < nr) s1 += v[u];
+      else s2 += v[u];
+    }
   }
-  for (int j = threadIdx.x; j < nc; j += blockDim.x) {
+  const double g = block_sum_d((double)s1, red) / (double)nc +
+                   block_sum_d((double)s2, red) / (double)nr;
+  const double mn = (double)nr + (double)nc;
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l < nr) {
+    const float F = f1[l] / (float)nc;
+    const float A1 = ab[l];
+    const float rs = -A1 - 2.0f * F;
+    A.rbar[l] = rs;
+    ab[l] = A1 + F;
+    A.pbar[l] -= rs;
+  } else if (l < nr + nc) {
+    const int j = l - nr;
     const float F = f2[j] / (float)nr;
     const float B1 = bb[j];
     const float cs = -B1 - 2.0f * F;
@@ -95,13 +112,23 @@ __global__ void gl_adj_vec(const GlaParams A) {
     bb[j] = B1 + F;
     A.qbar[j] -= cs;
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const float al = *alb;
     A.sbar[0] = (float)(-(double)al + 2.0 * g / mn);
     *alb = (float)((double)al - g / mn);
   }
-  for (int g2 = threadIdx.x; g2 < A.G; g2 += blockDim.x)
-    for (int i = A.bounds[g2]; i < A.bounds[g2 + 1]; ++i) A.gid[i] = g2;
+}
+
+// Group of row i: the last g with bounds[g] <= i (binary search; bounds
+// travel in the kernel parameters).
+__device__ __forceinline__ int group_of(const GlaParams& A, int i) {
+  int lo = 0, hi = A.G - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (A.bounds[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
 }
 
 // One warp per (group g, column j): n_gj, sig_gj and coef_gj.
@@ -114,17 +141,37 @@ __global__ void gl_adj_groups(const GlaParams A) {
     const int g = (int)(task % A.G), j = (int)(task / A.G);
     const int i0 = A.bounds[g], i1 = A.bounds[g + 1];
     const float f2 = A.phi2[j], cb = A.cbarv[j];
-    double n2 = 0.0, dot = 0.0;
-    for (int i = i0 + lane; i < i1; i += 32) {
-      const long long e = (long long)j * A.nr + i;
-      const float t = fmaf(-A.s, load_cost(A, e), (A.x[e] + A.phi1[i]) + f2);
-      const float y = fmaxf(t, 0.0f);
-      const float xt = ((A.xbar[e] + A.rbar[i]) + cb) + sb;
-      n2 += (double)y * (double)y;
-      dot += (double)xt * (double)y;
+    // Lane sums as float pairs (TwoSum), combined in FP64 across the warp
+    // (FP64 arithmetic is slow on this part; a per-element FP64 FMA cost
+    // more than the loads).
+    float n2h = 0.0f, n2l = 0.0f, dth = 0.0f, dtl = 0.0f;
+    for (int ib = i0 + lane; ib < i1; ib += 128) {
+      float xv[4], cv[4], f1[4], xb[4], rb[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {  // all loads of four rows first
+        const int i = ib + 32 * u;
+        const long long e = (long long)j * A.nr + (i < i1 ? i : i0);
+        xv[u] = A.x[e];
+        cv[u] = load_cost(A, e);
+        f1[u] = A.phi1[i < i1 ? i : i0];
+        xb[u] = A.xbar[e];
+        rb[u] = A.rbar[i < i1 ? i : i0];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (ib + 32 * u >= i1) break;
+        const float t = fmaf(-A.s, cv[u], (xv[u] + f1[u]) + f2);
+        const float y = fmaxf(t, 0.0f);
+        const float xt = ((xb[u] + rb[u]) + cb) + sb;
+        float e1;
+        two_sum(n2h, y * y, n2h, e1);
+        n2l += e1;
+        two_sum(dth, xt * y, dth, e1);
+        dtl += e1;
+      }
     }
-    n2 = warp_sum_d(n2);
-    dot = warp_sum_d(dot);
+    double n2 = warp_sum_d((double)n2h + (double)n2l);
+    double dot = warp_sum_d((double)dth + (double)dtl);
     if (lane == 0) {
       const double n = sqrt(n2);
       const double sh = 1.0 - (double)A.lambda / (n + kGlaNormEps);
@@ -135,57 +182,105 @@ __global__ void gl_adj_groups(const GlaParams A) {
   }
 }
 
-// One CTA per chunk of kGlaChunk columns; each thread owns rows
-// tid, tid + 256, ... of the chunk's row partial (shared memory).
+// One CTA per (chunk of kGlaChunk columns, block of kGlaRows rows); thread
+// t owns rows r0 + t + 256 u (u < 4) of the CTA's row partial (registers)
+// and loads its four rows of a column before using any.  Column sums: one
+// FP32 partial per warp and column in shared memory, combined in warp order
+// at the end into the row block's column partial.
 __global__ void __launch_bounds__(kGlaThreads) gl_adj_elems(const GlaParams A) {
-  extern __shared__ float rowacc[];  // [nr]
-  __shared__ double red[kGlaThreads / 32 + 1];
-  const int chunk = blockIdx.x;
+  __shared__ float wcol[kGlaThreads / 32][kGlaChunk];
+  const int chunk = blockIdx.x, rb = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int j0 = chunk * kGlaChunk, j1 = min(j0 + kGlaChunk, A.nc);
-  for (int i = threadIdx.x; i < A.nr; i += blockDim.x) rowacc[i] = 0.0f;
+  const int r0 = rb * kGlaRows, r1 = min(r0 + kGlaRows, A.nr);
+  constexpr int U = kGlaRows / kGlaThreads;
   const float sb = A.sbar[0];
+  int gi[U];
+  float f1[U], rbv[U], racc[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int i = r0 + threadIdx.x + u * kGlaThreads;
+    const int ic = i < r1 ? i : r0;
+    gi[u] = group_of(A, ic);
+    f1[u] = A.phi1[ic];
+    rbv[u] = A.rbar[ic];
+    racc[u] = 0.0f;
+  }
   for (int j = j0; j < j1; ++j) {
     const float f2 = A.phi2[j], cb = A.cbarv[j];
+    float xv[U], cv[U], xb[U], sg[U], cf[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = r0 + threadIdx.x + u * kGlaThreads;
+      const long long e = (long long)j * A.nr + (i < r1 ? i : r0);
+      const long long gj = (long long)j * A.G + gi[u];
+      xv[u] = A.x[e];
+      cv[u] = load_cost(A, e);
+      xb[u] = A.xbar[e];
+      sg[u] = A.sig[gj];
+      cf[u] = A.coef[gj];
+    }
     float colp = 0.0f;
-    for (int i = threadIdx.x; i < A.nr; i += blockDim.x) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = r0 + threadIdx.x + u * kGlaThreads;
+      if (i >= r1) continue;
       const long long e = (long long)j * A.nr + i;
-      const float cv = load_cost(A, e);
-      const float t = fmaf(-A.s, cv, (A.x[e] + A.phi1[i]) + f2);
-      const int g = A.gid[i];
-      const long long gj = (long long)j * A.G + g;
-      const float xt = ((A.xbar[e] + A.rbar[i]) + cb) + sb;
-      const float ybar = fmaf(A.coef[gj], fmaxf(t, 0.0f), A.sig[gj] * xt);
+      const float t = fmaf(-A.s, cv[u], (xv[u] + f1[u]) + f2);
+      const float xt = ((xb[u] + rbv[u]) + cb) + sb;
+      const float ybar = fmaf(cf[u], fmaxf(t, 0.0f), sg[u] * xt);
       const float tb = t > 0.0f ? ybar : 0.0f;
       A.xbar[e] = tb;
       A.cbar[e] = fmaf(-A.s, tb, A.cbar[e]);
-      rowacc[i] += tb;
+      racc[u] += tb;
       colp += tb;
     }
-    const double cs = block_sum_d((double)colp, red);
-    if (threadIdx.x == 0) A.vbar[A.nr + j] = (float)cs;  // phi2bar of s_k
+    colp = warp_sum(colp);
+    if (lane == 0) wcol[warp][j - j0] = colp;
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < A.nr; i += blockDim.x)
-    A.rowpart[(long long)chunk * A.nr + i] = rowacc[i];
+  if (threadIdx.x < j1 - j0) {
+    float cs = 0.0f;
+    for (int w = 0; w < kGlaThreads / 32; ++w) cs += wcol[w][threadIdx.x];
+    A.colpart[(long long)rb * A.nc + j0 + threadIdx.x] = cs;
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int i = r0 + threadIdx.x + u * kGlaThreads;
+    if (i < r1) A.rowpart[(long long)chunk * A.nr + i] = racc[u];
+  }
 }
 
-__global__ void gl_adj_rows(const GlaParams A, int chunks) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < A.nr; i += gridDim.x * blockDim.x) {
+// phi1bar = sum over column chunks of the row partials, phi2bar = sum over
+// row blocks of the column partials (fixed order).
+// One warp per line: lanes take partials lane, lane + 32, ... (fixed order),
+// then a shuffle tree.
+__global__ void gl_adj_rows(const GlaParams A, int chunks, int rblocks) {
+  const int n = A.nr + A.nc;
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int l = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); l < n; l += warps) {
+    const bool row = l < A.nr;
+    const float* base = row ? A.rowpart + l : A.colpart + (l - A.nr);
+    const long long stride = row ? A.nr : A.nc;
+    const int cnt = row ? chunks : rblocks;
     double s = 0.0;
-    for (int c = 0; c < chunks; ++c) s += (double)A.rowpart[(long long)c * A.nr + i];
-    A.vbar[i] = (float)s;  // phi1bar of s_k
+    for (int c = lane; c < cnt; c += 32) s += (double)base[c * stride];
+    s = warp_sum_d(s);
+    if (lane == 0) A.vbar[l] = (float)s;  // [phi1bar | phi2bar] of s_k
   }
 }
 
 struct GlaLayout {
-  size_t off_rbar, off_cbar, off_sbar, off_sig, off_coef, off_rowpart, off_gid, total;
-  int chunks;
+  size_t off_rbar, off_cbar, off_sbar, off_sig, off_coef, off_rowpart, off_colpart, total;
+  int chunks, rblocks;
 };
 
 static GlaLayout gla_layout(int nr, int nc, int G) {
   auto al = [](size_t v) { return (v + 255) / 256 * 256; };
   GlaLayout L;
   L.chunks = (nc + kGlaChunk - 1) / kGlaChunk;
+  L.rblocks = (nr + kGlaRows - 1) / kGlaRows;
   size_t off = 0;
   L.off_rbar = off;    off = al(off + sizeof(float) * nr);
   L.off_cbar = off;    off = al(off + sizeof(float) * nc);
@@ -193,7 +288,7 @@ static GlaLayout gla_layout(int nr, int nc, int G) {
   L.off_sig = off;     off = al(off + sizeof(float) * (size_t)G * nc);
   L.off_coef = off;    off = al(off + sizeof(float) * (size_t)G * nc);
   L.off_rowpart = off; off = al(off + sizeof(float) * (size_t)L.chunks * nr);
-  L.off_gid = off;     off = al(off + sizeof(int) * nr);
+  L.off_colpart = off; off = al(off + sizeof(float) * (size_t)L.rblocks * nc);
   L.total = off;
   return L;
 }
@@ -205,9 +300,7 @@ using namespace drot;
 extern "C" {
 
 size_t drot_gl_adjoint_workspace_bytes(int n_rows, int n_cols, int n_groups) {
-  if (n_rows <= 0 || n_cols <= 0 || n_groups <= 0 || n_groups > kMaxGroups ||
-      n_rows > 48 * 1024)
-    return 0;
+  if (n_rows <= 0 || n_cols <= 0 || n_groups <= 0 || n_groups > kMaxGroups) return 0;
   return gla_layout(n_rows, n_cols, n_groups).total;
 }
 
@@ -249,19 +342,50 @@ int drot_gl_adjoint_step(const void* c, int c_dtype, int n_rows, int n_cols, int
   A.sig = (float*)(ws + L.off_sig);
   A.coef = (float*)(ws + L.off_coef);
   A.rowpart = (float*)(ws + L.off_rowpart);
-  A.gid = (int*)(ws + L.off_gid);
-  gl_adj_vec<<<1, kGlaThreads, 0, st>>>(A);
+  A.colpart = (float*)(ws + L.off_colpart);
+  gl_adj_vec<<<(n_rows + n_cols + kGlaThreads - 1) / kGlaThreads, kGlaThreads, 0, st>>>(A);
   const long long tasks = (long long)n_groups * n_cols;
   const int gblocks = (int)std::min<long long>((tasks + 7) / 8, 4096);
   gl_adj_groups<<<gblocks, 256, 0, st>>>(A);
-  const size_t smem = sizeof(float) * (size_t)n_rows;
-  if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute((const void*)gl_adj_elems, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess)
-    return DROT_ERR_CUDA;
-  gl_adj_elems<<<L.chunks, kGlaThreads, smem, st>>>(A);
-  gl_adj_rows<<<(n_rows + 255) / 256, 256, 0, st>>>(A, L.chunks);
+  gl_adj_elems<<<dim3(L.chunks, L.rblocks), kGlaThreads, 0, st>>>(A);
+  gl_adj_rows<<<(n_rows + n_cols + 7) / 8, 256, 0, st>>>(A, L.chunks, L.rblocks);
   return cudaGetLastError() == cudaSuccess ? DROT_OK : DROT_ERR_CUDA;
+}
+
+int drot_gl_adjoint_segment(const void* c, int c_dtype, const float* p, const float* q,
+                            int n_rows, int n_cols, int n_groups, float step_size, float lambda,
+                            float* x, float* a, float* b, float* phi1, float* phi2, float* alpha,
+                            int n_steps, float* states, void* solve_ws, size_t solve_ws_bytes,
+                            float* xbar, float* vbar, float* cbar, float* pbar, float* qbar,
+                            void* adj_ws, size_t adj_ws_bytes, drot_stream_t stream) {
+  if (n_steps < 0 || !states || !x || !phi1 || !phi2) return DROT_ERR_INVALID_ARG;
+  const size_t mn = (size_t)n_rows * n_cols;
+  const size_t per = mn + n_rows + n_cols;
+  cudaStream_t st = (cudaStream_t)stream;
+  // Recompute: keep X, phi1, phi2 before every iteration of the segment.
+  for (int k = 0; k < n_steps; ++k) {
+    float* s_k = states + per * k;
+    if (cudaMemcpyAsync(s_k, x, sizeof(float) * mn, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(s_k + mn, phi1, sizeof(float) * n_rows, cudaMemcpyDeviceToDevice, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(s_k + mn + n_rows, phi2, sizeof(float) * n_cols, cudaMemcpyDeviceToDevice,
+                        st) != cudaSuccess)
+      return DROT_ERR_CUDA;
+    // One GL iteration; eps = -1 never stops it early.
+    const int rc = drot_gl_solve_ex(c, c_dtype, p, q, n_rows, n_cols, n_groups, step_size, lambda,
+                                    1, -1.0f, x, a, b, phi1, phi2, alpha, solve_ws,
+                                    solve_ws_bytes, nullptr, stream);
+    if (rc != DROT_OK) return rc;
+  }
+  // Reverse steps.
+  for (int k = n_steps - 1; k >= 0; --k) {
+    const float* s_k = states + per * k;
+    const int rc = drot_gl_adjoint_step(c, c_dtype, n_rows, n_cols, n_groups, step_size, lambda,
+                                        s_k, s_k + mn, s_k + mn + n_rows, xbar, vbar, cbar, pbar,
+                                        qbar, adj_ws, adj_ws_bytes, stream);
+    if (rc != DROT_OK) return rc;
+  }
+  return DROT_OK;
 }
 
 }  // extern "C"

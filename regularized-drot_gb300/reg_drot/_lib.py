@@ -141,6 +141,10 @@ SIGNATURES = {
     "drot_gl_adjoint_workspace_bytes": (_c_size, [_c_int, _c_int, _c_int]),
     "drot_gl_adjoint_step": (_c_int, [_vp, _c_int, _c_int, _c_int, _c_int, _c_float, _c_float,
                                       _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _c_size, _vp]),
+    "drot_gl_adjoint_segment": (_c_int, [_vp, _c_int, _vp, _vp, _c_int, _c_int, _c_int, _c_float,
+                                         _c_float, _vp, _vp, _vp, _vp, _vp, _vp, _c_int, _vp,
+                                         _vp, _c_size, _vp, _vp, _vp, _vp, _vp, _vp, _c_size,
+                                         _vp]),
     "drot_sqeuclidean_cost": (_c_int, [_c_int, _CIP, _vp, _vp, _c_int, _c_float, _c_int, _vp,
                                        _vp]),
 }

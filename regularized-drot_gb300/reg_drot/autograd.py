@@ -288,6 +288,7 @@ class _GLState:
             self.t[k].copy_(v)
 
 
+
 class GroupLassoDROTFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, c, p, q, n_class, rho, r_weight, max_iters, eps, segment):
@@ -330,21 +331,20 @@ class GroupLassoDROTFn(torch.autograd.Function):
         aws = torch.empty(abytes + 256, dtype=torch.uint8, device=dev)
         aptr = aws.data_ptr() + (-aws.data_ptr()) % 256
         cdt = C_BF16 if c.dtype == torch.bfloat16 else C_F32
+        states = torch.empty(seg * (nr * nc + nr + nc), device=dev)
+        t = st.t
         for si in reversed(range(len(ctx.checkpoints))):
             k0 = si * seg
             k1 = min(k0 + seg, T)
             st.restore(ctx.checkpoints[si])
-            saved = []
-            for _ in range(k0, k1):  # recompute the segment's states
-                saved.append((st.t["x"].clone(), st.t["phi1"].clone(), st.t["phi2"].clone()))
-                st.run(1, -1.0)
-            for xk, f1k, f2k in reversed(saved):
-                with torch.cuda.device(dev):
-                    rc = lib().drot_gl_adjoint_step(
-                        c.data_ptr(), cdt, nr, nc, G, s, lam, xk.data_ptr(), f1k.data_ptr(),
-                        f2k.data_ptr(), xbar.data_ptr(), vbar.data_ptr(), cbar.data_ptr(),
-                        pbar.data_ptr(), qbar.data_ptr(), aptr, abytes, st.stream())
-                check(rc, "gl_adjoint_step")
+            with torch.cuda.device(dev):
+                rc = lib().drot_gl_adjoint_segment(
+                    c.data_ptr(), cdt, p.data_ptr(), q.data_ptr(), nr, nc, G, s, lam,
+                    t["x"].data_ptr(), t["a"].data_ptr(), t["b"].data_ptr(), t["phi1"].data_ptr(),
+                    t["phi2"].data_ptr(), t["alpha"].data_ptr(), k1 - k0, states.data_ptr(),
+                    st.wptr, st.nbytes, xbar.data_ptr(), vbar.data_ptr(), cbar.data_ptr(),
+                    pbar.data_ptr(), qbar.data_ptr(), aptr, abytes, st.stream())
+            check(rc, "gl_adjoint_segment")
         return cbar.to(c.dtype), pbar, qbar, None, None, None, None, None, None
 
 
