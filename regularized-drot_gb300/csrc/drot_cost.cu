@@ -34,7 +34,7 @@
 namespace drot {
 
 constexpr int kCostM = 128;        // tile rows (x points) = TMEM lanes
-constexpr int kCostN = 256;        // tile columns (y points) = TMEM columns
+constexpr int kCostN = 128;        // tile columns (y points) = TMEM columns
 constexpr int kCostMaxInst = 256;  // instances per launch (descriptors travel in the parameters)
 constexpr int kCostThreads = 128;
 
