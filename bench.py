@@ -603,12 +603,44 @@ def run_gpu(args):
     return 0
 
 
+def run_diff_case(n_inst, iters):
+    """Profiler case: the differentiable workload's first n_inst instances,
+    one launch each of the cost kernel, the batched solve (iters iterations)
+    and the adjoint CG (--case diff:n_inst:iters)."""
+    import warnings
+    import torch
+    from reg_drot.autograd import batch_quadratic_drot_fn
+    from reg_drot.batch import QRBatch
+    from reg_drot.cost import packed_sqeuclidean_cost
+    warnings.simplefilter("ignore")
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(SEED + 5)
+    shapes = [(int(a), int(b)) for a, b in rng.integers(DIFF_MIN, DIFF_MAX + 1, size=(n_inst, 2))]
+    g = torch.Generator(device=dev).manual_seed(SEED + 5)
+    x = torch.randn(sum(m for m, _ in shapes), DIFF_DIM, generator=g, device=dev, requires_grad=True)
+    y = torch.randn(sum(n for _, n in shapes), DIFF_DIM, generator=g, device=dev, requires_grad=True)
+    B = QRBatch(shapes, RHO, ALPHA, [REL_EPS * math.sqrt(1.0 / m + 1.0 / n) for m, n in shapes],
+                device=dev, cols_per_tile=256)
+    p, q = B.pack_marginals([torch.full((m,), 1.0 / m) for m, _ in shapes],
+                            [torch.full((n,), 1.0 / n) for _, n in shapes])
+    c = packed_sqeuclidean_cost(B, x, y, DIFF_SCALE)
+    X = batch_quadratic_drot_fn(B, c, p, q, iters)
+    ((c * X).sum() + 0.5 * (X * X).sum()).backward()
+    torch.cuda.synchronize()
+    print(json.dumps({"case": f"diff:{n_inst}:{iters}", "elements": sum(m * n for m, n in shapes),
+                      "cg_iters": X.grad_fn.cg_iters[:4]}), flush=True)
+    return 0
+
+
 def run_case(spec):
     """One solve of the headline workload at size n for a fixed iteration count
-    (for profiler captures): --case n:iters[:gl][:bf16]."""
+    (for profiler captures): --case n:iters[:gl][:bf16]; --case diff:n_inst:iters
+    for the differentiable workload's kernels."""
     import torch
     import reg_drot
     parts = spec.split(":")
+    if parts[0] == "diff":
+        return run_diff_case(int(parts[1]), int(parts[2]))
     n, iters = int(parts[0]), int(parts[1])
     dev = torch.device("cuda", 0)
     c, p, q, _ = make_problem(n)
@@ -632,7 +664,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--case", default=None,
-                    help="n:iters[:gl] -- one fixed-length solve, for profiler captures")
+                    help="n:iters[:gl][:bf16] -- one fixed-length solve; diff:n_inst:iters -- "
+                         "cost, batched solve and adjoint of the differentiable workload; "
+                         "for profiler captures")
     args = ap.parse_args()
     if args.case:
         return run_case(args.case)

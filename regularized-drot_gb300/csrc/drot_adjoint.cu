@@ -261,12 +261,27 @@ __global__ void __launch_bounds__(256, 2) adj_pcg_kernel(const AdjParams A) {
       const float beta = it == 0 ? 0.0f : (float)(inst_sum(ry_cur, I) / inst_sum(ry_prev, I));
       const int nv = I.nr + I.nc;
       __syncthreads();
-      for (int t = threadIdx.x; t < nv; t += blockDim.x) {
-        const int g = I.v_off + t;
-        const float y = __ldcg(A.invdiag + g) * __ldcg(A.r + g);
-        const float dv = it == 0 ? y : fmaf(beta, __ldcg(dold + g), y);
-        sv[t] = dv;
-        if (t >= S.l0 && t < S.l1) dcur[g] = dv;
+      // Stage d = M^-1 r + beta d_old for the whole instance: a thread takes
+      // 4 entries and issues their 12 loads before using any.
+      for (int t0 = threadIdx.x; t0 < nv; t0 += 4 * blockDim.x) {
+        float iv[4], rv[4], dv0[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int t = t0 + u * blockDim.x;
+          const int g = I.v_off + (t < nv ? t : 0);
+          iv[u] = __ldcg(A.invdiag + g);
+          rv[u] = __ldcg(A.r + g);
+          dv0[u] = it == 0 ? 0.0f : __ldcg(dold + g);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int t = t0 + u * blockDim.x;
+          if (t >= nv) break;
+          const float y = iv[u] * rv[u];
+          const float dv = it == 0 ? y : fmaf(beta, dv0[u], y);
+          sv[t] = dv;
+          if (t >= S.l0 && t < S.l1) dcur[I.v_off + t] = dv;
+        }
       }
       __syncthreads();
       double dq = 0.0;
