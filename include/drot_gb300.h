@@ -286,6 +286,11 @@ typedef struct drot_batch_plan_s *drot_batch_plan;
  * 512 rows x cols_per_tile columns (<= 0: 128), plus the launch shape. */
 int drot_batch_plan_create(int n_inst, const drot_batch_instance *inst,
                            int cols_per_tile, drot_batch_plan *plan);
+/* The same with the tile height: band_rows 512 (cost-matrix launches) or
+ * 128 (required by drot_qr_batch_launch_points). */
+int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance *inst,
+                              int cols_per_tile, int band_rows,
+                              drot_batch_plan *plan);
 void drot_batch_plan_destroy(drot_batch_plan plan);
 /* Workspace bytes of a plan (device memory, 256-byte aligned). */
 size_t drot_batch_plan_workspace_bytes(drot_batch_plan plan);
@@ -300,6 +305,20 @@ int drot_qr_batch_launch(drot_batch_plan plan, const void *c, int c_dtype,
                          const float *p, const float *q, float *x,
                          int max_iters, void *workspace, size_t workspace_bytes,
                          drot_stream_t stream);
+/* Point-cloud launch: the cost is never stored.  Instance k's C_ij =
+ * cost_scale * max(|x_i|^2 + |y_j|^2 - 2 <x_i, y_j>, 0) is recomputed
+ * inside the fused update on the iterations that read C, from x_i =
+ * xpts[(R_k + i) * dim ...] and y_j = ypts[(S_k + j) * dim ...] (R_k, S_k:
+ * the earlier instances' total rows / columns, i.e. the points of all
+ * instances concatenated in order, row-major, 16-byte aligned); dim 8 or
+ * 16; FP32 FMA arithmetic, k ascending.  8 bytes per element on every
+ * iteration instead of 12 on those that read C.  The plan must be built
+ * with band_rows = 128; c_offset of the descriptors is unused. */
+int drot_qr_batch_launch_points(drot_batch_plan plan, const float *xpts,
+                                const float *ypts, int dim, float cost_scale,
+                                const float *p, const float *q, float *x,
+                                int max_iters, void *workspace,
+                                size_t workspace_bytes, drot_stream_t stream);
 /* Copies the per-instance outcomes to out[n_inst]; synchronises `stream`.
  * Returns DROT_ERR_BARRIER_TIMEOUT when the launch gave up on a barrier. */
 int drot_batch_results(drot_batch_plan plan, const void *workspace,

@@ -80,6 +80,12 @@ struct BatchParams {
   double *tile_sum, *tile_obj;
   int* conv;
   BatchStat* stats;
+  // On-the-fly cost (point-cloud launches): C_ij = cscale * max(|x_i|^2 +
+  // |y_j|^2 - 2 <x_i, y_j>, 0) with x_i = xpts[row_off + i], y_j =
+  // ypts[col_off + j] (dim floats each), norms precomputed.
+  const float *xpts, *ypts, *xnorm, *ynorm;
+  float cscale;
+  int dim;
   unsigned* counters;  // [0], [1]: tile counters of even / odd iterations; [2]: converged
                        // instances; [3]: coarse tiles of unconverged instances
   unsigned* bar;
@@ -126,12 +132,14 @@ __global__ void batch_init_kernel(const BatchParams P) {
 // the folded X - sC), else odd (reads X only).  FULL: the band is exactly
 // 128 * KVR rows (no row masks).  Element arithmetic as in the
 // single-instance kernel: t = (X + phi1) + phi2 (- sC), y = max(t, 0) / kappa.
-template <int KVR, bool EV, bool FULL, typename CT>
+template <int KVR, bool EV, bool FULL, typename CT, int DIM>
 __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const BatchInst& I,
                                                    const BatchTile& T, const float* f1s,
+                                                   const float* xs, const float* xns,
                                                    float (&acc)[4][4], float& ms_hi,
                                                    float& ms_lo, float& ob_hi, float& ob_lo,
                                                    int lane, int warp, int W) {
+  static_assert(DIM == 0 || KVR == 1, "point-cloud tiles are 128-row bands");
   constexpr int VEC = 4, SV = 128, NCOL = 4 / KVR;
   const CT* const cbase = reinterpret_cast<const CT*>(P.c);
   const int lo = T.lo, hi = T.hi, c1 = T.c1;
@@ -146,7 +154,7 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
       const int r = lo + (v % KVR) * SV + lane * VEC;
       if ((NCOL == 1 || jc < c1) && (FULL || r < hi)) {
         load_vec<VEC>(P.x + I.x_off + (long long)jc * I.ld + r, xv[v]);
-        if constexpr (EV) load_c<VEC, CT>(cbase + I.c_off + (long long)jc * I.ld + r, cv[v]);
+        if constexpr (EV && DIM == 0) load_c<VEC, CT>(cbase + I.c_off + (long long)jc * I.ld + r, cv[v]);
         else {
 #pragma unroll
           for (int e = 0; e < VEC; ++e) cv[v][e] = 0.0f;
@@ -159,6 +167,46 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
 #pragma unroll
     for (int cc = 0; cc < NCOL; ++cc)
       f2[cc] = (NCOL == 1 || j0 + cc < c1) ? __ldcg(P.phi2 + I.col_off + j0 + cc) : 0.0f;
+    if constexpr (EV && DIM > 0) {
+      // C of the step's 4 columns x the lane's 4 rows from the points: the
+      // band's x (k-major in shared memory) against y_j (broadcast loads),
+      // k ascending; cv = cscale * max(|x|^2 + |y|^2 - 2 <x, y>, 0).
+      float dot[4][VEC], yn[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int jc = min(j0 + v, c1 - 1);
+        yn[v] = __ldg(P.ynorm + I.col_off + jc);
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) dot[v][e] = 0.0f;
+      }
+#pragma unroll
+      for (int k0 = 0; k0 < DIM; k0 += 4) {
+        float4 yk[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const int jc = min(j0 + v, c1 - 1);
+          yk[v] = __ldg(reinterpret_cast<const float4*>(P.ypts + (long long)(I.col_off + jc) * DIM + k0));
+        }
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          const float4 xk = *reinterpret_cast<const float4*>(xs + (k0 + kk) * SV + lane * VEC);
+          const float xa[VEC] = {xk.x, xk.y, xk.z, xk.w};
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            const float yv = kk == 0 ? yk[v].x : (kk == 1 ? yk[v].y : (kk == 2 ? yk[v].z : yk[v].w));
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) dot[v][e] = fmaf(xa[e], yv, dot[v][e]);
+          }
+        }
+      }
+      const float4 xn4 = *reinterpret_cast<const float4*>(xns + lane * VEC);
+      const float xna[VEC] = {xn4.x, xn4.y, xn4.z, xn4.w};
+#pragma unroll
+      for (int v = 0; v < 4; ++v)
+#pragma unroll
+        for (int e = 0; e < VEC; ++e)
+          cv[v][e] = P.cscale * fmaxf(fmaf(-2.0f, dot[v][e], xna[e] + yn[v]), 0.0f);
+    }
 
     auto valid = [&](int v, int e) -> bool {
       if constexpr (FULL && NCOL == 1) return true;
@@ -274,7 +322,31 @@ __device__ __forceinline__ void reduce_lines(const float* base, int stride, int 
   }
 }
 
-template <typename CT>
+// C_ij of a point-cloud launch, the same arithmetic as the fused update.
+template <int DIM>
+__device__ __forceinline__ float point_cost(const BatchParams& P, const BatchInst& I, int i, int j) {
+  const float* xr = P.xpts + (long long)(I.row_off + i) * DIM;
+  const float* yr = P.ypts + (long long)(I.col_off + j) * DIM;
+  float dot = 0.0f;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) dot = fmaf(__ldg(xr + k), __ldg(yr + k), dot);
+  return P.cscale *
+         fmaxf(fmaf(-2.0f, dot, __ldg(P.xnorm + I.row_off + i) + __ldg(P.ynorm + I.col_off + j)), 0.0f);
+}
+
+// Norms |x_i|^2 (k ascending, FMA) of n points of dimension dim.
+__global__ void point_norms_kernel(const float* pts, int n, int dim, float* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float s = 0.0f;
+    for (int k = 0; k < dim; ++k) {
+      const float v = pts[(long long)i * dim + k];
+      s = fmaf(v, v, s);
+    }
+    out[i] = s;
+  }
+}
+
+template <typename CT, int DIM>
 __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P) {
   constexpr int VEC = 4, KV = kBatchKV, S = kBatchS;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -283,6 +355,12 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
   float* f1s = red + (size_t)W * S;                 // [S]
   double* dscr = reinterpret_cast<double*>(f1s + S);  // [W + 1]
   double* oscr = dscr + W + 1;                        // [W]
+  // Point launches: the band's x, k-major [DIM][128], and their norms [128].
+  // float4 reads: 16-byte aligned (the FP64 scratch above ends on an 8-byte
+  // boundary).
+  float* xs = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(oscr + W) + 15) &
+                                       ~static_cast<uintptr_t>(15));
+  float* xns = xs + DIM * 128;
   __shared__ int s_flag, s_tile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int G = gridDim.x;
@@ -317,6 +395,17 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
         const int r = lo + idx;
         f1s[idx] = r < hi ? __ldcg(P.phi1 + I.row_off + r) : 0.0f;
       }
+      if constexpr (DIM > 0) {
+        if (even) {
+          for (int idx = threadIdx.x; idx < 128 * DIM; idx += blockDim.x) {
+            const int rl = idx / DIM, k = idx - rl * DIM;
+            xs[k * 128 + rl] =
+                lo + rl < hi ? __ldg(P.xpts + (long long)(I.row_off + lo + rl) * DIM + k) : 0.0f;
+          }
+          for (int rl = threadIdx.x; rl < 128; rl += blockDim.x)
+            xns[rl] = lo + rl < hi ? __ldg(P.xnorm + I.row_off + lo + rl) : 0.0f;
+        }
+      }
       __syncthreads();
       float acc[4][4];
 #pragma unroll
@@ -328,16 +417,19 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
         constexpr int KVR = decltype(kvr_tag)::value;
         constexpr bool EV = decltype(ev_tag)::value;
         if (hi - lo == 128 * KVR)
-          batch_tile_columns<KVR, EV, true, CT>(P, I, T, f1s, acc, ms_hi, ms_lo, ob_hi, ob_lo,
-                                                lane, warp, W);
+          batch_tile_columns<KVR, EV, true, CT, DIM>(P, I, T, f1s, xs, xns, acc, ms_hi, ms_lo,
+                                                     ob_hi, ob_lo, lane, warp, W);
         else
-          batch_tile_columns<KVR, EV, false, CT>(P, I, T, f1s, acc, ms_hi, ms_lo, ob_hi, ob_lo,
-                                                 lane, warp, W);
+          batch_tile_columns<KVR, EV, false, CT, DIM>(P, I, T, f1s, xs, xns, acc, ms_hi, ms_lo,
+                                                      ob_hi, ob_lo, lane, warp, W);
       };
       using K1 = std::integral_constant<int, 1>;
       using K2 = std::integral_constant<int, 2>;
       using K4 = std::integral_constant<int, 4>;
-      if (even) {
+      if constexpr (DIM > 0) {  // point launches plan 128-row bands only
+        if (even) run(K1(), std::true_type());
+        else run(K1(), std::false_type());
+      } else if (even) {
         if (T.kvr == 1) run(K1(), std::true_type());
         else if (T.kvr == 2) run(K2(), std::true_type());
         else run(K4(), std::true_type());
@@ -500,7 +592,12 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
           if (r >= T.hi) continue;
           float xv[VEC], cv[VEC];
           load_vec<VEC>(xcol + r, xv);
-          load_c<VEC, CT>(ccol + r, cv);
+          if constexpr (DIM > 0) {
+#pragma unroll
+            for (int e = 0; e < VEC; ++e) cv[e] = r + e < T.hi ? point_cost<DIM>(P, I, r + e, j) : 0.0f;
+          } else {
+            load_c<VEC, CT>(ccol + r, cv);
+          }
 #pragma unroll
           for (int e = 0; e < VEC; ++e) xv[e] = fmaxf(fmaf(I.s, cv[e], xv[e]), 0.0f);
           if (r + VEC <= T.hi) store_vec<VEC>(xcol + r, xv);
@@ -535,6 +632,7 @@ static inline size_t al(size_t v) { return (v + kAl - 1) / kAl * kAl; }
 
 struct BatchPlanImpl {
   int n_inst = 0, n_tiles = 0, n_tiles_f = 0, grid = 0, threads = 256, cols_per_tile = 0;
+  int band_rows = 512;
   size_t smem = 0;
   long long rows = 0, cols = 0, rowpart = 0, colpart = 0;
   std::vector<BatchInst> inst;
@@ -543,7 +641,8 @@ struct BatchPlanImpl {
   // workspace layout
   size_t off_ctrl = 0, off_inst = 0, off_tiles = 0, off_items = 0, off_a = 0, off_b = 0,
          off_phi1 = 0, off_phi2 = 0, off_alpha = 0, off_rp = 0, off_cp = 0, off_tsum = 0,
-         off_tobj = 0, off_res = 0, off_obj = 0, off_conv = 0, off_stats = 0, total = 0;
+         off_tobj = 0, off_res = 0, off_obj = 0, off_conv = 0, off_stats = 0, off_xn = 0,
+         off_yn = 0, total = 0;
   bool uploaded_any = false;
 };
 
@@ -579,8 +678,8 @@ static void add_tiles(std::vector<BatchTile>& tiles, int k, const BatchInst& I, 
       T.inst = k;
       T.band = b;
       T.chunk = c;
-      T.lo = b * kBatchS;
-      T.hi = std::min(T.lo + kBatchS, I.nr);
+      T.lo = b * I.band_h;
+      T.hi = std::min(T.lo + I.band_h, I.nr);
       T.c0 = (int)(((long long)I.nc * c) / chunks);
       T.c1 = (int)(((long long)I.nc * (c + 1)) / chunks);
       const int h = T.hi - T.lo;
@@ -589,8 +688,11 @@ static void add_tiles(std::vector<BatchTile>& tiles, int k, const BatchInst& I, 
     }
 }
 
-static size_t batch_smem(int warps) {
-  return sizeof(float) * ((size_t)warps * kBatchS + kBatchS) + sizeof(double) * (2 * warps + 1);
+// Dynamic shared memory: row reduction [warps][512], phi1 stage [512], FP64
+// scratch, and for point launches the band's x (k-major) and norms.
+static size_t batch_smem(int warps, int dim) {
+  return sizeof(float) * ((size_t)warps * kBatchS + kBatchS) + sizeof(double) * (2 * warps + 1) +
+         16 /* alignment of the point stage */ + sizeof(float) * ((size_t)dim * 128 + 128);
 }
 
 }  // namespace drot
@@ -605,7 +707,13 @@ extern "C" {
 
 int drot_batch_plan_create(int n_inst, const drot_batch_instance* desc, int cols_per_tile,
                            drot_batch_plan* out) {
+  return drot_batch_plan_create_ex(n_inst, desc, cols_per_tile, 512, out);
+}
+
+int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int cols_per_tile,
+                              int band_rows, drot_batch_plan* out) {
   if (!out || n_inst <= 0 || n_inst > 65535 || !desc) return DROT_ERR_INVALID_ARG;
+  if (band_rows != 128 && band_rows != 512) return DROT_ERR_INVALID_ARG;
   *out = nullptr;
   if (cols_per_tile <= 0) cols_per_tile = 128;
   BatchPlanImpl P;
@@ -631,8 +739,8 @@ int drot_batch_plan_create(int n_inst, const drot_batch_instance* desc, int cols
     I.q_off = d.q_offset;
     // Bands of 512 rows; the last one takes the remainder and the narrowest
     // warp step (128, 256 or 512 rows x 4, 2 or 1 columns) that covers it.
-    I.band_h = kBatchS;
-    I.nbands = (d.n_rows + kBatchS - 1) / kBatchS;
+    I.band_h = band_rows;
+    I.nbands = (d.n_rows + band_rows - 1) / band_rows;
     I.P = (d.n_cols + cols_per_tile - 1) / cols_per_tile;
     I.Pf = (d.n_cols + fine_cols() - 1) / fine_cols();
     I.tile0 = (int)P.tiles.size();
@@ -704,15 +812,19 @@ int drot_batch_plan_create(int n_inst, const drot_batch_instance* desc, int cols
       cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
     return DROT_ERR_CUDA;
   P.threads = 256;
-  P.smem = batch_smem(P.threads / 32);
-  int occ_f = 0, occ_b = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, (const void*)batch_solve_kernel<float>,
-                                                    P.threads, P.smem) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &occ_b, (const void*)batch_solve_kernel<__nv_bfloat16>, P.threads, P.smem) !=
-          cudaSuccess)
-    return DROT_ERR_CUDA;
-  const int occ = std::min(occ_f, occ_b);
+  P.band_rows = band_rows;
+  P.smem = batch_smem(P.threads / 32, 16);  // sized for every kernel variant
+  const void* kernels[] = {(const void*)batch_solve_kernel<float, 0>,
+                           (const void*)batch_solve_kernel<__nv_bfloat16, 0>,
+                           (const void*)batch_solve_kernel<float, 8>,
+                           (const void*)batch_solve_kernel<float, 16>};
+  int occ = 1 << 30;
+  for (const void* fn : kernels) {
+    int o = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, P.threads, P.smem) != cudaSuccess)
+      return DROT_ERR_CUDA;
+    occ = std::min(occ, o);
+  }
   if (occ <= 0) return DROT_ERR_CUDA;
   P.grid = occ * sms;
 
@@ -734,6 +846,8 @@ int drot_batch_plan_create(int n_inst, const drot_batch_instance* desc, int cols
   P.off_obj = off;   off = al(off + sizeof(double) * n_inst);
   P.off_conv = off;  off = al(off + sizeof(int) * n_inst);
   P.off_stats = off; off = al(off + sizeof(BatchStat) * n_inst);
+  P.off_xn = off;    off = al(off + sizeof(float) * rows);
+  P.off_yn = off;    off = al(off + sizeof(float) * cols);
   P.total = off;
 
   drot_batch_plan h = new (std::nothrow) drot_batch_plan_s;
@@ -769,23 +883,12 @@ int drot_batch_upload(drot_batch_plan plan, void* workspace, size_t workspace_by
   return DROT_OK;
 }
 
-int drot_qr_batch_launch(drot_batch_plan plan, const void* c, int c_dtype, const float* p,
-                         const float* q, float* x, int max_iters, void* workspace,
-                         size_t workspace_bytes, drot_stream_t stream) {
-  if (!plan || !c || !p || !q || !x || !workspace || max_iters < 0) return DROT_ERR_INVALID_ARG;
-  if (c_dtype != DROT_C_F32 && c_dtype != DROT_C_BF16) return DROT_ERR_INVALID_ARG;
-  const BatchPlanImpl& P = plan->p;
+// Shared by the cost-matrix and the point-cloud launches: parameter block,
+// control words, warm start, then the cooperative solve kernel `fn`.
+static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, void* workspace,
+                        size_t workspace_bytes, int max_iters, cudaStream_t st) {
   if (workspace_bytes < P.total || ((uintptr_t)workspace & 255u)) return DROT_ERR_WORKSPACE;
-  if (((uintptr_t)x & 15u) || ((uintptr_t)c & (c_dtype == DROT_C_F32 ? 15u : 7u)))
-    return DROT_ERR_INVALID_ARG;
   char* ws = (char*)workspace;
-  cudaStream_t st = (cudaStream_t)stream;
-  BatchParams B;
-  memset(&B, 0, sizeof(B));
-  B.c = c;
-  B.p = p;
-  B.q = q;
-  B.x = x;
   B.inst = (const BatchInst*)(ws + P.off_inst);
   B.tiles = (const BatchTile*)(ws + P.off_tiles);
   B.n_inst = P.n_inst;
@@ -817,8 +920,10 @@ int drot_qr_batch_launch(drot_batch_plan plan, const void* c, int c_dtype, const
   if (cudaMemsetAsync(ws + P.off_ctrl, 0, 512, st) != cudaSuccess) return DROT_ERR_CUDA;
   batch_init_kernel<<<dim3(64, P.n_inst), 256, 0, st>>>(B);
   if (cudaGetLastError() != cudaSuccess) return DROT_ERR_CUDA;
-  const void* fn = c_dtype == DROT_C_F32 ? (const void*)batch_solve_kernel<float>
-                                         : (const void*)batch_solve_kernel<__nv_bfloat16>;
+  if (P.smem > 48 * 1024 &&
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem) !=
+          cudaSuccess)
+    return DROT_ERR_CUDA;
   void* args[] = {(void*)&B};
   if (cudaLaunchCooperativeKernel(fn, dim3(P.grid), dim3(P.threads), args, P.smem, st) !=
       cudaSuccess) {
@@ -826,6 +931,60 @@ int drot_qr_batch_launch(drot_batch_plan plan, const void* c, int c_dtype, const
     return DROT_ERR_CUDA;
   }
   return DROT_OK;
+}
+
+int drot_qr_batch_launch(drot_batch_plan plan, const void* c, int c_dtype, const float* p,
+                         const float* q, float* x, int max_iters, void* workspace,
+                         size_t workspace_bytes, drot_stream_t stream) {
+  if (!plan || !c || !p || !q || !x || !workspace || max_iters < 0) return DROT_ERR_INVALID_ARG;
+  if (c_dtype != DROT_C_F32 && c_dtype != DROT_C_BF16) return DROT_ERR_INVALID_ARG;
+  if (((uintptr_t)x & 15u) || ((uintptr_t)c & (c_dtype == DROT_C_F32 ? 15u : 7u)))
+    return DROT_ERR_INVALID_ARG;
+  BatchParams B;
+  memset(&B, 0, sizeof(B));
+  B.c = c;
+  B.p = p;
+  B.q = q;
+  B.x = x;
+  const void* fn = c_dtype == DROT_C_F32 ? (const void*)batch_solve_kernel<float, 0>
+                                         : (const void*)batch_solve_kernel<__nv_bfloat16, 0>;
+  return batch_launch(plan->p, fn, B, workspace, workspace_bytes, max_iters,
+                      (cudaStream_t)stream);
+}
+
+int drot_qr_batch_launch_points(drot_batch_plan plan, const float* xpts, const float* ypts,
+                                int dim, float cost_scale, const float* p, const float* q,
+                                float* x, int max_iters, void* workspace, size_t workspace_bytes,
+                                drot_stream_t stream) {
+  if (!plan || !xpts || !ypts || !p || !q || !x || !workspace || max_iters < 0)
+    return DROT_ERR_INVALID_ARG;
+  if (dim != 8 && dim != 16) return DROT_ERR_UNSUPPORTED;
+  if (plan->p.band_rows != 128) return DROT_ERR_INVALID_ARG;  // point tiles are 128-row bands
+  if (((uintptr_t)x & 15u) || ((uintptr_t)xpts & 15u) || ((uintptr_t)ypts & 15u))
+    return DROT_ERR_INVALID_ARG;
+  const BatchPlanImpl& P = plan->p;
+  if (workspace_bytes < P.total || ((uintptr_t)workspace & 255u)) return DROT_ERR_WORKSPACE;
+  char* ws = (char*)workspace;
+  cudaStream_t st = (cudaStream_t)stream;
+  BatchParams B;
+  memset(&B, 0, sizeof(B));
+  B.p = p;
+  B.q = q;
+  B.x = x;
+  B.xpts = xpts;
+  B.ypts = ypts;
+  B.xnorm = (const float*)(ws + P.off_xn);
+  B.ynorm = (const float*)(ws + P.off_yn);
+  B.cscale = cost_scale;
+  B.dim = dim;
+  point_norms_kernel<<<(int)std::min<long long>((P.rows + 255) / 256, 1024), 256, 0, st>>>(
+      xpts, (int)P.rows, dim, (float*)(ws + P.off_xn));
+  point_norms_kernel<<<(int)std::min<long long>((P.cols + 255) / 256, 1024), 256, 0, st>>>(
+      ypts, (int)P.cols, dim, (float*)(ws + P.off_yn));
+  if (cudaGetLastError() != cudaSuccess) return DROT_ERR_CUDA;
+  const void* fn = dim == 8 ? (const void*)batch_solve_kernel<float, 8>
+                            : (const void*)batch_solve_kernel<float, 16>;
+  return batch_launch(P, fn, B, workspace, workspace_bytes, max_iters, st);
 }
 
 int drot_batch_state(drot_batch_plan plan, void* workspace, float** phi1, float** phi2) {

@@ -125,6 +125,9 @@ SIGNATURES = {
     "drot_quadratic_drot_noalloc": (_c_int, [_vp, _vp, _vp, _c_int, _c_int, _c_float, _c_float,
                                              _c_int, _c_float, _vp, _RP, _vp]),
     "drot_batch_plan_create": (_c_int, [_c_int, _BIP, _c_int, ctypes.POINTER(_vp)]),
+    "drot_batch_plan_create_ex": (_c_int, [_c_int, _BIP, _c_int, _c_int, ctypes.POINTER(_vp)]),
+    "drot_qr_batch_launch_points": (_c_int, [_vp, _vp, _vp, _c_int, _c_float, _vp, _vp, _vp, _c_int,
+                                             _vp, _c_size, _vp]),
     "drot_batch_plan_destroy": (None, [_vp]),
     "drot_batch_plan_workspace_bytes": (_c_size, [_vp]),
     "drot_batch_plan_tiles": (_c_int, [_vp]),

@@ -172,8 +172,12 @@ def quadratic_drot_fn(c, p, q, rho, r_weight, max_iters, eps, *, cg_tol=CG_TOL,
 
 class BatchQuadraticDROTFn(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, c, p, q, batch, max_iters, cg_tol, cg_max_iters):
-        x, info = batch.solve(c.detach(), p.detach(), q.detach(), max_iters)
+    def forward(ctx, c, p, q, batch, max_iters, cg_tol, cg_max_iters, points):
+        if points is None:
+            x, info = batch.solve(c.detach(), p.detach(), q.detach(), max_iters)
+        else:  # the same cost recomputed from the clouds inside the solve
+            xs, ys, scale = points
+            x, info = batch.solve_points(xs, ys, p.detach(), q.detach(), max_iters, scale)
         if not all(r["converged"] for r in info):
             warnings.warn("batch_quadratic_drot_fn: some instances did not converge; the "
                           "implicit gradient assumes optimal plans")
@@ -214,17 +218,21 @@ class BatchQuadraticDROTFn(torch.autograd.Function):
             B.view(gc, k).copy_(g)
             gp.append(a)
             gq.append(b)
-        return gc.to(c.dtype), torch.cat(gp), torch.cat(gq), None, None, None, None
+        return gc.to(c.dtype), torch.cat(gp), torch.cat(gq), None, None, None, None, None
 
 
 def batch_quadratic_drot_fn(batch, c, p, q, max_iters, *, cg_tol=CG_TOL,
-                            cg_max_iters=CG_MAX_ITERS):
+                            cg_max_iters=CG_MAX_ITERS, points=None):
     """QRBatch.solve with a backward; c, p, q packed (QRBatch.pack_c /
-    pack_marginals), returns the packed plans (QRBatch.unpack gives views)."""
+    pack_marginals), returns the packed plans (QRBatch.unpack gives views).
+    points=(x_cat, y_cat, scale): the forward recomputes the cost from the
+    clouds inside the solve (QRBatch.solve_points; the batch must have
+    band_rows=128) -- c must hold the same cost (e.g. packed_sqeuclidean_cost
+    of the clouds); the backward reads it once."""
     if not all(r > 0 for r in batch.r_weight):
         raise RuntimeError("batch_quadratic_drot_fn needs r_weight > 0 for every instance")
     return BatchQuadraticDROTFn.apply(c, p, q, batch, int(max_iters), float(cg_tol),
-                                      int(cg_max_iters))
+                                      int(cg_max_iters), points)
 
 
 def gl_step_and_lambda(rho, r_weight, n_rows, n_cols, n_class):

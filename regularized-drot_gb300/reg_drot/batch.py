@@ -45,7 +45,8 @@ def _as_list(v, n, name):
 class QRBatch:
     """A fixed set of instance shapes and parameters, planned once."""
 
-    def __init__(self, shapes, rho, r_weight, eps, *, device=None, cols_per_tile=None):
+    def __init__(self, shapes, rho, r_weight, eps, *, device=None, cols_per_tile=None,
+                 band_rows=512):
         shapes = [(int(a), int(b)) for a, b in shapes]
         if not shapes:
             raise RuntimeError("QRBatch needs at least one instance")
@@ -85,6 +86,9 @@ class QRBatch:
         self._ws = None
         self._ws_plan = None
         self.cols_per_tile = cols_per_tile
+        if band_rows not in (128, 512):
+            raise RuntimeError("band_rows must be 128 or 512")
+        self.band_rows = band_rows  # 128: plans for point-cloud launches (solve_points)
 
     # ------------------------------------------------------------------ packing
     def pack_c(self, costs, dtype=torch.float32):
@@ -122,8 +126,8 @@ class QRBatch:
         if cpt not in self._plans:
             h = ctypes.c_void_p()
             with torch.cuda.device(self.device):
-                check(lib().drot_batch_plan_create(self.n, self._desc, cpt, ctypes.byref(h)),
-                      "batch_plan_create")
+                check(lib().drot_batch_plan_create_ex(self.n, self._desc, cpt, self.band_rows,
+                                                      ctypes.byref(h)), "batch_plan_create")
             self._plans[cpt] = h
         return self._plans[cpt]
 
@@ -170,6 +174,41 @@ class QRBatch:
                                         p.data_ptr(), q.data_ptr(), x.data_ptr(), int(max_iters),
                                         ptr, nbytes, s.cuda_stream)
         check(rc, "qr_batch_launch")
+
+    def launch_points(self, x_cat, y_cat, p, q, x, max_iters, scale=1.0, cols_per_tile=None,
+                      stream=None):
+        """Enqueue a point-cloud solve: instance k's cost is scale * |x_i - y_j|^2
+        of its points (x_cat, y_cat: every instance's points concatenated in
+        order, [rows, dim] / [cols, dim] float32, dim 8 or 16), recomputed in
+        the fused update instead of read from memory."""
+        if self.band_rows != 128:
+            raise RuntimeError("point-cloud solves need a QRBatch built with band_rows=128")
+        for t, name, n in ((x_cat, "x_cat", self.total_rows), (y_cat, "y_cat", self.total_cols)):
+            if t.device != self.device or t.dtype != torch.float32 or t.dim() != 2 or \
+                    t.size(0) != n or t.size(1) not in (8, 16) or not t.is_contiguous():
+                raise RuntimeError(f"{name} must be a contiguous float32 [{n}, 8 or 16] tensor")
+        if x_cat.size(1) != y_cat.size(1):
+            raise RuntimeError("x_cat and y_cat must have the same dimension")
+        cpt = cols_per_tile or self.cols_per_tile or 512
+        h, ptr, nbytes = self.workspace_for(cpt, stream)
+        s = torch.cuda.current_stream(self.device) if stream is None else stream
+        rc = lib().drot_qr_batch_launch_points(h, x_cat.data_ptr(), y_cat.data_ptr(), x_cat.size(1),
+                                               float(scale), p.data_ptr(), q.data_ptr(),
+                                               x.data_ptr(), int(max_iters), ptr, nbytes,
+                                               s.cuda_stream)
+        check(rc, "qr_batch_launch_points")
+
+    def solve_points(self, x_cat, y_cat, p, q, max_iters, scale=1.0, *, out=None, stream=None,
+                     sync=True):
+        """solve() with the cost recomputed from point clouds (launch_points)."""
+        x = self.empty_x() if out is None else out
+        with torch.cuda.device(self.device):
+            if self.cols_per_tile is None:
+                self.cols_per_tile = 512
+            self.launch_points(x_cat.detach(), y_cat.detach(), p, q, x, max_iters, scale,
+                               stream=stream)
+            info = self.results(stream) if sync else None
+        return x, info
 
     def results(self, stream=None):
         """Per-instance records of the last launch (waits for the stream)."""

@@ -1,0 +1,131 @@
+"""GPU: batched solves whose cost is recomputed from point clouds inside the
+fused update (drot_qr_batch_launch_points; QRBatch.solve_points).
+
+The cost C_ij = scale * max(|x_i|^2 + |y_j|^2 - 2 <x_i, y_j>, 0) is never
+stored; each iteration that reads C recomputes it in FP32 (FMA, k
+ascending).  Checks: against the FP32 oracle on the FP64 cost rounded to
+FP32 (the two costs differ by FP32 rounding, about 1e-7 relative), against
+the same batch solved on the stored cost of the tensor-core kernel, and the
+autograd path with a point-cloud forward.  Bars as for the other batch
+tests: ||X - X_ref||_F <= 1e-5 ||X_ref||_F (max entry 1e-4), n_iter within
+one stop check.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+from oracle import adjoint as A  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+SHAPES = [(64, 96), (300, 257), (513, 200), (130, 1100), (1000, 700), (2, 3), (257, 129)]
+SCALE = 1.0 / 64
+
+
+def _clouds(shapes, dim, seed):
+    rng = np.random.default_rng(seed)
+    xs = [rng.normal(size=(m, dim)).astype(np.float32) for m, _ in shapes]
+    ys = [rng.normal(size=(n, dim)).astype(np.float32) for _, n in shapes]
+    ps = [rng.dirichlet(np.ones(m)).astype(np.float32) for m, _ in shapes]
+    qs = [rng.dirichlet(np.ones(n)).astype(np.float32) for _, n in shapes]
+    return xs, ys, ps, qs
+
+
+def _close(xg, xo):
+    xg = np.asarray(xg, np.float64)
+    xo = np.asarray(xo, np.float64)
+    fro = np.linalg.norm(xg - xo) / np.linalg.norm(xo)
+    mx = np.abs(xg - xo).max() / np.abs(xo).max()
+    return fro <= 1e-5 and mx <= 1e-4, (fro, mx)
+
+
+@pytest.mark.parametrize("dim", [8, 16])
+def test_points_solve_matches_oracle(cuda, solver_lib, dim):
+    from reg_drot.batch import QRBatch
+    xs, ys, ps, qs = _clouds(SHAPES, dim, dim)
+    B = QRBatch(SHAPES, 2.0, 1e-3, 1e-5, device=cuda, band_rows=128, cols_per_tile=256)
+    p, q = B.pack_marginals([torch.tensor(v) for v in ps], [torch.tensor(v) for v in qs])
+    xc = torch.tensor(np.concatenate(xs), device=cuda)
+    yc = torch.tensor(np.concatenate(ys), device=cuda)
+    x, info = B.solve_points(xc, yc, p, q, 50000, SCALE)
+    for k in range(len(SHAPES)):
+        c = (A.sqeuclidean(xs[k], ys[k]) * SCALE).astype(np.float32)
+        o = O.quadratic_drot(c, ps[k], qs[k], 2.0, 1e-3, 50000, 1e-5)
+        assert info[k]["converged"] == 1
+        assert abs(info[k]["n_iter"] - o["n_iter"]) <= 2, (k, info[k], o["n_iter"])
+        if info[k]["n_iter"] == o["n_iter"]:
+            ok, err = _close(B.view(x, k).cpu().numpy(), o["x"])
+            assert ok, (k, err)
+
+
+def test_points_solve_matches_stored_cost_solve(cuda, solver_lib):
+    from reg_drot.batch import QRBatch
+    from reg_drot.cost import packed_sqeuclidean_cost
+    xs, ys, ps, qs = _clouds(SHAPES, 16, 3)
+    xc = torch.tensor(np.concatenate(xs), device=cuda)
+    yc = torch.tensor(np.concatenate(ys), device=cuda)
+    B = QRBatch(SHAPES, 2.0, 1e-3, 1e-5, device=cuda, band_rows=128, cols_per_tile=256)
+    p, q = B.pack_marginals([torch.tensor(v) for v in ps], [torch.tensor(v) for v in qs])
+    c = packed_sqeuclidean_cost(B, xc, yc, SCALE)
+    x1, i1 = B.solve(c, p, q, 50000)
+    x1 = x1.clone()
+    x2, i2 = B.solve_points(xc, yc, p, q, 50000, SCALE)
+    for k in range(len(SHAPES)):
+        assert abs(i1[k]["n_iter"] - i2[k]["n_iter"]) <= 2
+        if i1[k]["n_iter"] == i2[k]["n_iter"]:
+            ok, err = _close(B.view(x2, k).cpu().numpy(), B.view(x1, k).cpu().numpy())
+            assert ok, (k, err)
+
+
+def test_points_fixed_iterations_and_determinism(cuda, solver_lib):
+    from reg_drot.batch import QRBatch
+    xs, ys, ps, qs = _clouds(SHAPES, 8, 5)
+    xc = torch.tensor(np.concatenate(xs), device=cuda)
+    yc = torch.tensor(np.concatenate(ys), device=cuda)
+    B = QRBatch(SHAPES, 2.0, 1e-3, 0.0, device=cuda, band_rows=128, cols_per_tile=128)
+    p, q = B.pack_marginals([torch.tensor(v) for v in ps], [torch.tensor(v) for v in qs])
+    for mi in (1, 2, 9):
+        x, info = B.solve_points(xc, yc, p, q, mi, SCALE)
+        x = x.clone()
+        x2, _ = B.solve_points(xc, yc, p, q, mi, SCALE)
+        assert torch.equal(x, x2)
+        for k in range(len(SHAPES)):
+            c = (A.sqeuclidean(xs[k], ys[k]) * SCALE).astype(np.float32)
+            o = O.quadratic_drot(c, ps[k], qs[k], 2.0, 1e-3, mi, 0.0)
+            assert info[k]["n_iter"] == mi + 1
+            ok, err = _close(B.view(x, k).cpu().numpy(), o["x"])
+            assert ok, (mi, k, err)
+
+
+def test_points_need_128_row_plans(cuda, solver_lib):
+    from reg_drot.batch import QRBatch
+    xs, ys, ps, qs = _clouds(SHAPES[:2], 8, 1)
+    B = QRBatch(SHAPES[:2], 2.0, 1e-3, 1e-4, device=cuda)  # 512-row bands
+    p, q = B.pack_marginals([torch.tensor(v) for v in ps], [torch.tensor(v) for v in qs])
+    with pytest.raises(RuntimeError):
+        B.solve_points(torch.tensor(np.concatenate(xs), device=cuda),
+                       torch.tensor(np.concatenate(ys), device=cuda), p, q, 10, SCALE)
+
+
+def test_points_forward_in_autograd(cuda, solver_lib):
+    from reg_drot.autograd import batch_quadratic_drot_fn
+    from reg_drot.batch import QRBatch
+    from reg_drot.cost import packed_sqeuclidean_cost
+    shapes = SHAPES[:4]
+    xs, ys, ps, qs = _clouds(shapes, 16, 9)
+    grads = []
+    for use_points in (False, True):
+        xc = torch.tensor(np.concatenate(xs), device=cuda, requires_grad=True)
+        yc = torch.tensor(np.concatenate(ys), device=cuda, requires_grad=True)
+        B = QRBatch(shapes, 2.0, 1e-2, 1e-7, device=cuda, band_rows=128, cols_per_tile=256)
+        p, q = B.pack_marginals([torch.tensor(v) for v in ps], [torch.tensor(v) for v in qs])
+        c = packed_sqeuclidean_cost(B, xc, yc, SCALE)
+        pts = (xc.detach(), yc.detach(), SCALE) if use_points else None
+        X = batch_quadratic_drot_fn(B, c, p, q, 200000, points=pts)
+        ((c * X).sum() + 0.3 * (X * X).sum()).backward()
+        grads.append((xc.grad.cpu().numpy(), yc.grad.cpu().numpy()))
+    for a, b in zip(grads[0], grads[1]):
+        rel = np.linalg.norm(a - b) / np.linalg.norm(a)
+        assert rel <= 2e-3, rel
