@@ -128,6 +128,26 @@ int drot_gl_solve(const float *c, const float *p, const float *q, int n_rows,
                   size_t workspace_bytes, drot_result *result,
                   drot_stream_t stream);
 
+/* The loop of the reference's numpy solvers (numpy/npdrot/solver.py:7-189:
+ * regdrot with trace_nonnegative_quad_prox or trace_nonnegative_l1l2_prox)
+ * on the device.  mode 0: QR with divisor scale_or_lambda (= 1 + step*reg);
+ * the stop test runs on every iteration with residual <= eps, and X is
+ * returned unfolded whatever the last step.  mode 1: GL with threshold
+ * scale_or_lambda (= reg*step) over the caller's contiguous row groups
+ * [bounds[g], bounds[g+1]) (bounds[0] = 0, bounds[n_groups] = n_rows,
+ * increasing; numpy's `groups` pairs).  State in / state out as in
+ * drot_qr_solve; the numpy loop's final extra prox is one more call with
+ * max_iters = 1. */
+size_t drot_np_workspace_bytes(int mode, int n_rows, int n_cols, int n_groups,
+                               const int *bounds);
+int drot_np_solve(int mode, const void *c, int c_dtype, const float *p,
+                  const float *q, int n_rows, int n_cols, int n_groups,
+                  const int *bounds, float step_size, float scale_or_lambda,
+                  int max_iters, float eps, float *x, float *a, float *b,
+                  float *phi1, float *phi2, float *alpha, void *workspace,
+                  size_t workspace_bytes, drot_result *result,
+                  drot_stream_t stream);
+
 /* drot_qr_solve / drot_gl_solve with the cost matrix stored as c_dtype
  * (DROT_C_F32 or DROT_C_BF16).  No counterpart in the reference (its C is
  * float only); the FP32 case is exactly drot_qr_solve / drot_gl_solve. */

@@ -170,7 +170,7 @@ static int reg_warps() {
 // Build the launch plan for one data path (tma: shared-memory TMA ring, else
 // register loads).  Returns a drot_status.
 static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma, int ctype,
-                              Plan& pl) {
+                              Plan& pl, const int* ubounds) {
   if (nr <= 0 || nc <= 0) return DROT_ERR_INVALID_ARG;
   if (tma && vec != 4) return DROT_ERR_UNSUPPORTED;
   const DeviceInfo dev = device_info();
@@ -189,7 +189,8 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
     if (G <= 0) return DROT_ERR_INVALID_ARG;
     if (G > kMaxGroups) return DROT_ERR_UNSUPPORTED;
     pl.bounds.resize(G + 1);
-    group_bounds(nr, G, pl.bounds.data());
+    if (ubounds) std::copy(ubounds, ubounds + G + 1, pl.bounds.begin());
+    else group_bounds(nr, G, pl.bounds.data());
     int hmax = 0;
     for (int g = 0; g < G; ++g) {
       const int lo = pl.bounds[g];
@@ -321,10 +322,11 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
 // occupancy calculator, which costs microseconds per call.
 struct PlanKey {
   int dev, mode, nr, nc, G, vec, tma, warps, ctas, ctype;
+  std::vector<int> ubounds;  // caller's GL group boundaries (empty: the reference's)
   bool operator==(const PlanKey& o) const {
     return dev == o.dev && mode == o.mode && nr == o.nr && nc == o.nc && G == o.G &&
            vec == o.vec && tma == o.tma && warps == o.warps && ctas == o.ctas &&
-           ctype == o.ctype;
+           ctype == o.ctype && ubounds == o.ubounds;
   }
 };
 
@@ -332,18 +334,20 @@ static std::mutex g_plan_mu;
 static std::vector<std::pair<PlanKey, Plan>> g_plans;
 
 static int make_plan(int mode, int nr, int nc, int G, int vec, bool tma, Plan& pl,
-                     int ctype = DROT_C_F32) {
+                     int ctype = DROT_C_F32, const int* ubounds = nullptr) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return DROT_ERR_CUDA;
-  const PlanKey key = {dev, mode, nr, nc, mode == MODE_GL ? G : 0, vec, tma ? 1 : 0,
-                       tma ? tma_warps() : reg_warps(),
-                       tma && getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1, ctype};
+  PlanKey key = {dev, mode, nr, nc, mode == MODE_GL ? G : 0, vec, tma ? 1 : 0,
+                 tma ? tma_warps() : reg_warps(),
+                 tma && getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1, ctype, {}};
+  if (mode == MODE_GL && ubounds) key.ubounds.assign(ubounds, ubounds + G + 1);
   {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     for (auto& e : g_plans)
       if (e.first == key) { pl = e.second; return DROT_OK; }
   }
-  const int rc = make_plan_uncached(mode, nr, nc, G, vec, tma, ctype, pl);
+  const int rc = make_plan_uncached(mode, nr, nc, G, vec, tma, ctype, pl,
+                                    mode == MODE_GL ? ubounds : nullptr);
   if (rc == DROT_OK) {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     if (g_plans.size() >= 64) g_plans.erase(g_plans.begin());
@@ -367,21 +371,24 @@ static int path_override() {
 // 8-warp CTAs per SM with register-resident segments beat one 16-warp CTA
 // fed by the shared-memory TMA ring.  DROT_PATH=tma selects the ring.
 static int choose_plan(int mode, int nr, int nc, int G, bool aligned4, Plan& pl,
-                       int ctype = DROT_C_F32) {
+                       int ctype = DROT_C_F32, const int* ubounds = nullptr) {
   const int ov = path_override();
   if (ov == 2 && ctype == DROT_C_F32) {
     if (!aligned4) return DROT_ERR_UNSUPPORTED;
-    return make_plan(mode, nr, nc, G, 4, true, pl);
+    return make_plan(mode, nr, nc, G, 4, true, pl, DROT_C_F32, ubounds);
   }
-  return make_plan(mode, nr, nc, G, aligned4 ? 4 : 1, false, pl, ctype);
+  return make_plan(mode, nr, nc, G, aligned4 ? 4 : 1, false, pl, ctype, ubounds);
 }
 
-static size_t scratch_bytes(int mode, int nr, int nc, int G) {
+static size_t scratch_bytes(int mode, int nr, int nc, int G, const int* ubounds = nullptr) {
   size_t best = 0;
   Plan pl;
-  if (make_plan(mode, nr, nc, G, 4, true, pl) == DROT_OK) best = std::max(best, pl.total);
-  if (make_plan(mode, nr, nc, G, 4, false, pl) == DROT_OK) best = std::max(best, pl.total);
-  if (make_plan(mode, nr, nc, G, 1, false, pl) == DROT_OK) best = std::max(best, pl.total);
+  if (make_plan(mode, nr, nc, G, 4, true, pl, DROT_C_F32, ubounds) == DROT_OK)
+    best = std::max(best, pl.total);
+  if (make_plan(mode, nr, nc, G, 4, false, pl, DROT_C_F32, ubounds) == DROT_OK)
+    best = std::max(best, pl.total);
+  if (make_plan(mode, nr, nc, G, 1, false, pl, DROT_C_F32, ubounds) == DROT_OK)
+    best = std::max(best, pl.total);
   return best;
 }
 
@@ -409,6 +416,8 @@ struct SolveArgs {
   void* ws;
   size_t ws_bytes;
   cudaStream_t stream;
+  const int* bounds = nullptr;  // GL: caller's group boundaries (null: the reference's)
+  int stop_every = 0, stop_le = 0;  // numpy-API stop rule (QR)
 };
 
 static int read_stats(const void* ws, drot_result* r, cudaStream_t stream) {
@@ -438,7 +447,7 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
   const bool c_aligned = A.ctype == DROT_C_F32 ? aligned16(A.c) : (((uintptr_t)A.c & 7u) == 0);
   const bool aligned4 = ld % 4 == 0 && aligned16(A.x) && c_aligned;
   Plan pl;
-  int rc = choose_plan(A.mode, A.nr, A.nc, A.G, aligned4, pl, A.ctype);
+  int rc = choose_plan(A.mode, A.nr, A.nc, A.G, aligned4, pl, A.ctype, A.bounds);
   if (rc != DROT_OK) return rc;
   if (A.ws_bytes < pl.total) return DROT_ERR_WORKSPACE;
 
@@ -456,6 +465,8 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
   prm.nr_rcp = (float)(1.0 / (double)(float)A.nr);
   prm.norm_eps = 1e-9;
   prm.max_iters = A.max_iters;
+  prm.stop_every = A.stop_every;
+  prm.stop_le = A.stop_le;
   prm.nbands = pl.nbands; prm.P = pl.P; prm.Wt = pl.wt; prm.nsb = pl.nsb;
   prm.band_h = pl.band_h;
   prm.ns = pl.ns;
@@ -644,6 +655,42 @@ int drot_gl_solve(const float* c, const float* p, const float* q, int n_rows, in
   return drot_gl_solve_ex(c, DROT_C_F32, p, q, n_rows, n_cols, n_groups, step_size, lambda,
                           max_iters, eps, x, a, b, phi1, phi2, alpha, workspace, workspace_bytes,
                           result, stream);
+}
+
+static bool valid_bounds(int nr, int G, const int* b) {
+  if (!b || G <= 0 || G > kMaxGroups || b[0] != 0 || b[G] != nr) return false;
+  for (int g = 0; g < G; ++g)
+    if (b[g + 1] <= b[g]) return false;
+  return true;
+}
+
+size_t drot_np_workspace_bytes(int mode, int n_rows, int n_cols, int n_groups,
+                               const int* bounds) {
+  if (n_rows <= 0 || n_cols <= 0) return 0;
+  if (mode == MODE_QR) return scratch_bytes(MODE_QR, n_rows, n_cols, 0);
+  if (mode != MODE_GL || !valid_bounds(n_rows, n_groups, bounds)) return 0;
+  return scratch_bytes(MODE_GL, n_rows, n_cols, n_groups, bounds);
+}
+
+int drot_np_solve(int mode, const void* c, int c_dtype, const float* p, const float* q,
+                  int n_rows, int n_cols, int n_groups, const int* bounds, float step_size,
+                  float scale_or_lambda, int max_iters, float eps, float* x, float* a, float* b,
+                  float* phi1, float* phi2, float* alpha, void* workspace,
+                  size_t workspace_bytes, drot_result* result, drot_stream_t stream) {
+  if (mode == MODE_QR) {
+    SolveArgs A = {MODE_QR, c, c_dtype, p, q, n_rows, n_cols, 0, step_size, scale_or_lambda,
+                   0.0f, max_iters, eps, x, a, b, phi1, phi2, alpha, workspace,
+                   workspace_bytes, (cudaStream_t)stream};
+    A.stop_every = 1;
+    A.stop_le = 1;
+    return run_solve(A, result);
+  }
+  if (mode != MODE_GL || !valid_bounds(n_rows, n_groups, bounds)) return DROT_ERR_INVALID_ARG;
+  SolveArgs A = {MODE_GL, c, c_dtype, p, q, n_rows, n_cols, n_groups, step_size, 1.0f,
+                 scale_or_lambda, max_iters, eps, x, a, b, phi1, phi2, alpha, workspace,
+                 workspace_bytes, (cudaStream_t)stream};
+  A.bounds = bounds;
+  return run_solve(A, result);
 }
 
 int drot_read_result(const void* workspace, drot_result* result, drot_stream_t stream) {

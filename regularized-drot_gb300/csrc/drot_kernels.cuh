@@ -91,6 +91,8 @@ struct SolveParams {
   float eps;           // absolute residual tolerance
   double norm_eps;     // GL: constant added to the group norm (1e-9)
   int max_iters;
+  int stop_every;      // QR: test every iteration (numpy-API loop), not only even ones
+  int stop_le;         // QR: stop on residual <= eps (numpy-API loop) instead of < eps
   int nbands;          // QR: row bands; GL: groups
   int P;               // CTAs per band (column chunks)
   int Wt;              // warps per team (sub-bands per band)
@@ -845,7 +847,7 @@ drot_solve_kernel(const SolveParams P) {
     //     (float tree, fixed order) and updates the marginal residuals and
     //     the duals a, b; (dual - residual) is staged until gamma is known;
     // (c) one block sync, then phi = (staged + gamma) / n_cols (or n_rows).
-    const bool check = (MODE == MODE_GL) || even;
+    const bool check = (MODE == MODE_GL) || even || P.stop_every;
     if (warp == 0) {
       const double t = warp_sum_strided(P.cta_sum, G, lane);
       if (lane == 0) {
@@ -920,8 +922,8 @@ drot_solve_kernel(const SolveParams P) {
       }
       __syncthreads();
       last_res = sqrt(s_misc_d[1]);
-      const bool stop = (MODE == MODE_QR) ? (last_res < (double)P.eps)
-                                          : (last_res <= (double)P.eps);
+      const bool stop = (MODE == MODE_QR && !P.stop_le) ? (last_res < (double)P.eps)
+                                                        : (last_res <= (double)P.eps);
       if (stop) {
         converged = true;
         stamp(4);
@@ -932,8 +934,13 @@ drot_solve_kernel(const SolveParams P) {
   }
 
   // ------------------------------------------------------------ epilogue
-  if (MODE == MODE_QR && converged && active_warp) {
-    // fix_x (kernel_qr.hpp:469-482): undo the fold of the last even step.
+  // fix_x (kernel_qr.hpp:469-482): undo the fold of the last step when it
+  // was even and the solve converged -- or, in the numpy-API loop
+  // (stop_every), whenever it ends on an even step (that loop always hands
+  // back an unfolded X).  An odd last step stores X as is.
+  const int last_it = converged ? it : it - 1;
+  if (MODE == MODE_QR && (converged || P.stop_every) && last_it >= 0 && (last_it & 1) == 0 &&
+      !aborted && active_warp) {
     for (int j = c0 + team; j < c1; j += nteams) {
       float* xcol = P.x + (long long)j * ld;
       const CT* ccol = cbase + (long long)j * ld;

@@ -98,6 +98,10 @@ SIGNATURES = {
                                _c_int, _c_float, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _c_size,
                                _RP, _vp]),
     "drot_read_result": (_c_int, [_vp, _RP, _vp]),
+    "drot_np_workspace_bytes": (_c_size, [_c_int, _c_int, _c_int, _c_int, _ip]),
+    "drot_np_solve": (_c_int, [_c_int, _vp, _c_int, _vp, _vp, _c_int, _c_int, _c_int, _ip, _c_float,
+                               _c_float, _c_int, _c_float, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                               _c_size, _RP, _vp]),
     "drot_qr_solve_ex": (_c_int, [_vp, _c_int, _vp, _vp, _c_int, _c_int, _c_float, _c_float,
                                   _c_int, _c_float, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _c_size,
                                   _RP, _vp]),
