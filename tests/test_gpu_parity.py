@@ -16,8 +16,9 @@ the iterates agree to FP32 rounding:
   * objective within 1e-5 relative,
   * the same iteration count (a tie at the stop threshold may move the stop
     by one check: 2 iterations for QR, 1 for GL).
-Each parity case runs on both data paths: the TMA shared-memory ring
-(default for 16-byte aligned data) and the register path (DROT_PATH=reg).
+Each parity case runs on both data paths: the register path (the default,
+DROT_PATH=reg) and the TMA shared-memory ring (DROT_PATH=tma, shapes with
+n_rows % 4 == 0).
 """
 import ctypes
 import json
@@ -37,13 +38,16 @@ RTOL_XMAX = 1e-4    # relative max-entry error on X
 RTOL_OBJ = 1e-5
 
 
-@pytest.fixture(params=["default", "reg"])
+@pytest.fixture(params=["reg", "tma"])
 def path(request, monkeypatch):
-    if request.param == "reg":
-        monkeypatch.setenv("DROT_PATH", "reg")
-    else:
-        monkeypatch.delenv("DROT_PATH", raising=False)
+    monkeypatch.setenv("DROT_PATH", request.param)
     return request.param
+
+
+def _tma_needs_aligned_rows(path, nr):
+    """The TMA ring needs 16-byte aligned columns (n_rows % 4 == 0)."""
+    if path == "tma" and nr % 4:
+        pytest.skip("TMA path: n_rows % 4 != 0")
 
 
 def _problem(nr, nc, seed, marg="uniform"):
@@ -91,6 +95,7 @@ QR_CASES = [
                          ids=[f"{c[0]}x{c[1]}" for c in QR_CASES])
 def test_quadratic_drot_matches_oracle(cuda, path, nr, nc, rho, rw, eps, mi):
     import reg_drot
+    _tma_needs_aligned_rows(path, nr)
     c, p, q = _problem(nr, nc, seed=nr * 7 + nc)
     x, info, _ = reg_drot.solve_qr(c.to(cuda), p.to(cuda), q.to(cuda), rho, rw, mi, eps)
     o = O.quadratic_drot(c.numpy(), p.numpy(), q.numpy(), rho, rw, mi, eps)
@@ -131,6 +136,7 @@ def test_group_lasso_drot_matches_oracle(cuda, path, nr, nc, G, rho, rw, eps, mi
     on the objective.
     """
     import reg_drot
+    _tma_needs_aligned_rows(path, nr)
     c, p, q = _problem(nr, nc, seed=nr * 11 + nc + G)
     x, info, _ = reg_drot.solve_gl(c.to(cuda), p.to(cuda), q.to(cuda), G, rho, rw, mi, eps)
     o32 = O.group_lasso_drot(c.numpy(), p.numpy(), q.numpy(), G, rho, rw, mi, eps)
@@ -181,6 +187,8 @@ def test_first_iteration_is_bitwise_identical_to_oracle(cuda, path):
     import reg_drot
     for kind in ("qr", "gl"):
         for nr, nc in ((1000, 333), (777, 129)):
+            if path == "tma" and nr % 4:
+                continue
             c, p, q = _problem(nr, nc, seed=nr)
             if kind == "qr":
                 x, _, _ = reg_drot.solve_qr(c.to(cuda), p.to(cuda), q.to(cuda), 2.0, 1e-2, 1, 0.0)
