@@ -184,6 +184,12 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
     // Four 128-bit vectors per lane (512-row sub-bands); short panels use
     // fewer so lanes are not left idle.
     pl.kv = nr <= SV ? 1 : (nr <= 2 * SV ? 2 : 4);
+    // DROT_QR_KV (1, 2 or 4) caps the vectors per lane: shorter bands, fewer
+    // registers per thread, more CTAs per SM (tuning knob).
+    if (const char* e = getenv("DROT_QR_KV")) {
+      const int k = atoi(e);
+      if (k == 1 || k == 2 || k == 4) pl.kv = std::min(pl.kv, k);
+    }
     pl.wt = 1;
   } else {
     if (G <= 0) return DROT_ERR_INVALID_ARG;
@@ -323,10 +329,11 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
 struct PlanKey {
   int dev, mode, nr, nc, G, vec, tma, warps, ctas, ctype;
   std::vector<int> ubounds;  // caller's GL group boundaries (empty: the reference's)
+  int qr_kv;                 // DROT_QR_KV knob
   bool operator==(const PlanKey& o) const {
     return dev == o.dev && mode == o.mode && nr == o.nr && nc == o.nc && G == o.G &&
            vec == o.vec && tma == o.tma && warps == o.warps && ctas == o.ctas &&
-           ctype == o.ctype && ubounds == o.ubounds;
+           ctype == o.ctype && ubounds == o.ubounds && qr_kv == o.qr_kv;
   }
 };
 
@@ -339,7 +346,8 @@ static int make_plan(int mode, int nr, int nc, int G, int vec, bool tma, Plan& p
   if (cudaGetDevice(&dev) != cudaSuccess) return DROT_ERR_CUDA;
   PlanKey key = {dev, mode, nr, nc, mode == MODE_GL ? G : 0, vec, tma ? 1 : 0,
                  tma ? tma_warps() : reg_warps(),
-                 tma && getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1, ctype, {}};
+                 tma && getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1, ctype, {},
+                 getenv("DROT_QR_KV") ? atoi(getenv("DROT_QR_KV")) : 0};
   if (mode == MODE_GL && ubounds) key.ubounds.assign(ubounds, ubounds + G + 1);
   {
     std::lock_guard<std::mutex> lk(g_plan_mu);
