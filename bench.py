@@ -263,7 +263,60 @@ def hbm_point(dev, flush):
             "phase_us_per_iteration_cta0": [round(v * 1e3, 2) for v in ph]}
 
 
-def gl_da_point(dev):
+def config_points(dev, flush):
+    """The other single-instance configurations: QR 1000^2 on N(0, I_2) clouds
+    (the reference's CPU-runnable case; GPU solve and the oracle solve on the
+    host cores), and the 3000^2 workload at alpha 1e-2 and 1e-4 and with the
+    cost stored in BF16 (alpha 1e-3)."""
+    import torch
+    import reg_drot
+    from oracle import oracle as O
+    out = {}
+
+    def timed(fn):
+        fn()
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        r = fn()
+        b.record()
+        b.synchronize()
+        return a.elapsed_time(b) / 1e3, r
+
+    rng = np.random.default_rng(SEED)
+    xs = rng.normal(size=(1000, 2))
+    yt = rng.normal(size=(1000, 2))
+    C = ((yt[:, None, :] - xs[None, :, :]) ** 2).sum(-1)
+    C = (C / C.max()).astype(np.float32)
+    p1 = np.full(1000, 1e-3, np.float32)
+    eps1 = REL_EPS * math.sqrt(2 * 1000 * 1e-6)
+    c1, pp1 = torch.from_numpy(C).to(dev), torch.from_numpy(p1).to(dev)
+    t, (x, info, _) = timed(lambda: reg_drot.solve_qr(c1, pp1, pp1, RHO, ALPHA, 10 ** 6, eps1))
+    t0 = time.perf_counter()
+    o = O.quadratic_drot(C, p1, p1, RHO, ALPHA, 10 ** 6, eps1)
+    t_cpu = time.perf_counter() - t0
+    out["config1_qr_1000_clouds"] = {
+        "workload": "QR-DROT 1000x1000, C = sq. Euclidean of N(0,I_2) clouds / max, uniform "
+                    f"marginals, alpha={ALPHA}, relative eps {REL_EPS}",
+        "gpu_s_per_solve": t, "n_iter": info["n_iter"], "cpu_oracle_s_per_solve": t_cpu,
+        "cpu_oracle_n_iter": o["n_iter"], "cpu_threads": int(O.lib().oracle_max_threads())}
+    c, p, q, eps = make_problem(N, SEED)
+    cd, pd, qd = (torch.from_numpy(a).to(dev) for a in (c, p, q))
+    for alpha in (1e-2, 1e-4):
+        t, (x, info, _) = timed(lambda: reg_drot.solve_qr(cd, pd, qd, RHO, alpha, 10 ** 7, eps))
+        out[f"config2_qr_3000_alpha_{alpha:g}"] = {
+            "s_per_solve": t, "n_iter": info["n_iter"], "converged": info["converged"],
+            "objective": info["objective_f64"], "residual": info["residual"]}
+    cb = cd.to(torch.bfloat16)
+    t, (x, info, _) = timed(lambda: reg_drot.solve_qr(cb, pd, qd, RHO, ALPHA, 10 ** 7, eps))
+    out["config2_qr_3000_bf16_cost"] = {
+        "s_per_solve": t, "n_iter": info["n_iter"], "converged": info["converged"],
+        "objective": info["objective_f64"], "residual": info["residual"],
+        "note": "the solve of the BF16-rounded cost (FP32 iterates)"}
+    return out
+
+
+def gl_da_point(dev, gl_weight=1e-3):
     """Group-lasso domain-adaptation solve (1500 source x 1000 target, 2 classes)."""
     import reg_drot  # noqa: F401
     from reg_drot import _lib
@@ -289,14 +342,14 @@ def gl_da_point(dev):
         nit, obj = ctypes.c_int(), ctypes.c_float()
         for rep in range(2):
             ptr = L.drot_gl_wrapper(cm.ctypes.data, p.ctypes.data, q.ctypes.data, ns, nt, 2, s,
-                                    1e-3, 20000, 1e-4, ctypes.byref(dur), ctypes.byref(prep),
+                                    gl_weight, 20000, 1e-4, ctypes.byref(dur), ctypes.byref(prep),
                                     ctypes.byref(nit), ctypes.byref(obj), 1, 0)
         times.append(dur.value / 1e3)
         iters.append(nit.value)
-    return {"workload": "GL-DROT domain adaptation 1500 src x 1000 tgt, 2 classes, GL weight 1e-3 "
+    return {"workload": f"GL-DROT domain adaptation 1500 src x 1000 tgt, 2 classes, GL weight {gl_weight:g} "
                         "(C++ wrapper convention), eps 1e-4, rho 2, 20000 max iterations",
             "median_solve_s": statistics.median(times), "median_iterations": statistics.median(iters),
-            "published_v100_median_s": 0.0619}
+            "published_v100_median_s": 0.0619 if gl_weight == 1e-3 else None}
 
 
 BATCH_INSTANCES = 256
@@ -574,6 +627,7 @@ def run_gpu(args):
 
     e2e = e2e_wrapper(c, p, q, eps, args.steps)
     extra = {"hbm_point": hbm_point(dev, flush), "gl_da": gl_da_point(dev),
+             "gl_da_weight_5e-3": gl_da_point(dev, 5e-3), "configs": config_points(dev, flush),
              "batched": batched_point(dev, flush), "differentiable": differentiable_point(dev)}
     cpu = cpu_sample(budget_s=12.0) if world == 1 else None
     line = {
