@@ -552,6 +552,24 @@ def differentiable_point(dev, n_inst=DIFF_INSTANCES, gl_inst=4, single_sample=8,
     return out
 
 
+def max_over_ranks(values, dist, device):
+    """Element-wise maximum of per-rank timings (the slowest replica sets the
+    job's time); identity without a process group."""
+    import torch
+    if not dist:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
+def replica_throughput(world, steps, slowest_total_s):
+    """Whole-job solves/s of `world` independent replicas, each doing `steps`
+    solves, timed by the slowest replica (weak scaling: no collective on the
+    solve path)."""
+    return world * steps / slowest_total_s
+
+
 def run_gpu(args):
     import torch
     import reg_drot
@@ -601,11 +619,8 @@ def run_gpu(args):
     info = reg_drot.read_result(ws)
     step_s = [a.elapsed_time(b) / 1e3 for a, b in zip(starts, ends)]
     total = sum(step_s)
-    if dist:
-        t = torch.tensor([total, wall], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total, wall = float(t[0]), float(t[1])
-    value = world * args.steps / total
+    total, wall = max_over_ranks([total, wall], dist, dev)
+    value = replica_throughput(world, args.steps, total)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
