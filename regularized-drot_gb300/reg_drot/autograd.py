@@ -37,7 +37,7 @@ import torch
 from ._lib import DrotAdjointInstance, check, lib
 
 C_F32, C_BF16 = 0, 1
-CG_TOL = 1e-6
+CG_TOL = 1e-7
 CG_MAX_ITERS = 5000
 
 f32 = np.float32

@@ -8,9 +8,11 @@ differences (tests/test_adjoint_reference.py).  The GPU path: the CUDA solve
 duals) and drot_qr_adjoint_solve (masked Jacobi-PCG, one persistent launch).
 
 Loss: L = <C, X*> + w ||X*||_F^2.  Tolerances: the forward runs in FP32 to
-a marginal residual of 1e-7 and CG to 1e-6 relative residual, so gradients
-agree with the FP64 reference to about 1e-5 relative (Frobenius); the bar is
-2e-3 for dL/dC (and for the point-cloud chain rule), 5e-3 for dL/dp, dL/dq.
+a marginal residual of 1e-7 and CG to 1e-7 relative residual (at 1e-6 a
+weakly regularised case is off by 7e-4); measured
+dL/dC errors against the FP64 reference are 5e-6..6e-5 relative
+(Frobenius), and the bar is 1e-4 for dL/dC (and for the point-cloud chain
+rule and the batch-vs-single comparison), 5e-3 for dL/dp, dL/dq.
 The forward tolerance matters for dL/dp, dL/dq: at 1e-6 a weakly
 regularised case (200 x 150, r_weight 1e-3) leaves one support entry of 359
 undecided, which moves dL/dp by a few percent while dL/dC stays within
@@ -26,7 +28,7 @@ torch = pytest.importorskip("torch")
 from oracle import adjoint as A  # noqa: E402
 
 RHO = 2.0
-TOL_C = 2e-3
+TOL_C = 1e-4
 TOL_PQ = 5e-3
 EPS_FWD = 1e-7
 
@@ -168,7 +170,8 @@ def test_batch_gradients_match_single_instance(cuda, solver_lib):
         c1 = costs[k].clone().requires_grad_(True)
         x1 = quadratic_drot_fn(c1, ps[k].to(cuda), qs[k].to(cuda), RHO, rw, 200000, EPS_FWD)
         ((c1 * x1).sum() + w * (x1 * x1).sum()).backward()
-        assert _rel(leaves[k].grad.cpu().numpy(), c1.grad.cpu().numpy()) <= TOL_C
+        # two FP32 results, each within TOL_C of the FP64 reference
+        assert _rel(leaves[k].grad.cpu().numpy(), c1.grad.cpu().numpy()) <= 2 * TOL_C
         L, gc, *_ = A.loss_and_grads(costs[k].double().cpu().numpy(), ps[k].double().numpy(),
                                      qs[k].double().numpy(), RHO, rw, w)
         assert _rel(leaves[k].grad.cpu().numpy(), gc) <= TOL_C, k

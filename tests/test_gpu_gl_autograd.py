@@ -5,8 +5,9 @@ oracle's GL loop and to finite differences on the CPU) differentiated by
 torch autograd, for the same number of iterations the GPU solve ran.  The
 GPU backward recomputes each segment's states from checkpoints (segment
 lengths below force several segments, one of them partial) and applies
-drot_gl_adjoint_step once per iteration.  Tolerance 2e-3 relative
-(Frobenius): FP32 forward and FP32 adjoint recursion over the iterations.
+drot_gl_adjoint_step once per iteration.  Tolerance 1e-4 relative
+(Frobenius; measured 2e-7..7e-5): FP32 forward and FP32 adjoint recursion
+over the iterations.
 """
 import numpy as np
 import pytest
@@ -17,7 +18,7 @@ torch = pytest.importorskip("torch")
 
 from oracle import adjoint as A  # noqa: E402
 
-TOL = 2e-3
+TOL = 1e-4
 
 
 def _problem(nr, nc, seed):
