@@ -92,6 +92,12 @@ def _regdrot_gpu(mode, init, C, p, q, coef, groups=None, device=None, **kwargs):
     if np.shape(C) != (m, n) or len(p) != m or len(q) != n:
         raise ValueError("shapes of init, C, p, q do not match")
 
+    G = 0
+    barr = None
+    if mode == MODE_GL:  # validated before any device work
+        bounds = group_bounds_from_pairs(groups, m)
+        G = len(bounds) - 1
+        barr = (ctypes.c_int * (G + 1))(*bounds)
     dev = torch.device("cuda", torch.cuda.current_device()) if device is None else \
         torch.device(device)
     st0 = initial_state(init, p, q, init_strategy)
@@ -103,12 +109,6 @@ def _regdrot_gpu(mode, init, C, p, q, coef, groups=None, device=None, **kwargs):
          "a": torch.tensor(st0["a"], **f32), "b": torch.tensor(st0["b"], **f32),
          "phi1": torch.zeros(m, **f32), "phi2": torch.zeros(n, **f32),
          "alpha": torch.tensor(st0["alpha"], **f32)}
-    G = 0
-    barr = None
-    if mode == MODE_GL:
-        bounds = group_bounds_from_pairs(groups, m)
-        G = len(bounds) - 1
-        barr = (ctypes.c_int * (G + 1))(*bounds)
     with torch.cuda.device(dev):
         nbytes = int(lib().drot_np_workspace_bytes(mode, m, n, G, barr))
         if nbytes == 0:
