@@ -154,7 +154,8 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
       const int r = lo + (v % KVR) * SV + lane * VEC;
       if ((NCOL == 1 || jc < c1) && (FULL || r < hi)) {
         load_vec<VEC>(P.x + I.x_off + (long long)jc * I.ld + r, xv[v]);
-        if constexpr (EV && DIM == 0) load_c<VEC, CT>(cbase + I.c_off + (long long)jc * I.ld + r, cv[v]);
+        if constexpr (EV && DIM == 0)
+          load_c_raw<VEC, CT>(cbase + I.c_off + (long long)jc * I.ld + r, cv[v]);
         else {
 #pragma unroll
           for (int e = 0; e < VEC; ++e) cv[v][e] = 0.0f;
@@ -221,7 +222,7 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
 #pragma unroll
       for (int e = 0; e < VEC; ++e) {
         float tt = (xv[v][e] + f1a[e]) + f2[v / KVR];
-        if constexpr (EV) tt = fmaf(-s, cv[v][e], tt);
+        if constexpr (EV) tt = fmaf(-s, c_at<CT>(cv[v], e), tt);
         xv[v][e] = tt;
         const unsigned key = (unsigned)__float_as_int(tt) - 1u;
         tmin = min(tmin, valid(v, e) ? key : 0xffffffffu);
@@ -244,7 +245,7 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
           float y = SLOW ? a0 / kappa : div_rn_by_fma(a0, kappa, krcp);
           y = ok ? y : 0.0f;
           if constexpr (EV) {
-            const float c = ok ? cv[v][e] : 0.0f;  // the caller's padding may hold anything
+            const float c = ok ? c_at<CT>(cv[v], e) : 0.0f;  // the caller's padding may hold anything
             xv[v][e] = fmaf(-s, c, y);
             objp = fmaf(y, c, objp);
           } else {

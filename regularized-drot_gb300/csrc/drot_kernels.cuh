@@ -319,6 +319,35 @@ __device__ __forceinline__ void load_c(const CT* ptr, float (&v)[VEC]) {
   }
 }
 
+// C in the registers of the fused update: FP32 as loaded; BF16 kept as the
+// raw packed pairs (two bf16 per 32-bit word: half the registers of the
+// widened values, so the BF16 kernel fits the register budget without
+// spilling) and widened exactly where it is used (c_at).
+template <int VEC, typename CT>
+__device__ __forceinline__ void load_c_raw(const CT* ptr, float (&v)[VEC]) {
+  if constexpr (std::is_same<CT, float>::value) {
+    load_vec_nc<VEC>(ptr, v);
+  } else if constexpr (VEC == 4) {
+    const uint2 t = __ldg(reinterpret_cast<const uint2*>(ptr));
+    v[0] = __uint_as_float(t.x);
+    v[1] = __uint_as_float(t.y);
+    v[2] = 0.0f;
+    v[3] = 0.0f;
+  } else {
+    v[0] = __uint_as_float((unsigned)__ldg(reinterpret_cast<const unsigned short*>(ptr)));
+  }
+}
+
+template <typename CT, int VEC>
+__device__ __forceinline__ float c_at(const float (&v)[VEC], int e) {
+  if constexpr (std::is_same<CT, float>::value) {
+    return v[e];
+  } else {
+    const unsigned w = __float_as_uint(v[e >> 1]);
+    return __uint_as_float((e & 1) ? (w & 0xffff0000u) : (w << 16));
+  }
+}
+
 template <int VEC>
 __device__ __forceinline__ void store_vec(float* ptr, const float (&v)[VEC]) {
   if constexpr (VEC == 4) {
@@ -587,7 +616,7 @@ drot_solve_kernel(const SolveParams P) {
         for (int v = 0; v < KV; ++v) {
           if (FULL || vanyf(v)) {
             load_vec<VEC>(xcol + row0f(v), xv[v]);
-            if constexpr (WITH_C) load_c<VEC, CT>(ccol + row0f(v), cv[v]);
+            if constexpr (WITH_C) load_c_raw<VEC, CT>(ccol + row0f(v), cv[v]);
             else {
 #pragma unroll
               for (int e = 0; e < VEC; ++e) cv[v][e] = 0.0f;
@@ -665,7 +694,7 @@ drot_solve_kernel(const SolveParams P) {
 #pragma unroll
             for (int e = 0; e < VEC; ++e) {
               float t = (xv[v][e] + f1[v][e]) + f2;
-              if constexpr (EV) t = fmaf(-s, cv[v][e], t);
+              if constexpr (EV) t = fmaf(-s, c_at<CT>(cv[v], e), t);
               xv[v][e] = t;
               tmin = min(tmin, (unsigned)__float_as_int(t) - 1u);
             }
@@ -680,8 +709,9 @@ drot_solve_kernel(const SolveParams P) {
                 float y = SLOW ? a / kappa : div_rn_by_fma(a, kappa, kappa_rcp);
                 if constexpr (!FULL) y = einf(v, e) ? y : 0.0f;
                 if constexpr (EV) {
-                  xv[v][e] = fmaf(-s, cv[v][e], y);
-                  objp = fmaf(y, cv[v][e], objp);
+                  const float c = c_at<CT>(cv[v], e);
+                  xv[v][e] = fmaf(-s, c, y);
+                  objp = fmaf(y, c, objp);
                 } else {
                   xv[v][e] = y;
                 }
@@ -697,7 +727,7 @@ drot_solve_kernel(const SolveParams P) {
           for (int v = 0; v < KV; ++v)
 #pragma unroll
             for (int e = 0; e < VEC; ++e) {
-              const float t = fmaf(-s, cv[v][e], (xv[v][e] + f1[v][e]) + f2);
+              const float t = fmaf(-s, c_at<CT>(cv[v], e), (xv[v][e] + f1[v][e]) + f2);
               float y = fmaxf(t, 0.0f);
               if constexpr (!FULL) y = einf(v, e) ? y : 0.0f;
               xv[v][e] = y;
@@ -721,7 +751,7 @@ drot_solve_kernel(const SolveParams P) {
               xv[v][e] = y;
               acc[v][e] += y;
               colp += y;
-              objp = fmaf(y, cv[v][e], objp);
+              objp = fmaf(y, c_at<CT>(cv[v], e), objp);
             }
         }
 
