@@ -171,44 +171,47 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
     if constexpr (EV && DIM > 0) {
       // C of the step's 4 columns x the lane's 4 rows from the points: the
       // band's x (k-major in shared memory) against y_j (broadcast loads),
-      // k ascending; cv = cscale * max(|x|^2 + |y|^2 - 2 <x, y>, 0).
-      float dot[4][VEC], yn[4];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        const int jc = min(j0 + v, c1 - 1);
-        yn[v] = __ldg(P.ynorm + I.col_off + jc);
-#pragma unroll
-        for (int e = 0; e < VEC; ++e) dot[v][e] = 0.0f;
-      }
-#pragma unroll
-      for (int k0 = 0; k0 < DIM; k0 += 4) {
-        float4 yk[4];
-#pragma unroll
-        for (int v = 0; v < 4; ++v) {
-          const int jc = min(j0 + v, c1 - 1);
-          yk[v] = __ldg(reinterpret_cast<const float4*>(P.ypts + (long long)(I.col_off + jc) * DIM + k0));
-        }
-#pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          const float4 xk = *reinterpret_cast<const float4*>(xs + (k0 + kk) * SV + lane * VEC);
-          const float xa[VEC] = {xk.x, xk.y, xk.z, xk.w};
-#pragma unroll
-          for (int v = 0; v < 4; ++v) {
-            const float yv = kk == 0 ? yk[v].x : (kk == 1 ? yk[v].y : (kk == 2 ? yk[v].z : yk[v].w));
-#pragma unroll
-            for (int e = 0; e < VEC; ++e) dot[v][e] = fmaf(xa[e], yv, dot[v][e]);
-          }
-        }
-      }
+      // k ascending; cv = cscale * max(|x|^2 + |y|^2 - 2 <x, y>, 0).  Two
+      // columns at a time keeps the accumulators and y in registers without
+      // spilling.
       const float4 xn4 = *reinterpret_cast<const float4*>(xns + lane * VEC);
       const float xna[VEC] = {xn4.x, xn4.y, xn4.z, xn4.w};
 #pragma unroll
-      for (int v = 0; v < 4; ++v)
+      for (int v0 = 0; v0 < 4; v0 += 2) {
+        float dot[2][VEC];
 #pragma unroll
-        for (int e = 0; e < VEC; ++e)
-          cv[v][e] = P.cscale * fmaxf(fmaf(-2.0f, dot[v][e], xna[e] + yn[v]), 0.0f);
+        for (int v = 0; v < 2; ++v)
+#pragma unroll
+          for (int e = 0; e < VEC; ++e) dot[v][e] = 0.0f;
+#pragma unroll
+        for (int k0 = 0; k0 < DIM; k0 += 4) {
+          float4 yk[2];
+#pragma unroll
+          for (int v = 0; v < 2; ++v) {
+            const int jc = min(j0 + v0 + v, c1 - 1);
+            yk[v] = __ldg(reinterpret_cast<const float4*>(P.ypts + (long long)(I.col_off + jc) * DIM + k0));
+          }
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk) {
+            const float4 xk = *reinterpret_cast<const float4*>(xs + (k0 + kk) * SV + lane * VEC);
+            const float xa[VEC] = {xk.x, xk.y, xk.z, xk.w};
+#pragma unroll
+            for (int v = 0; v < 2; ++v) {
+              const float yv = kk == 0 ? yk[v].x : (kk == 1 ? yk[v].y : (kk == 2 ? yk[v].z : yk[v].w));
+#pragma unroll
+              for (int e = 0; e < VEC; ++e) dot[v][e] = fmaf(xa[e], yv, dot[v][e]);
+            }
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+          const float yn = __ldg(P.ynorm + I.col_off + min(j0 + v0 + v, c1 - 1));
+#pragma unroll
+          for (int e = 0; e < VEC; ++e)
+            cv[v0 + v][e] = P.cscale * fmaxf(fmaf(-2.0f, dot[v][e], xna[e] + yn), 0.0f);
+        }
+      }
     }
-
     auto valid = [&](int v, int e) -> bool {
       if constexpr (FULL && NCOL == 1) return true;
       const bool colok = (NCOL == 1) || (j0 + v / KVR < c1);
