@@ -204,12 +204,24 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
       hmax = std::max(hmax, pl.bounds[g + 1] - base);
     }
     hmax = std::max(hmax, 1);
+    // Vectors per lane: the smallest that covers a group in one warp, up to
+    // a cap (DROT_GL_KV, 1/2/4/8, default 8); taller groups use teams of
+    // warps.
+    int kvcap = 8;
+    if (const char* e = getenv("DROT_GL_KV")) {
+      const int k = atoi(e);
+      if (k == 1 || k == 2 || k == 4 || k == 8) kvcap = k;
+    }
     pl.kv = 0;
     for (int kv : {1, 2, 4, 8})
-      if (SV * kv >= hmax) { pl.kv = kv; break; }
+      if (kv <= kvcap && SV * kv >= hmax) { pl.kv = kv; break; }
     if (pl.kv == 0) {
-      pl.kv = 8;
-      pl.wt = (hmax + 8 * SV - 1) / (8 * SV);
+      // Groups taller than one warp covers: teams of 4-vector warps (the
+      // 8-vector kernel spills at the register cap; measured at 3000^2 with
+      // two 1500-row groups: 26.7 us per iteration against 31.8).
+      if (!getenv("DROT_GL_KV")) kvcap = std::min(kvcap, 4);
+      pl.kv = kvcap;
+      pl.wt = (hmax + kvcap * SV - 1) / (kvcap * SV);
       if (pl.wt > 16) return DROT_ERR_UNSUPPORTED;
     } else {
       pl.wt = 1;
@@ -329,7 +341,7 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
 struct PlanKey {
   int dev, mode, nr, nc, G, vec, tma, warps, ctas, ctype;
   std::vector<int> ubounds;  // caller's GL group boundaries (empty: the reference's)
-  int qr_kv;                 // DROT_QR_KV knob
+  int qr_kv;                 // DROT_QR_KV and DROT_GL_KV knobs
   bool operator==(const PlanKey& o) const {
     return dev == o.dev && mode == o.mode && nr == o.nr && nc == o.nc && G == o.G &&
            vec == o.vec && tma == o.tma && warps == o.warps && ctas == o.ctas &&
@@ -347,7 +359,8 @@ static int make_plan(int mode, int nr, int nc, int G, int vec, bool tma, Plan& p
   PlanKey key = {dev, mode, nr, nc, mode == MODE_GL ? G : 0, vec, tma ? 1 : 0,
                  tma ? tma_warps() : reg_warps(),
                  tma && getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1, ctype, {},
-                 getenv("DROT_QR_KV") ? atoi(getenv("DROT_QR_KV")) : 0};
+                 (getenv("DROT_QR_KV") ? atoi(getenv("DROT_QR_KV")) : 0) +
+                     16 * (getenv("DROT_GL_KV") ? atoi(getenv("DROT_GL_KV")) : 0)};
   if (mode == MODE_GL && ubounds) key.ubounds.assign(ubounds, ubounds + G + 1);
   {
     std::lock_guard<std::mutex> lk(g_plan_mu);
