@@ -99,12 +99,13 @@ __global__ void outer_kernel(float* __restrict__ x, const float* __restrict__ p,
 static const size_t kAlign = 256;
 static inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
 
+
 // Scratch layout (offsets from the workspace base):
 //   [0, 256)     DeviceStats
 //   [256, 512)   barrier counter + abort flag
 //   rowpart      P * nr floats
 //   colpart      nsb * nc floats
-//   cta_sum/obj/res  grid doubles each
+//   cta_sum/obj/res  grid float pairs (8 bytes) each
 struct Plan {
   int mode = 0, vec = 4, kv = 4, wt = 1, threads = 256, nbands = 1, P = 1, grid = 1, nsb = 1;
   int band_h = 0, ns = 1, p2_smem = 0, p2_cap_r = 0, p2_cap_c = 0, ctype = DROT_C_F32;
@@ -327,11 +328,11 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
   pl.off_colpart = off;
   off = align_up(off + sizeof(float) * (size_t)pl.nsb * nc);
   pl.off_sum = off;
-  off = align_up(off + sizeof(double) * pl.grid);
+  off = align_up(off + sizeof(float2) * pl.grid);
   pl.off_obj = off;
-  off = align_up(off + sizeof(double) * pl.grid);
+  off = align_up(off + sizeof(float2) * pl.grid);
   pl.off_res = off;
-  off = align_up(off + sizeof(double) * pl.grid);
+  off = align_up(off + sizeof(float2) * pl.grid);
   pl.total = off;
   return DROT_OK;
 }
@@ -488,6 +489,7 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
   prm.max_iters = A.max_iters;
   prm.stop_every = A.stop_every;
   prm.stop_le = A.stop_le;
+  prm.res2_stop = res2_threshold(A.eps, A.mode == MODE_QR && !A.stop_le);
   prm.nbands = pl.nbands; prm.P = pl.P; prm.Wt = pl.wt; prm.nsb = pl.nsb;
   prm.band_h = pl.band_h;
   prm.ns = pl.ns;
@@ -497,9 +499,9 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
   for (size_t k = 0; k < pl.bounds.size(); ++k) prm.gbounds[k] = pl.bounds[k];
   prm.rowpart = (float*)(ws + pl.off_rowpart);
   prm.colpart = (float*)(ws + pl.off_colpart);
-  prm.cta_sum = (double*)(ws + pl.off_sum);
-  prm.cta_obj = (double*)(ws + pl.off_obj);
-  prm.cta_res = (double*)(ws + pl.off_res);
+  prm.cta_sum = (float2*)(ws + pl.off_sum);
+  prm.cta_obj = (float2*)(ws + pl.off_obj);
+  prm.cta_res = (float2*)(ws + pl.off_res);
   prm.bar = (unsigned int*)(ws + pl.off_ctrl);
   prm.abort_flag = (int*)(ws + pl.off_ctrl + 64);
   prm.stats = (DeviceStats*)(ws + pl.off_stats);

@@ -46,6 +46,7 @@ struct BatchInst {
   float s, kappa, kappa_rcp, eps, nc_rcp, nr_rcp;
   float w_phi1, w_phi2, w_a, w_b, w_alpha;  // warm-start constants
   int pad;
+  double res2_stop;  // converged when the squared residual is below this (res2_threshold)
 };
 
 struct BatchTile {
@@ -59,7 +60,7 @@ struct BatchItem {
 
 struct BatchStat {
   int n_iter, iters_run, converged, objective_valid;
-  double objective, residual;
+  double objective, residual;  // residual: squared on the device, rooted by the host
 };
 
 struct BatchParams {
@@ -75,9 +76,10 @@ struct BatchParams {
   int fine_threshold;  // fine list once fewer active coarse tiles remain
   float *a, *b, *phi1, *phi2;  // packed state
   float* alpha;                // [2][n_inst], by iteration parity
-  double *res_slot, *obj_slot; // per item: squared residual; per instance: objective
+  float2* res_slot;            // per item: squared residual (float pair)
+  double* obj_slot;            // per instance: objective
   float *rowpart, *colpart;
-  double *tile_sum, *tile_obj;
+  float2 *tile_sum, *tile_obj; // per tile: mass and objective (float pairs)
   int* conv;
   BatchStat* stats;
   // On-the-fly cost (point-cloud launches): C_ij = cscale * max(|x_i|^2 +
@@ -357,10 +359,10 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
   const int W = blockDim.x >> 5;
   float* red = reinterpret_cast<float*>(smem_raw);  // [W][S]
   float* f1s = red + (size_t)W * S;                 // [S]
-  double* dscr = reinterpret_cast<double*>(f1s + S);  // [W + 1]
-  double* oscr = dscr + W + 1;                        // [W]
+  fpair* dscr = reinterpret_cast<fpair*>(f1s + S);  // [W + 1]
+  fpair* oscr = dscr + W + 1;                       // [W]
   // Point launches: the band's x, k-major [DIM][128], and their norms [128].
-  // float4 reads: 16-byte aligned (the FP64 scratch above ends on an 8-byte
+  // float4 reads: 16-byte aligned (the pair scratch above ends on an 8-byte
   // boundary).
   float* xs = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(oscr + W) + 15) &
                                        ~static_cast<uintptr_t>(15));
@@ -442,9 +444,9 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
         else if (T.kvr == 2) run(K2(), std::false_type());
         else run(K4(), std::false_type());
       }
-      // Tile partials: rows (fixed warp order), mass and objective (FP64).
-      const double wsum = warp_sum_d((double)ms_hi + (double)ms_lo);
-      const double wobj = even ? warp_sum_d((double)ob_hi + (double)ob_lo) : 0.0;
+      // Tile partials: rows (fixed warp order), mass and objective (float pairs).
+      const fpair wsum = warp_sum_fp(fpair{ms_hi, ms_lo});
+      const fpair wobj = even ? warp_sum_fp(fpair{ob_hi, ob_lo}) : fp_make(0.0f);
 #pragma unroll
       for (int v = 0; v < 4; ++v)
         if (v < T.kvr)
@@ -464,13 +466,13 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
         }
       }
       if (warp == 0) {
-        double a1 = lane < W ? dscr[lane] : 0.0;
-        double a2 = lane < W ? oscr[lane] : 0.0;
-        a1 = warp_sum_d(a1);
-        a2 = warp_sum_d(a2);
+        fpair a1 = lane < W ? dscr[lane] : fp_make(0.0f);
+        fpair a2 = lane < W ? oscr[lane] : fp_make(0.0f);
+        a1 = warp_sum_fp(a1);
+        if (even) a2 = warp_sum_fp(a2);
         if (lane == 0) {
-          P.tile_sum[t] = a1;
-          if (even) P.tile_obj[t] = a2;
+          P.tile_sum[t] = make_float2(a1.hi, a1.lo);
+          if (even) P.tile_obj[t] = make_float2(a2.hi, a2.lo);
         }
       }
     }
@@ -495,28 +497,32 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       const int t0 = fine ? I.tile0f : I.tile0;
       const int ntl = fine ? I.ntilesf : I.ntiles;
       const int nchunks = fine ? I.Pf : I.P;
-      double sg = 0.0, og = 0.0;
+      fpair sg = fp_make(0.0f), og = fp_make(0.0f);
       for (int i = threadIdx.x; i < ntl; i += blockDim.x) {
-        sg += __ldcg(P.tile_sum + t0 + i);
-        if (even && first) og += __ldcg(P.tile_obj + t0 + i);
+        const float2 u = __ldcg(P.tile_sum + t0 + i);
+        sg = fp_add(sg, fpair{u.x, u.y});
+        if (even && first) {
+          const float2 o = __ldcg(P.tile_obj + t0 + i);
+          og = fp_add(og, fpair{o.x, o.y});
+        }
       }
-      sg = block_sum_d(sg, dscr);
-      if (even && first) og = block_sum_d(og, dscr);
-      const float sigma = (float)sg;
+      sg = block_sum_fp(sg, dscr);
+      if (even && first) og = block_sum_fp(og, dscr);
+      const float sigma = sg.hi + sg.lo;  // the float total mass
       const float alpha = __ldcg(P.alpha + (size_t)(it & 1) * P.n_inst + k);
       const float gamma =
           (float)((2.0 * ((double)sigma - 1.0) - (double)alpha) / (double)(I.nr + I.nc));
       if (first && threadIdx.x == 0)
         P.alpha[(size_t)((it + 1) & 1) * P.n_inst + k] =
             (float)(((double)alpha + 1.0) - (double)sigma);
-      double res = 0.0;
+      fpair res = fp_make(0.0f);
       const float ncf = (float)I.nc, nrf = (float)I.nr;
       reduce_lines(P.rowpart + I.rp_off, I.nr, Q.l0, min(Q.l1, I.nr), nchunks, [&](int i, float r) {
         const float rs = r - __ldg(P.p + I.p_off + i);
         const float ab = P.a[I.row_off + i] - rs;
         P.phi1[I.row_off + i] = div_rn_by((ab - rs) + gamma, ncf, I.nc_rcp);
         P.a[I.row_off + i] = ab;
-        res = fma((double)rs, (double)rs, res);
+        res = fp_add(res, fp_sqr(rs));
       });
       reduce_lines(P.colpart + I.cp_off, I.nc, max(Q.l0 - I.nr, 0), Q.l1 - I.nr, I.nbands,
                    [&](int j, float cs_) {
@@ -524,12 +530,12 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
         const float ab = P.b[I.col_off + j] - cs;
         P.phi2[I.col_off + j] = div_rn_by((ab - cs) + gamma, nrf, I.nr_rcp);
         P.b[I.col_off + j] = ab;
-        res = fma((double)cs, (double)cs, res);
+        res = fp_add(res, fp_sqr(cs));
       });
-      res = block_sum_d(res, dscr);
+      res = block_sum_fp(res, dscr);
       if (threadIdx.x == 0) {
-        P.res_slot[qi] = res;
-        if (even && first) P.obj_slot[k] = og;
+        P.res_slot[qi] = make_float2(res.hi, res.lo);
+        if (even && first) P.obj_slot[k] = fp_value(og);
       }
       __syncthreads();
     }
@@ -548,13 +554,16 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
           const int k = P.items[qi].inst;
           const BatchInst& I = P.inst[k];
           if (qi != I.item0 || __ldcg(P.conv + k)) continue;
-          double r2 = 0.0;
-          for (int t = 0; t < I.nitems; ++t) r2 += __ldcg(P.res_slot + I.item0 + t);
+          fpair r2 = fp_make(0.0f);
+          for (int t = 0; t < I.nitems; ++t) {
+            const float2 u = __ldcg(P.res_slot + I.item0 + t);
+            r2 = fp_add(r2, fpair{u.x, u.y});
+          }
           BatchStat st = P.stats[k];
           st.objective = __ldcg(P.obj_slot + k);
           st.objective_valid = 1;
-          st.residual = sqrt(r2);
-          if (st.residual < (double)I.eps) {
+          st.residual = fp_value(r2);
+          if (st.residual < I.res2_stop) {
             // Converged at iteration it: the instance keeps its folded X
             // until the unfold pass at the end of the launch.
             st.converged = 1;
@@ -695,7 +704,7 @@ static void add_tiles(std::vector<BatchTile>& tiles, int k, const BatchInst& I, 
 // Dynamic shared memory: row reduction [warps][512], phi1 stage [512], FP64
 // scratch, and for point launches the band's x (k-major) and norms.
 static size_t batch_smem(int warps, int dim) {
-  return sizeof(float) * ((size_t)warps * kBatchS + kBatchS) + sizeof(double) * (2 * warps + 1) +
+  return sizeof(float) * ((size_t)warps * kBatchS + kBatchS) + sizeof(fpair) * (2 * warps + 1) +
          16 /* alignment of the point stage */ + sizeof(float) * ((size_t)dim * 128 + 128);
 }
 
@@ -778,6 +787,7 @@ int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int c
     I.kappa = 1.0f + t;
     I.kappa_rcp = (float)(1.0 / (double)I.kappa);
     I.eps = d.eps;
+    I.res2_stop = res2_threshold(d.eps, true);
     I.nc_rcp = (float)(1.0 / (double)(float)d.n_cols);
     I.nr_rcp = (float)(1.0 / (double)(float)d.n_rows);
     const float n = (float)d.n_rows, m = (float)d.n_cols;
@@ -844,9 +854,9 @@ int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int c
   P.off_alpha = off; off = al(off + sizeof(float) * 2 * n_inst);
   P.off_rp = off;    off = al(off + sizeof(float) * rp);
   P.off_cp = off;    off = al(off + sizeof(float) * cpp);
-  P.off_tsum = off;  off = al(off + sizeof(double) * P.tiles.size());
-  P.off_tobj = off;  off = al(off + sizeof(double) * P.tiles.size());
-  P.off_res = off;   off = al(off + sizeof(double) * P.items.size());
+  P.off_tsum = off;  off = al(off + sizeof(float2) * P.tiles.size());
+  P.off_tobj = off;  off = al(off + sizeof(float2) * P.tiles.size());
+  P.off_res = off;   off = al(off + sizeof(float2) * P.items.size());
   P.off_obj = off;   off = al(off + sizeof(double) * n_inst);
   P.off_conv = off;  off = al(off + sizeof(int) * n_inst);
   P.off_stats = off; off = al(off + sizeof(BatchStat) * n_inst);
@@ -901,7 +911,7 @@ static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, 
   B.fine_threshold = P.grid / fine_divisor();
   B.items = (const BatchItem*)(ws + P.off_items);
   B.n_items = (int)P.items.size();
-  B.res_slot = (double*)(ws + P.off_res);
+  B.res_slot = (float2*)(ws + P.off_res);
   B.obj_slot = (double*)(ws + P.off_obj);
   B.max_iters = max_iters;
   B.a = (float*)(ws + P.off_a);
@@ -911,8 +921,8 @@ static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, 
   B.alpha = (float*)(ws + P.off_alpha);
   B.rowpart = (float*)(ws + P.off_rp);
   B.colpart = (float*)(ws + P.off_cp);
-  B.tile_sum = (double*)(ws + P.off_tsum);
-  B.tile_obj = (double*)(ws + P.off_tobj);
+  B.tile_sum = (float2*)(ws + P.off_tsum);
+  B.tile_obj = (float2*)(ws + P.off_tobj);
   B.conv = (int*)(ws + P.off_conv);
   B.stats = (BatchStat*)(ws + P.off_stats);
   B.counters = (unsigned*)(ws + P.off_ctrl);
@@ -1019,7 +1029,7 @@ int drot_batch_results(drot_batch_plan plan, const void* workspace, drot_batch_r
     out[k].converged = st[k].converged;
     out[k].objective_valid = st[k].objective_valid;
     out[k].objective = st[k].objective;
-    out[k].residual = st[k].residual;
+    out[k].residual = st[k].residual >= 0.0 ? sqrt(st[k].residual) : st[k].residual;
   }
   return abort_flag ? DROT_ERR_BARRIER_TIMEOUT : DROT_OK;
 }

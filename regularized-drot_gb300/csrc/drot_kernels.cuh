@@ -23,14 +23,14 @@
 // Per iteration (all on device, no host round trip):
 //   phase 1  fused X-update over the CTA's tile: prox (QR divisor or GL group
 //            shrink), store, per-lane row partials, per-warp column partials,
-//            per-CTA FP64 mass and objective partials;
+//            per-CTA mass and objective partials (float pairs);
 //   barrier A
 //   phase 2  CTA b reduces rows [b*nr/G, (b+1)*nr/G) and the same share of
 //            columns: marginal residuals, duals a/b, phi1/phi2 (the
-//            reference's update_aux, kernel_qr.hpp:405-467), and an FP64
-//            residual partial;
+//            reference's update_aux, kernel_qr.hpp:405-467), and a
+//            float-pair partial of the squared residual;
 //   barrier B
-//   stop test on the FP64 residual (QR: even iterations only, "< eps";
+//   stop test on the squared residual (QR: even iterations only, "< eps";
 //            GL: every iteration, "<= eps"), identical in every CTA.
 //
 // Every wait is bounded by wall time (globaltimer): a grid barrier or an
@@ -89,6 +89,9 @@ struct SolveParams {
   float nr_rcp;        // RN(1 / float(nr))
   float lambda;        // GL threshold
   float eps;           // absolute residual tolerance
+  double res2_stop;    // stop when the squared residual (FP64) is below this:
+                       // the exact image of the "< eps" / "<= eps" test on
+                       // its square root (set by the host)
   double norm_eps;     // GL: constant added to the group norm (1e-9)
   int max_iters;
   int stop_every;      // QR: test every iteration (numpy-API loop), not only even ones
@@ -104,15 +107,16 @@ struct SolveParams {
   int p2_cap_c;
   float* rowpart;      // [P][nr]
   float* colpart;      // [nsb][nc]
-  double* cta_sum;     // [grid]
-  double* cta_obj;     // [grid]
-  double* cta_res;     // [grid]
+  float2* cta_sum;     // [grid] float pairs (hi, lo)
+  float2* cta_obj;     // [grid]
+  float2* cta_res;     // [grid]
   unsigned int* bar;   // barrier arrival counter (zeroed before launch)
   int* abort_flag;     // zeroed before launch
   DeviceStats* stats;
   long long timeout_ns;
   int gbounds[kMaxGroups + 1];  // GL: group row boundaries
 };
+
 
 // ---------------------------------------------------------------------------
 // device helpers
@@ -152,6 +156,40 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
+// Warp sum of float pairs (fixed butterfly order; lane 0's result is the
+// one used, so runs are bitwise repeatable).
+__device__ __forceinline__ fpair warp_sum_fp(fpair v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const fpair u{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+    v = fp_add(v, u);
+  }
+  return v;
+}
+
+// Sum of the float pairs v[0..n) over one warp: 16 strided loads per lane in
+// flight at once (grids up to 512 CTAs take one round trip), a fixed add
+// tree, then the shuffle tree.
+__device__ __forceinline__ fpair warp_sum_strided_fp(const float2* v, int n, int lane) {
+  fpair a[16];
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    const int i = lane + 32 * u;
+    const float2 t = i < n ? __ldcg(v + i) : make_float2(0.0f, 0.0f);
+    a[u] = fpair{t.x, t.y};
+  }
+#pragma unroll
+  for (int w = 8; w > 0; w >>= 1)
+#pragma unroll
+    for (int u = 0; u < w; ++u) a[u] = fp_add(a[u], a[u + w]);
+  fpair t = a[0];
+  for (int i = lane + 512; i < n; i += 32) {
+    const float2 x = __ldcg(v + i);
+    t = fp_add(t, fpair{x.x, x.y});
+  }
+  return warp_sum_fp(t);
+}
+
 // Deterministic block-wide FP64 sum; every thread receives the result.
 // `scratch` holds blockDim/32 + 1 doubles.  FP64 runs on a narrow pipe here,
 // so only warp 0 combines the per-warp sums.
@@ -164,6 +202,23 @@ __device__ __forceinline__ double block_sum_d(double v, double* scratch) {
   if (w == 0) {
     double t = lane < nw ? scratch[lane] : 0.0;
     t = warp_sum_d(t);
+    if (lane == 0) scratch[nw] = t;
+  }
+  __syncthreads();
+  return scratch[nw];
+}
+
+// Deterministic block-wide sum of float pairs; every thread receives the
+// result.  `scratch` holds blockDim/32 + 1 pairs.
+__device__ __forceinline__ fpair block_sum_fp(fpair v, fpair* scratch) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  v = warp_sum_fp(v);
+  __syncthreads();
+  if (lane == 0) scratch[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    fpair t = lane < nw ? scratch[lane] : fp_make(0.0f);
+    t = warp_sum_fp(t);
     if (lane == 0) scratch[nw] = t;
   }
   __syncthreads();
@@ -407,8 +462,8 @@ __device__ __forceinline__ void reduce_partials(int r0, int r1, int k0, int k1,
 //   f1s     Wt * S floats (phi1 of the band rows)
 //   st2     3 * (cap_r + cap_c) floats when the phase-2 state is in shared
 //           memory (p, a, staged phi1 of the CTA's rows; q, b, phi2 of its columns)
-//   dscr    W + 1 doubles
-//   nslot   2 * W doubles (per-warp objective sums; GL team norms)
+//   dscr    W + 1 float pairs (per-warp mass / residual sums)
+//   nslot   2 * W float pairs (per-warp objective sums; GL team norms)
 //   mbar    W * ns uint64 (TMA only)
 __host__ __device__ constexpr size_t solve_smem_bytes(int warps, int wt, int S, int ns, bool tma,
                                                       int p2_floats = 0) {
@@ -444,10 +499,11 @@ drot_solve_kernel(const SolveParams P) {
   float* s_q = s_t1 + capr;
   float* s_b = s_q + capc;
   float* s_t2 = s_b + capc;
-  double* dscr = reinterpret_cast<double*>(s_t2 + capc);
-  double* nslot = dscr + W + 1;
+  fpair* dscr = reinterpret_cast<fpair*>(s_t2 + capc);
+  fpair* nslot = dscr + W + 1;
   uint64_t* mbar = reinterpret_cast<uint64_t*>(nslot + 2 * W);
   __shared__ int s_flag;
+  __shared__ int s_stop;
   __shared__ float s_misc_f[2];
   __shared__ double s_misc_d[2];
 
@@ -549,17 +605,17 @@ drot_solve_kernel(const SolveParams P) {
   // the registers of every thread).
   const bool timer = blockIdx.x == 0;
   __shared__ unsigned long long s_tp;
-  __shared__ double s_tacc[4];
+  __shared__ unsigned long long s_tacc[4];
   if (threadIdx.x == 0) {
     s_tp = 0;
-    for (int q = 0; q < 4; ++q) s_tacc[q] = 0.0;
+    for (int q = 0; q < 4; ++q) s_tacc[q] = 0ull;
   }
   auto stamp = [&](int k2) {  // CTA 0 only (block-uniform)
     if (timer) {
       __syncthreads();
       if (threadIdx.x == 0) {
         const unsigned long long now = globaltimer_ns();
-        if (k2 > 0) s_tacc[k2 - 1] += (double)(now - s_tp);
+        if (k2 > 0) s_tacc[k2 - 1] += now - s_tp;
         s_tp = now;
       }
     }
@@ -829,9 +885,9 @@ drot_solve_kernel(const SolveParams P) {
     if (wfail && lane == 0) atomicExch(P.abort_flag, 1);
 
     // CTA reduction of the row partials (fixed order over teams) and of the
-    // mass / objective (FP64 across lanes and warps).
-    const double wsum = warp_sum_d((double)ms_hi + (double)ms_lo);
-    const double wobj = with_c ? warp_sum_d((double)ob_hi + (double)ob_lo) : 0.0;
+    // mass / objective (float pairs across lanes and warps).
+    const fpair wsum = warp_sum_fp(fpair{ms_hi, ms_lo});
+    const fpair wobj = with_c ? warp_sum_fp(fpair{ob_hi, ob_lo}) : fp_make(0.0f);
     __syncthreads();
 #pragma unroll
     for (int v = 0; v < KV; ++v)
@@ -856,13 +912,13 @@ drot_solve_kernel(const SolveParams P) {
       }
     }
     if (warp == 0) {
-      double t = lane < W ? dscr[lane] : 0.0;
-      double o = lane < W ? nslot[lane] : 0.0;
-      t = warp_sum_d(t);
-      if (with_c) o = warp_sum_d(o);
+      fpair t = lane < W ? dscr[lane] : fp_make(0.0f);
+      fpair o = lane < W ? nslot[lane] : fp_make(0.0f);
+      t = warp_sum_fp(t);
+      if (with_c) o = warp_sum_fp(o);
       if (lane == 0) {
-        P.cta_sum[blockIdx.x] = t;
-        if (with_c) P.cta_obj[blockIdx.x] = o;
+        P.cta_sum[blockIdx.x] = make_float2(t.hi, t.lo);
+        if (with_c) P.cta_obj[blockIdx.x] = make_float2(o.hi, o.lo);
       }
     }
 
@@ -879,16 +935,18 @@ drot_solve_kernel(const SolveParams P) {
     // (c) one block sync, then phi = (staged + gamma) / n_cols (or n_rows).
     const bool check = (MODE == MODE_GL) || even || P.stop_every;
     if (warp == 0) {
-      const double t = warp_sum_strided(P.cta_sum, G, lane);
+      const fpair ts = warp_sum_strided_fp(P.cta_sum, G, lane);
       if (lane == 0) {
-        const float sigma = (float)t;
+        // The float total mass: RN(hi + lo) of the normalised pair.
+        const float sigma = ts.hi + ts.lo;
+        const double t = fp_value(ts);
         s_misc_f[0] = (float)((2.0 * ((double)sigma - 1.0) - (double)alpha) /
                               (double)(P.nr + P.nc));
         alpha = (float)(((double)alpha + 1.0) - (double)sigma);
         s_misc_d[0] = t;
       }
     }
-    double res = 0.0;
+    fpair res = fp_make(0.0f);
     const bool sm2 = P.p2_smem != 0;
     reduce_partials(
         r_lo, r_hi, k_lo, k_hi, P.rowpart, P.colpart, P.nr, P.nc, P.P, P.nsb,
@@ -903,7 +961,7 @@ drot_solve_kernel(const SolveParams P) {
             P.a[i] = ab;
             P.phi1[i] = ab - rs;
           }
-          res = fma((double)rs, (double)rs, res);
+          res = fp_add(res, fp_sqr(rs));
         },
         [&](int j, float t) {
           const int lj = j - k_lo;
@@ -916,10 +974,10 @@ drot_solve_kernel(const SolveParams P) {
             P.b[j] = ab;
             P.phi2[j] = ab - cs;
           }
-          res = fma((double)cs, (double)cs, res);
+          res = fp_add(res, fp_sqr(cs));
         });
     if (check) {
-      res = warp_sum_d(res);
+      res = warp_sum_fp(res);
       if (lane == 0) dscr[warp] = res;
     }
     __syncthreads();
@@ -935,9 +993,9 @@ drot_solve_kernel(const SolveParams P) {
       }
     }
     if (check && warp == 0) {
-      double t = lane < W ? dscr[lane] : 0.0;
-      t = warp_sum_d(t);
-      if (lane == 0) P.cta_res[blockIdx.x] = t;
+      fpair t = lane < W ? dscr[lane] : fp_make(0.0f);
+      t = warp_sum_fp(t);
+      if (lane == 0) P.cta_res[blockIdx.x] = make_float2(t.hi, t.lo);
     }
     last_sigma = s_misc_d[0];
     if (with_c) obj_valid = 1;
@@ -946,15 +1004,19 @@ drot_solve_kernel(const SolveParams P) {
     if (!grid_barrier(P, epoch, &s_flag)) { aborted = true; break; }
 
     if (check) {
+      // One thread turns the squared residual into the decision; the square
+      // root is taken once, after the loop.
       if (warp == 0) {
-        const double t = warp_sum_strided(P.cta_res, G, lane);
-        if (lane == 0) s_misc_d[1] = t;
+        const fpair t = warp_sum_strided_fp(P.cta_res, G, lane);
+        if (lane == 0) {
+          const double r2 = fp_value(t);
+          s_misc_d[1] = r2;
+          s_stop = r2 < P.res2_stop ? 1 : 0;
+        }
       }
       __syncthreads();
-      last_res = sqrt(s_misc_d[1]);
-      const bool stop = (MODE == MODE_QR && !P.stop_le) ? (last_res < (double)P.eps)
-                                                        : (last_res <= (double)P.eps);
-      if (stop) {
+      last_res = s_misc_d[1];  // squared until the epilogue
+      if (s_stop) {
         converged = true;
         stamp(4);
         break;
@@ -1000,7 +1062,7 @@ drot_solve_kernel(const SolveParams P) {
   // <C, X> of the last objective-bearing iteration: the CTA partials of that
   // iteration are the last ones written (visible since its barriers).
   if (blockIdx.x == 0 && warp == 0 && obj_valid && !aborted)
-    last_obj = warp_sum_strided(P.cta_obj, G, lane);
+    last_obj = fp_value(warp_sum_strided_fp(P.cta_obj, G, lane));
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     DeviceStats* st = P.stats;
     st->iters_run = converged ? it + 1 : it;
@@ -1011,9 +1073,9 @@ drot_solve_kernel(const SolveParams P) {
     st->status = (aborted || ld_volatile_i32(P.abort_flag)) ? 3 : 0;
     st->objective_valid = obj_valid;
     st->objective = last_obj;
-    st->residual = last_res;
+    st->residual = last_res >= 0.0 ? sqrt(last_res) : last_res;
     st->sigma = last_sigma;
-    for (int q = 0; q < 4; ++q) st->phase_ns[q] = s_tacc[q];
+    for (int q = 0; q < 4; ++q) st->phase_ns[q] = (double)s_tacc[q];
     *P.alpha = alpha;
   }
 }

@@ -70,6 +70,55 @@ DROT_HD void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
+// Float-pair ("double-float") sums for the per-iteration reductions (mass,
+// objective, squared residual).  A pair (hi, lo) stands for hi + lo with
+// |lo| <= ulp(hi)/2 after fp_add; sums of n terms carry about 44 bits, which
+// is more than the reference's float sums (core/kernel_qr.hpp:92-111, 432-440)
+// and, unlike FP64 -- a narrow pipe on this part -- run on the FP32 units.
+struct fpair {
+  float hi, lo;
+};
+
+DROT_HD fpair fp_make(float v) { return fpair{v, 0.0f}; }
+
+// Sum of two pairs (TwoSum of the heads, tails added, Fast2Sum renormalise).
+DROT_HD fpair fp_add(fpair a, fpair b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  e += a.lo + b.lo;
+  const float h = s + e;
+  return fpair{h, e - (h - s)};
+}
+
+// Exact square v*v as a pair (TwoProduct with one fma).
+DROT_HD fpair fp_sqr(float v) {
+#ifdef __CUDA_ARCH__
+  const float p = __fmul_rn(v, v);  // not contracted into the fma below
+  return fpair{p, __fmaf_rn(v, v, -p)};
+#else
+  const float p = v * v;
+  return fpair{p, fmaf(v, v, -p)};
+#endif
+}
+
+DROT_HD double fp_value(fpair a) { return (double)a.hi + (double)a.lo; }
+
+// The device tests the squared residual r2 (FP64) against one threshold T:
+// sqrt(r2) < eps (strict, QR) or sqrt(r2) <= eps (GL, numpy-API loop) holds
+// exactly when r2 < T, with T the smallest double whose correctly rounded
+// square root is >= eps (strict) or > eps.  sqrt is monotonic, so T is found
+// by stepping from eps^2 one ulp at a time (a few steps at most).
+inline double res2_threshold(float eps_f, bool strict) {
+  const double e = (double)eps_f;
+  if (!(e >= 0.0)) return -1.0;              // eps < 0 or NaN: never stop
+  if (isinf(e)) return INFINITY;             // every finite residual stops
+  auto ok = [&](double t) { return strict ? sqrt(t) >= e : sqrt(t) > e; };
+  double t = e * e;
+  while (t > 0.0 && ok(nextafter(t, 0.0))) t = nextafter(t, 0.0);
+  while (!ok(t)) t = nextafter(t, INFINITY);
+  return t;
+}
+
 // Group-lasso shrink factor max(1 - lambda / (sqrt(ns) + 1e-9), 0).
 //
 // The reference evaluates it in double from a float norm

@@ -51,3 +51,20 @@ def test_gl_shrink_matches_double_formula(tmp_path):
     n, exact, one, more = (int(v) for v in out.stdout.split())
     assert out.returncode == 0 and more == 0
     assert one <= n * 1e-5 and exact + one == n
+
+
+def test_pair_sums_and_stop_threshold(tmp_path):
+    """The float-pair reductions (mass, objective, squared residual) carry at
+    least 2^-40 relative accuracy in the kernels' summation orders, and the
+    squared-residual threshold reproduces sqrt(r2) < eps / <= eps exactly
+    (drot_math.cuh: fp_add, fp_sqr, res2_threshold)."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no host C++ compiler")
+    exe = str(tmp_path / "sum_check")
+    subprocess.check_call([cxx, "-O2", "-ffp-contract=off", "-I", INC, "-o", exe,
+                           os.path.join(REPO, "tests", "native", "sum_check.cpp")])
+    out = subprocess.run([exe], capture_output=True, text=True)
+    bad, worst = out.stdout.split()
+    assert out.returncode == 0 and int(bad) == 0
+    assert float(worst) < 2.0 ** -40
