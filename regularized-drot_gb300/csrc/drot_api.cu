@@ -505,6 +505,10 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
   prm.bar = (unsigned int*)(ws + pl.off_ctrl);
   prm.abort_flag = (int*)(ws + pl.off_ctrl + 64);
   prm.stats = (DeviceStats*)(ws + pl.off_stats);
+  // DROT_TIMER_CTA: the CTA whose stage times the result record reports
+  // (default 0; a profiling knob).
+  prm.timer_cta = getenv("DROT_TIMER_CTA") ? atoi(getenv("DROT_TIMER_CTA")) : 0;
+  if (prm.timer_cta < 0 || prm.timer_cta >= pl.grid) prm.timer_cta = 0;
   prm.timeout_ns = barrier_timeout_ns();
 
   if (cudaMemsetAsync(ws, 0, 512, A.stream) != cudaSuccess) return DROT_ERR_CUDA;

@@ -224,12 +224,19 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
     for (int v = 0; v < 4; ++v) {
       const float4 f1 = *reinterpret_cast<const float4*>(f1s + (v % KVR) * SV + lane * VEC);
       const float f1a[VEC] = {f1.x, f1.y, f1.z, f1.w};
+      // Element math on packed pairs (.f32x2; each lane rounds as the scalar
+      // instruction).
+      const f32x2 f2b = x2_pack(f2[v / KVR], f2[v / KVR]);
+#pragma unroll
+      for (int h = 0; h < VEC; h += 2) {
+        f32x2 tt = x2_add(x2_add(x2_pack(xv[v][h], xv[v][h + 1]), x2_pack(f1a[h], f1a[h + 1])), f2b);
+        if constexpr (EV)
+          tt = x2_fma(x2_pack(-s, -s), x2_pack(c_at<CT>(cv[v], h), c_at<CT>(cv[v], h + 1)), tt);
+        x2_unpack(tt, xv[v][h], xv[v][h + 1]);
+      }
 #pragma unroll
       for (int e = 0; e < VEC; ++e) {
-        float tt = (xv[v][e] + f1a[e]) + f2[v / KVR];
-        if constexpr (EV) tt = fmaf(-s, c_at<CT>(cv[v], e), tt);
-        xv[v][e] = tt;
-        const unsigned key = (unsigned)__float_as_int(tt) - 1u;
+        const unsigned key = (unsigned)__float_as_int(xv[v][e]) - 1u;
         tmin = min(tmin, valid(v, e) ? key : 0xffffffffu);
       }
     }
@@ -241,6 +248,49 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
     for (int cc = 0; cc < NCOL; ++cc) colp[cc] = 0.0f;
     auto body = [&](auto slow_tag) {
       constexpr bool SLOW = decltype(slow_tag)::value;
+      if constexpr (!SLOW) {
+        const f32x2 nk = x2_pack(-kappa, -kappa), ky = x2_pack(krcp, krcp);
+        const f32x2 ns2 = x2_pack(-s, -s);
+        f32x2 col2[NCOL], obj2 = x2_pack(0.0f, 0.0f);
+#pragma unroll
+        for (int cc = 0; cc < NCOL; ++cc) col2[cc] = x2_pack(0.0f, 0.0f);
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+#pragma unroll
+          for (int h = 0; h < VEC; h += 2) {
+            const bool ok0 = valid(v, h), ok1 = valid(v, h + 1);
+            f32x2 y = x2_div_rn_by_fma(
+                x2_pack(fmaxf(xv[v][h], 0.0f), fmaxf(xv[v][h + 1], 0.0f)), nk, ky);
+            if constexpr (!(FULL && NCOL == 1)) {
+              float y0, y1;
+              x2_unpack(y, y0, y1);
+              y = x2_pack(ok0 ? y0 : 0.0f, ok1 ? y1 : 0.0f);
+            }
+            if constexpr (EV) {
+              // the caller's padding may hold anything
+              const f32x2 c2 = x2_pack(ok0 ? c_at<CT>(cv[v], h) : 0.0f,
+                                       ok1 ? c_at<CT>(cv[v], h + 1) : 0.0f);
+              x2_unpack(x2_fma(ns2, c2, y), xv[v][h], xv[v][h + 1]);
+              obj2 = x2_fma(y, c2, obj2);
+            } else {
+              x2_unpack(y, xv[v][h], xv[v][h + 1]);
+            }
+            float* ac = acc[v % KVR];
+            x2_unpack(x2_add(x2_pack(ac[h], ac[h + 1]), y), ac[h], ac[h + 1]);
+            col2[v / KVR] = x2_add(col2[v / KVR], y);
+          }
+        float u0, u1;
+#pragma unroll
+        for (int cc = 0; cc < NCOL; ++cc) {
+          x2_unpack(col2[cc], u0, u1);
+          colp[cc] = u0 + u1;
+        }
+        if constexpr (EV) {
+          x2_unpack(obj2, u0, u1);
+          objp = u0 + u1;
+        }
+        return;
+      }
 #pragma unroll
       for (int v = 0; v < 4; ++v)
 #pragma unroll

@@ -17,6 +17,15 @@ The forward tolerance matters for dL/dp, dL/dq: at 1e-6 a weakly
 regularised case (200 x 150, r_weight 1e-3) leaves one support entry of 359
 undecided, which moves dL/dp by a few percent while dL/dC stays within
 1e-4 (measured with the FP32 oracle on the CPU).
+
+dL/dp, dL/dq are unique up to one constant per connected component of the
+support graph.  An entry whose FP64 margin phi1_i + phi2_j - s C_ij is
+within 1e-5 of s max C is not decided by an FP32 forward at 1e-7 (the
+1000 x 64 case has one at 4e-6 that bridges two components).  Flipping one
+such bridge leaves the adjoint solution the same up to the constants of the
+two components it joins (the bridge only adds the relation a_i + b_j =
+G_ij), so dL/dC is unchanged and dL/dp, dL/dq are compared in the gauge of
+the components of the support without the undecided entries.
 """
 import numpy as np
 import pytest
@@ -66,6 +75,14 @@ def _component_gauge(S, a, b):
     return a, b
 
 
+def _decided_support(o, c, s, rel=1e-5):
+    """The FP64 support minus the entries an FP32 forward cannot decide
+    (|margin| below rel * s * max C)."""
+    c = np.asarray(c, np.float64)
+    m = o["phi1"][None, :] + o["phi2"][:, None] - s * c
+    return (m > 0) & (np.abs(m) >= rel * s * np.abs(c).max())
+
+
 def _rel(a, b):
     a = np.asarray(a, np.float64)
     b = np.asarray(b, np.float64)
@@ -91,7 +108,7 @@ def test_qr_gradient_matches_fp64_reference(cuda, solver_lib, nr, nc, rw, w):
     assert abs(loss.item() - L) <= 1e-4 * abs(L)
     assert _rel(c.grad.cpu().numpy(), gc) <= TOL_C, _rel(c.grad.cpu().numpy(), gc)
     assert abs(float(pt.grad.sum() - qt.grad.sum())) <= 1e-5 * float(pt.grad.abs().sum())
-    S = A.support(o, c.detach().double().cpu().numpy(), A.O.step_size(RHO, nr, nc))
+    S = _decided_support(o, c.detach().double().cpu().numpy(), A.O.step_size(RHO, nr, nc))
     ga_g, gb_g = _component_gauge(S, pt.grad.cpu().numpy(), qt.grad.cpu().numpy())
     ga_r, gb_r = _component_gauge(S, ga, gb)
     assert _rel(ga_g, ga_r) <= TOL_PQ, _rel(ga_g, ga_r)
