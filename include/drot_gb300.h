@@ -314,6 +314,14 @@ int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance *inst,
 void drot_batch_plan_destroy(drot_batch_plan plan);
 /* Workspace bytes of a plan (device memory, 256-byte aligned). */
 size_t drot_batch_plan_workspace_bytes(drot_batch_plan plan);
+/* Profiling (no counterpart in the reference): later launches of the plan
+ * record, for iterations it < cap, CTA 0's device clock (globaltimer, ns) at
+ * the start of iteration it, after its fused-update tiles, after the first
+ * grid barrier and after its dual-update items in times[4 it + 0..3] (4 cap
+ * entries), and the coarse tiles of unconverged instances at the start in
+ * active_tiles[it] (cap entries).  cap = 0 switches the record off. */
+int drot_batch_set_iteration_log(drot_batch_plan plan, unsigned long long *times,
+                                 unsigned *active_tiles, int cap);
 /* Number of tiles (work units of one iteration). */
 int drot_batch_plan_tiles(drot_batch_plan plan);
 /* Copies the plan's descriptors into the workspace; synchronises `stream`. */

@@ -41,7 +41,9 @@ struct BatchInst {
   int nbands, band_h;
   int tile0, ntiles, P;                  // coarse tiles (global indices), column chunks
   int tile0f, ntilesf, Pf;               // fine tiles (global indices), column chunks
+  int tile0x, ntilesx, Px;               // finest tiles (global indices), column chunks
   int item0, nitems;                     // dual-update items (contiguous)
+  int item0x, nitemsx;                   // short items of the finest level (contiguous)
   int row_off, col_off;                  // its rows / columns in the packed state arrays
   float s, kappa, kappa_rcp, eps, nc_rcp, nr_rcp;
   float w_phi1, w_phi2, w_a, w_b, w_alpha;  // warm-start constants
@@ -73,7 +75,12 @@ struct BatchParams {
   const BatchItem* items;
   int n_inst, n_tiles, max_iters, n_items;
   int n_tiles_f;       // fine tiles, stored after the n_tiles coarse ones
-  int fine_threshold;  // fine list once fewer active coarse tiles remain
+  int n_tiles_x;       // finest tiles, stored after the fine ones
+  int n_items_x;       // short items of the finest level, stored after the n_items others
+  const int* order;    // instances by decreasing size (the order of the active lists)
+  int* act;            // active lists: tile indices per level in the tiles' own index
+                       // ranges, then item indices (n_tiles + ... entries, then items)
+  int fine_threshold;  // next (finer) list once fewer active tiles of the current one remain
   float *a, *b, *phi1, *phi2;  // packed state
   float* alpha;                // [2][n_inst], by iteration parity
   float2* res_slot;            // per item: squared residual (float pair)
@@ -89,10 +96,19 @@ struct BatchParams {
   float cscale;
   int dim;
   unsigned* counters;  // [0], [1]: tile counters of even / odd iterations; [2]: converged
-                       // instances; [3]: coarse tiles of unconverged instances
+                       // instances; [3]: coarse tiles of unconverged instances;
+                       // [8..12]: lengths of the active lists (tiles of levels 0-2,
+                       // items, short items)
   unsigned* bar;
   int* abort_flag;
   long long timeout_ns;
+  // Optional profile of CTA 0 for iterations it < iter_log_cap: globaltimer
+  // at the start of the iteration, after its fused-update tiles, after the
+  // first barrier and after its dual-update items (iter_log[4 it + 0..3]),
+  // and the active coarse tiles at the start.
+  unsigned long long* iter_log;
+  unsigned* iter_tiles;
+  int iter_log_cap;
 };
 
 constexpr int kBatchKV = 4;
@@ -289,26 +305,26 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
           x2_unpack(obj2, u0, u1);
           objp = u0 + u1;
         }
-        return;
-      }
+      } else {
 #pragma unroll
-      for (int v = 0; v < 4; ++v)
+        for (int v = 0; v < 4; ++v)
 #pragma unroll
-        for (int e = 0; e < VEC; ++e) {
-          const bool ok = valid(v, e);
-          const float a0 = fmaxf(xv[v][e], 0.0f);
-          float y = SLOW ? a0 / kappa : div_rn_by_fma(a0, kappa, krcp);
-          y = ok ? y : 0.0f;
-          if constexpr (EV) {
-            const float c = ok ? c_at<CT>(cv[v], e) : 0.0f;  // the caller's padding may hold anything
-            xv[v][e] = fmaf(-s, c, y);
-            objp = fmaf(y, c, objp);
-          } else {
-            xv[v][e] = y;
+          for (int e = 0; e < VEC; ++e) {
+            const bool ok = valid(v, e);
+            const float a0 = fmaxf(xv[v][e], 0.0f);
+            float y = a0 / kappa;
+            y = ok ? y : 0.0f;
+            if constexpr (EV) {
+              const float c = ok ? c_at<CT>(cv[v], e) : 0.0f;  // the caller's padding may hold anything
+              xv[v][e] = fmaf(-s, c, y);
+              objp = fmaf(y, c, objp);
+            } else {
+              xv[v][e] = y;
+            }
+            acc[v % KVR][e] += y;
+            colp[v / KVR] += y;
           }
-          acc[v % KVR][e] += y;
-          colp[v / KVR] += y;
-        }
+      }
     };
     if (slow) body(std::true_type());
     else body(std::false_type());
@@ -351,10 +367,37 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
 // 4 lines and issues the loads of 8 partials of each before adding any (one
 // L2 round trip per 32 loads instead of one per line); per line the
 // partials are added in index order.  use(l, sum) consumes each line.
+// Short ranges (fewer lines than threads / 2) take g = 2..32 threads per
+// line instead: thread `sub` of a line adds partials sub, sub + g, ... in
+// index order and a shuffle tree of fixed shape combines the g sums.
 template <typename F>
 __device__ __forceinline__ void reduce_lines(const float* base, int stride, int lo, int hi, int n,
                                              F&& use) {
   const int nt = blockDim.x;
+  if (hi <= lo) return;
+  int g = 1;
+  while (g < 32 && (hi - lo) * g * 2 <= nt) g <<= 1;
+  if (g > 1) {
+    const int sub = threadIdx.x & (g - 1);
+    const int l = lo + (int)threadIdx.x / g;
+    float t = 0.0f;
+    if (l < hi) {
+      for (int c0 = sub; c0 < n; c0 += 8 * g) {
+        float v[8];
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) {
+          const int c = c0 + cc * g;
+          v[cc] = c < n ? __ldcg(base + (long long)c * stride + l) : 0.0f;
+        }
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc)
+          if (c0 + cc * g < n) t += v[cc];
+      }
+    }
+    for (int o = g >> 1; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (sub == 0 && l < hi) use(l, t);
+    return;
+  }
   for (int l0 = lo + threadIdx.x; l0 < hi; l0 += 4 * nt) {
     float s[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     for (int c0 = 0; c0 < n; c0 += 8) {
@@ -402,6 +445,60 @@ __global__ void point_norms_kernel(const float* pts, int n, int dim, float* out)
   }
 }
 
+// Active lists (CTA 0, all threads): the tiles of every level and the
+// dual-update items of the unconverged instances, largest instances first
+// (P.order), so the fused update and the dual update never step over
+// converged instances and the last tiles taken in an iteration are small
+// ones (the wait at the following barrier is the length of the last tile).
+// Rebuilt at the start and whenever an instance converged (at most once per
+// instance); a grid barrier publishes them.  scan: 5 * blockDim ints.
+__device__ void build_active_lists(const BatchParams& P, int* scan) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int base[5] = {0, P.n_tiles, P.n_tiles + P.n_tiles_f, 0, P.n_items};
+  const int T = P.n_tiles + P.n_tiles_f + P.n_tiles_x;
+  __shared__ int s_carry[5];  // running totals of the lists
+  if (tid < 5) s_carry[tid] = 0;
+  __syncthreads();
+  for (int k0 = 0; k0 < P.n_inst; k0 += nt) {
+    const int k = k0 + tid < P.n_inst ? P.order[k0 + tid] : -1;
+    int cnt[5] = {0, 0, 0, 0, 0};
+    BatchInst I;
+    const bool live = k >= 0 && !__ldcg(P.conv + k);
+    if (live) {
+      I = P.inst[k];
+      cnt[0] = I.ntiles;
+      cnt[1] = P.n_tiles_f > 0 ? I.ntilesf : 0;
+      cnt[2] = P.n_tiles_x > 0 ? I.ntilesx : 0;
+      cnt[3] = I.nitems;
+      cnt[4] = P.n_items_x > 0 ? I.nitemsx : 0;
+    }
+#pragma unroll
+    for (int l = 0; l < 5; ++l) scan[l * nt + tid] = cnt[l];
+    __syncthreads();
+    for (int o = 1; o < nt; o <<= 1) {  // inclusive Hillis-Steele scan
+      int v[5];
+#pragma unroll
+      for (int l = 0; l < 5; ++l) v[l] = tid >= o ? scan[l * nt + tid - o] : 0;
+      __syncthreads();
+#pragma unroll
+      for (int l = 0; l < 5; ++l) scan[l * nt + tid] += v[l];
+      __syncthreads();
+    }
+    if (live) {
+      const int src0[5] = {I.tile0, I.tile0f, I.tile0x, I.item0, I.item0x};
+#pragma unroll
+      for (int l = 0; l < 5; ++l) {
+        int* dst = P.act + (l < 3 ? 0 : T) + base[l] + s_carry[l] + scan[l * nt + tid] - cnt[l];
+        for (int u = 0; u < cnt[l]; ++u) dst[u] = src0[l] + u;
+      }
+    }
+    __syncthreads();
+    if (tid < 5) s_carry[tid] += scan[tid * nt + nt - 1];
+    __syncthreads();
+  }
+  if (tid < 5) P.counters[8 + tid] = (unsigned)s_carry[tid];
+}
+
 template <typename CT, int DIM>
 __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P) {
   constexpr int VEC = 4, KV = kBatchKV, S = kBatchS;
@@ -424,17 +521,43 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
   unsigned epoch = 0;
   bool aborted = false;
   int it = 0;
-  // Tile list of the iteration: the coarse one while enough tiles remain to
-  // keep every CTA busy, then the fine one.  The switch is read from the
-  // active-tile count after the decision barrier, so every CTA switches at
-  // the same iteration.
-  bool fine = P.n_tiles_f > 0 && P.n_tiles < P.fine_threshold;
+  // Tile list of the iteration (level 0: coarse, 1: fine, 2: finest, with
+  // its own short dual-update items): the coarse one while enough tiles
+  // remain to keep every CTA busy, then the next finer one.  The switch is
+  // read from the active-tile counts after the decision barrier, so every CTA
+  // switches at the same iteration.
+  const int list1 = P.n_tiles, list2 = P.n_tiles + P.n_tiles_f;
+  const int items0 = P.n_tiles + P.n_tiles_f + P.n_tiles_x;  // item part of P.act
+  int n_act[5];        // active list lengths (tiles of levels 0-2, items, short items)
+  unsigned conv_seen;  // converged instances when the lists were last built
+  int level = 0;
+  // Builds the lists (CTA 0), publishes them and moves to a finer level once
+  // the current one leaves CTAs idle.  False when the run was aborted.
+  auto rebuild = [&]() -> bool {
+    if (blockIdx.x == 0) build_active_lists(P, reinterpret_cast<int*>(smem_raw));
+    if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag)) return false;
+#pragma unroll
+    for (int l = 0; l < 5; ++l) n_act[l] = (int)__ldcg(P.counters + 8 + l);
+    conv_seen = __ldcg(P.counters + 2);
+    if (level == 0 && P.n_tiles_f > 0 && n_act[0] < P.fine_threshold) level = 1;
+    if (level == 1 && P.n_tiles_x > 0 && n_act[1] < P.fine_threshold) level = 2;
+    return true;
+  };
+  if (!rebuild()) aborted = true;
 
-  for (; it < P.max_iters; ++it) {
+  for (; it < P.max_iters && !aborted; ++it) {
     const bool even = (it & 1) == 0;
     unsigned* counter = P.counters + (it & 1);
-    const int n_list = fine ? P.n_tiles_f : P.n_tiles;
-    const int list0 = fine ? P.n_tiles : 0;
+    const bool logit = P.iter_log && it < P.iter_log_cap && blockIdx.x == 0 && threadIdx.x == 0;
+    if (logit) {
+      P.iter_log[4 * it] = globaltimer_ns();
+      P.iter_tiles[it] = __ldcg(P.counters + 3);
+    }
+    const int n_list = n_act[level];
+    const int list0 = level == 0 ? 0 : (level == 1 ? list1 : list2);
+    // Active dual-update items of the level: P.act[qa + 0 .. nq).
+    const int qa = items0 + (level == 2 ? P.n_items : 0);
+    const int nq = n_act[level == 2 ? 4 : 3];
 
     // ---------------------------------------------------------- fused update
     for (;;) {
@@ -442,7 +565,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
       __syncthreads();
       if (s_tile >= n_list) break;
-      const int t = list0 + s_tile;
+      const int t = __ldcg(P.act + list0 + s_tile);
       const BatchTile T = P.tiles[t];
       if (__ldcg(P.conv + T.inst)) continue;
       const BatchInst I = P.inst[T.inst];
@@ -527,26 +650,29 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       }
     }
 
+    if (logit) P.iter_log[4 * it + 1] = globaltimer_ns();
     if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag)) {
       aborted = true;
       break;
     }
 
+    if (logit) P.iter_log[4 * it + 2] = globaltimer_ns();
     // ---------------------------------------------------------- dual update
     // Item q: lines [l0, l1) of one instance (kernel_qr.hpp:405-467).  Every
     // item of the instance recomputes sigma from the tile sums; alpha is
     // read from this iteration's parity and written (by the first item) to
     // the other one.
     if (blockIdx.x == 0 && threadIdx.x == 0) P.counters[(it + 1) & 1] = 0u;
-    for (int qi = blockIdx.x; qi < P.n_items; qi += G) {
+    for (int qq = blockIdx.x; qq < nq; qq += G) {
+      const int qi = __ldcg(P.act + qa + qq);
       const BatchItem Q = P.items[qi];
       const int k = Q.inst;
       if (__ldcg(P.conv + k)) continue;
       const BatchInst I = P.inst[k];
-      const bool first = qi == I.item0;
-      const int t0 = fine ? I.tile0f : I.tile0;
-      const int ntl = fine ? I.ntilesf : I.ntiles;
-      const int nchunks = fine ? I.Pf : I.P;
+      const bool first = qi == (level == 2 ? I.item0x : I.item0);
+      const int t0 = level == 0 ? I.tile0 : (level == 1 ? I.tile0f : I.tile0x);
+      const int ntl = level == 0 ? I.ntiles : (level == 1 ? I.ntilesf : I.ntilesx);
+      const int nchunks = level == 0 ? I.P : (level == 1 ? I.Pf : I.Px);
       fpair sg = fp_make(0.0f), og = fp_make(0.0f);
       for (int i = threadIdx.x; i < ntl; i += blockDim.x) {
         const float2 u = __ldcg(P.tile_sum + t0 + i);
@@ -590,6 +716,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       __syncthreads();
     }
 
+    if (logit) P.iter_log[4 * it + 3] = globaltimer_ns();
     if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag)) {
       aborted = true;
       break;
@@ -599,16 +726,23 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       // Stop test (drot_qr.hpp:219-229: even iterations, residual < eps), by
       // the CTA of each instance's first item, then one more barrier so the
       // next fused update sees every decision.
-      if (threadIdx.x == 0) {
-        for (int qi = blockIdx.x; qi < P.n_items; qi += G) {
+      // Warp 0 sums an instance's item residuals (lanes in parallel, fixed
+      // order), lane 0 decides.
+      if (warp == 0) {
+        for (int qq = blockIdx.x; qq < nq; qq += G) {
+          const int qi = __ldcg(P.act + qa + qq);
           const int k = P.items[qi].inst;
           const BatchInst& I = P.inst[k];
-          if (qi != I.item0 || __ldcg(P.conv + k)) continue;
+          const int i0 = level == 2 ? I.item0x : I.item0;
+          const int ni = level == 2 ? I.nitemsx : I.nitems;
+          if (qi != i0 || __ldcg(P.conv + k)) continue;
           fpair r2 = fp_make(0.0f);
-          for (int t = 0; t < I.nitems; ++t) {
-            const float2 u = __ldcg(P.res_slot + I.item0 + t);
+          for (int t = lane; t < ni; t += 32) {
+            const float2 u = __ldcg(P.res_slot + i0 + t);
             r2 = fp_add(r2, fpair{u.x, u.y});
           }
+          r2 = warp_sum_fp(r2);
+          if (lane != 0) continue;
           BatchStat st = P.stats[k];
           st.objective = __ldcg(P.obj_slot + k);
           st.objective_valid = 1;
@@ -634,7 +768,10 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
         ++it;
         break;
       }
-      if (!fine && P.n_tiles_f > 0 && (int)__ldcg(P.counters + 3) < P.fine_threshold) fine = true;
+      if (__ldcg(P.counters + 2) != conv_seen && !rebuild()) {
+        aborted = true;
+        break;
+      }
     }
   }
 
@@ -694,17 +831,20 @@ static const size_t kAl = 256;
 static inline size_t al(size_t v) { return (v + kAl - 1) / kAl * kAl; }
 
 struct BatchPlanImpl {
-  int n_inst = 0, n_tiles = 0, n_tiles_f = 0, grid = 0, threads = 256, cols_per_tile = 0;
+  int n_inst = 0, n_tiles = 0, n_tiles_f = 0, n_tiles_x = 0, n_items = 0, n_items_x = 0;
+  int grid = 0, threads = 256, cols_per_tile = 0;
   int band_rows = 512;
   size_t smem = 0;
   long long rows = 0, cols = 0, rowpart = 0, colpart = 0;
   std::vector<BatchInst> inst;
-  std::vector<BatchTile> tiles;  // coarse tiles, then fine tiles
+  std::vector<BatchTile> tiles;  // coarse tiles, then fine tiles, then finest tiles
+  // dual-update items (n_items), then the finest level's short ones (n_items_x)
   std::vector<BatchItem> items;
+  std::vector<int> order;        // instances by decreasing n_rows * n_cols
   // workspace layout
   size_t off_ctrl = 0, off_inst = 0, off_tiles = 0, off_items = 0, off_a = 0, off_b = 0,
          off_phi1 = 0, off_phi2 = 0, off_alpha = 0, off_rp = 0, off_cp = 0, off_tsum = 0,
-         off_tobj = 0, off_res = 0, off_obj = 0, off_conv = 0, off_stats = 0, off_xn = 0,
+         off_tobj = 0, off_res = 0, off_obj = 0, off_conv = 0, off_stats = 0, off_act = 0, off_order = 0, off_xn = 0,
          off_yn = 0, total = 0;
   bool uploaded_any = false;
 };
@@ -731,6 +871,23 @@ static int item_lines() {  // lines per dual-update item (DROT_BATCH_ITEM_LINES 
   const char* e = getenv("DROT_BATCH_ITEM_LINES");
   const int v = e ? atoi(e) : 0;
   return v > 0 ? v : 1024;
+}
+// The finest level, used once the fine list too leaves CTAs idle (in the
+// 256-instance workload: the last few instances, mostly the single largest,
+// for the last two thirds of the iterations): 32-column tiles, so a lone
+// 2048-column instance still spreads over ~250 CTAs, and 64-line dual-update
+// items, so the row sums over its ~60 column chunks are spread as widely.
+// DROT_BATCH_FINEST_COLS (0 disables the level) and
+// DROT_BATCH_FINEST_ITEM_LINES override them.
+static int finest_cols() {
+  const char* e = getenv("DROT_BATCH_FINEST_COLS");
+  const int v = e ? atoi(e) : -1;
+  return v >= 0 ? v : 32;
+}
+static int finest_item_lines() {
+  const char* e = getenv("DROT_BATCH_FINEST_ITEM_LINES");
+  const int v = e ? atoi(e) : 0;
+  return v > 0 ? v : 64;
 }
 
 // Tiles of one instance: every 512-row band x `chunks` column chunks.
@@ -764,6 +921,9 @@ using namespace drot;
 
 struct drot_batch_plan_s {
   BatchPlanImpl p;
+  unsigned long long* iter_log = nullptr;  // optional profile (drot_batch_set_iteration_log)
+  unsigned* iter_tiles = nullptr;
+  int iter_log_cap = 0;
 };
 
 extern "C" {
@@ -806,6 +966,7 @@ int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int c
     I.nbands = (d.n_rows + band_rows - 1) / band_rows;
     I.P = (d.n_cols + cols_per_tile - 1) / cols_per_tile;
     I.Pf = (d.n_cols + fine_cols() - 1) / fine_cols();
+    I.Px = finest_cols() > 0 ? (d.n_cols + finest_cols() - 1) / finest_cols() : 0;
     I.tile0 = (int)P.tiles.size();
     add_tiles(P.tiles, k, I, I.P);
     I.ntiles = (int)P.tiles.size() - I.tile0;
@@ -815,7 +976,7 @@ int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int c
     I.cp_off = cpp;
     rows += d.n_rows;
     cols += d.n_cols;
-    rp += (long long)std::max(I.P, I.Pf) * d.n_rows;
+    rp += (long long)std::max(std::max(I.P, I.Pf), I.Px) * d.n_rows;
     I.item0 = (int)P.items.size();
     const int ilines = item_lines();
     for (int l = 0; l < d.n_rows + d.n_cols; l += ilines) {
@@ -864,6 +1025,36 @@ int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int c
     I.ntilesf = (int)P.tiles.size() - I.tile0f;
   }
   P.n_tiles_f = fine_cols() < cols_per_tile ? (int)P.tiles.size() - P.n_tiles : 0;
+  // The finest list after the fine one (only when the fine list is used).
+  const bool use_x = P.n_tiles_f > 0 && finest_cols() > 0 && finest_cols() < fine_cols();
+  const int x0 = (int)P.tiles.size();
+  P.n_items = (int)P.items.size();
+  for (int k = 0; k < n_inst; ++k) {
+    BatchInst& I = P.inst[k];
+    I.tile0x = (int)P.tiles.size();
+    if (use_x) add_tiles(P.tiles, k, I, I.Px);
+    I.ntilesx = (int)P.tiles.size() - I.tile0x;
+    I.item0x = (int)P.items.size();
+    if (use_x) {
+      const int xl = finest_item_lines();
+      for (int l = 0; l < I.nr + I.nc; l += xl) {
+        BatchItem Q;
+        Q.inst = k;
+        Q.l0 = l;
+        Q.l1 = std::min(l + xl, I.nr + I.nc);
+        Q.pad = 0;
+        P.items.push_back(Q);
+      }
+    }
+    I.nitemsx = (int)P.items.size() - I.item0x;
+  }
+  P.n_tiles_x = (int)P.tiles.size() - x0;
+  P.n_items_x = (int)P.items.size() - P.n_items;
+  P.order.resize(n_inst);
+  for (int k = 0; k < n_inst; ++k) P.order[k] = k;
+  std::stable_sort(P.order.begin(), P.order.end(), [&](int a, int b) {
+    return (long long)P.inst[a].nr * P.inst[a].nc > (long long)P.inst[b].nr * P.inst[b].nc;
+  });
   P.rows = rows;
   P.cols = cols;
   P.rowpart = rp;
@@ -910,6 +1101,8 @@ int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int c
   P.off_obj = off;   off = al(off + sizeof(double) * n_inst);
   P.off_conv = off;  off = al(off + sizeof(int) * n_inst);
   P.off_stats = off; off = al(off + sizeof(BatchStat) * n_inst);
+  P.off_act = off;   off = al(off + sizeof(int) * (P.tiles.size() + P.items.size()));
+  P.off_order = off; off = al(off + sizeof(int) * n_inst);
   P.off_xn = off;    off = al(off + sizeof(float) * rows);
   P.off_yn = off;    off = al(off + sizeof(float) * cols);
   P.total = off;
@@ -942,6 +1135,8 @@ int drot_batch_upload(drot_batch_plan plan, void* workspace, size_t workspace_by
                       cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaMemcpyAsync(ws + P.off_items, P.items.data(), sizeof(BatchItem) * P.items.size(),
                       cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(ws + P.off_order, P.order.data(), sizeof(int) * P.n_inst,
+                      cudaMemcpyHostToDevice, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return DROT_ERR_CUDA;
   return DROT_OK;
@@ -958,9 +1153,11 @@ static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, 
   B.n_inst = P.n_inst;
   B.n_tiles = P.n_tiles;
   B.n_tiles_f = P.n_tiles_f;
+  B.n_tiles_x = P.n_tiles_x;
+  B.n_items_x = P.n_items_x;
   B.fine_threshold = P.grid / fine_divisor();
   B.items = (const BatchItem*)(ws + P.off_items);
-  B.n_items = (int)P.items.size();
+  B.n_items = P.n_items;
   B.res_slot = (float2*)(ws + P.off_res);
   B.obj_slot = (double*)(ws + P.off_obj);
   B.max_iters = max_iters;
@@ -975,6 +1172,8 @@ static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, 
   B.tile_obj = (float2*)(ws + P.off_tobj);
   B.conv = (int*)(ws + P.off_conv);
   B.stats = (BatchStat*)(ws + P.off_stats);
+  B.act = (int*)(ws + P.off_act);
+  B.order = (const int*)(ws + P.off_order);
   B.counters = (unsigned*)(ws + P.off_ctrl);
   B.bar = (unsigned*)(ws + P.off_ctrl + 64);
   B.abort_flag = (int*)(ws + P.off_ctrl + 128);
@@ -1010,6 +1209,9 @@ int drot_qr_batch_launch(drot_batch_plan plan, const void* c, int c_dtype, const
   B.p = p;
   B.q = q;
   B.x = x;
+  B.iter_log = plan->iter_log;
+  B.iter_tiles = plan->iter_tiles;
+  B.iter_log_cap = plan->iter_log_cap;
   const void* fn = c_dtype == DROT_C_F32 ? (const void*)batch_solve_kernel<float, 0>
                                          : (const void*)batch_solve_kernel<__nv_bfloat16, 0>;
   return batch_launch(plan->p, fn, B, workspace, workspace_bytes, max_iters,
@@ -1041,6 +1243,9 @@ int drot_qr_batch_launch_points(drot_batch_plan plan, const float* xpts, const f
   B.ynorm = (const float*)(ws + P.off_yn);
   B.cscale = cost_scale;
   B.dim = dim;
+  B.iter_log = plan->iter_log;
+  B.iter_tiles = plan->iter_tiles;
+  B.iter_log_cap = plan->iter_log_cap;
   point_norms_kernel<<<(int)std::min<long long>((P.rows + 255) / 256, 1024), 256, 0, st>>>(
       xpts, (int)P.rows, dim, (float*)(ws + P.off_xn));
   point_norms_kernel<<<(int)std::min<long long>((P.cols + 255) / 256, 1024), 256, 0, st>>>(
@@ -1049,6 +1254,15 @@ int drot_qr_batch_launch_points(drot_batch_plan plan, const float* xpts, const f
   const void* fn = dim == 8 ? (const void*)batch_solve_kernel<float, 8>
                             : (const void*)batch_solve_kernel<float, 16>;
   return batch_launch(P, fn, B, workspace, workspace_bytes, max_iters, st);
+}
+
+int drot_batch_set_iteration_log(drot_batch_plan plan, unsigned long long* times,
+                                 unsigned* active_tiles, int cap) {
+  if (!plan || cap < 0 || (cap > 0 && (!times || !active_tiles))) return DROT_ERR_INVALID_ARG;
+  plan->iter_log = cap > 0 ? times : nullptr;
+  plan->iter_tiles = cap > 0 ? active_tiles : nullptr;
+  plan->iter_log_cap = cap;
+  return DROT_OK;
 }
 
 int drot_batch_state(drot_batch_plan plan, void* workspace, float** phi1, float** phi2) {

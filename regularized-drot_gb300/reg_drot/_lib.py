@@ -135,6 +135,7 @@ SIGNATURES = {
     "drot_batch_plan_destroy": (None, [_vp]),
     "drot_batch_plan_workspace_bytes": (_c_size, [_vp]),
     "drot_batch_plan_tiles": (_c_int, [_vp]),
+    "drot_batch_set_iteration_log": (_c_int, [_vp, _vp, _vp, _c_int]),
     "drot_batch_upload": (_c_int, [_vp, _vp, _c_size, _vp]),
     "drot_qr_batch_launch": (_c_int, [_vp, _vp, _c_int, _vp, _vp, _vp, _c_int, _vp, _c_size,
                                       _vp]),

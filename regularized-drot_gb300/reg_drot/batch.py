@@ -150,6 +150,23 @@ class QRBatch:
     def tiles(self, cols_per_tile):
         return int(lib().drot_batch_plan_tiles(self._plan(cols_per_tile)))
 
+    def iteration_log(self, cap, cols_per_tile=None):
+        """Profile the next launches with tile width ``cols_per_tile``: returns
+        (times [cap, 4] int64, active_tiles [cap] int32) device tensors that
+        each launch fills, for iterations it < cap, with CTA 0's device clock
+        (ns) at the start of the iteration, after its fused-update tiles,
+        after the first grid barrier and after its dual-update items, and the
+        coarse tiles of unconverged instances at the start
+        (drot_batch_set_iteration_log).  cap = 0 switches it off."""
+        cpt = cols_per_tile or self.cols_per_tile or 128
+        times = torch.zeros(max(cap, 1), 4, dtype=torch.int64, device=self.device)
+        tiles = torch.zeros(max(cap, 1), dtype=torch.int32, device=self.device)
+        check(lib().drot_batch_set_iteration_log(self._plan(cpt), times.data_ptr(),
+                                                 tiles.data_ptr(), int(cap)),
+              "batch_set_iteration_log")
+        self._log = (times, tiles) if cap > 0 else None  # keeps the buffers alive
+        return times, tiles
+
     # ------------------------------------------------------------------ solve
     def _check(self, c, p, q, x):
         if c.device != self.device or c.dim() != 1 or c.numel() != self.total or \
