@@ -193,3 +193,36 @@ def test_batch_with_more_tiles_than_ctas(cuda, solver_lib):
         if info[k]["n_iter"] == ir["n_iter"]:
             _assert_close_x(xs[k].cpu().numpy(), xr.cpu().numpy())
     assert len({r["n_iter"] for r in info}) > 1
+
+
+@pytest.mark.parametrize("env", [{"DROT_BATCH_FINEST_COLS": "0"},
+                                 {"DROT_BATCH_FINEST_COLS": "0", "DROT_BATCH_FINE_DIV": "0"}])
+def test_batch_tile_levels_match_oracle(cuda, solver_lib, monkeypatch, env):
+    # The default plan moves to 128-column and then 32-column tiles (with
+    # 64-line dual items) as instances converge; these plans stop at the
+    # fine level or keep the coarse tiles throughout.  Every level must give
+    # the oracle's solution.
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    B, insts, c, p, q = _batch(SHAPES, cuda, marg="dirichlet", cpt=256)
+    x, info = B.solve(c, p, q, 20000)
+    xs = B.unpack(x)
+    for k, (ci, pi, qi) in enumerate(insts):
+        o = O.quadratic_drot(ci.numpy(), pi.numpy(), qi.numpy(), 2.0, 1e-3, 20000, 1e-4)
+        assert info[k]["converged"] == 1
+        assert abs(info[k]["n_iter"] - o["n_iter"]) <= 2, (k, info[k], o["n_iter"])
+        if info[k]["n_iter"] == o["n_iter"]:
+            _assert_close_x(xs[k].cpu().numpy(), o["x"])
+
+
+def test_batch_iteration_log(cuda, solver_lib):
+    B, insts, c, p, q = _batch(SHAPES, cuda, cpt=128)
+    times, tiles = B.iteration_log(100000, 128)
+    x, info = B.solve(c, p, q, 20000)
+    n = max(r["iters_run"] for r in info)
+    t = times[:n].cpu().numpy()
+    assert (t > 0).all()
+    assert (np.diff(t, axis=1) >= 0).all() and (t[1:, 0] >= t[:-1, 3]).all()
+    a = tiles[:n].cpu().numpy()
+    assert a[0] == B.tiles(128) and (np.diff(a) <= 0).all()
+    B.iteration_log(0, 128)
