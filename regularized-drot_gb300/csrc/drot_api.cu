@@ -479,13 +479,12 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
   prm.c = A.c; prm.p = A.p; prm.q = A.q; prm.x = A.x;
   prm.a = A.a; prm.b = A.b; prm.phi1 = A.phi1; prm.phi2 = A.phi2; prm.alpha = A.alpha;
   prm.ld = ld; prm.nr = A.nr; prm.nc = A.nc;
-  prm.s = A.s; prm.kappa = A.kappa; prm.lambda = A.lambda; prm.eps = A.eps;
+  prm.s = A.s; prm.kappa = A.kappa; prm.lambda = A.lambda;
   // RN(1/kappa): the double quotient rounded to float is the correctly
   // rounded float reciprocal (53 >= 2*24 + 2).
   prm.kappa_rcp = (float)(1.0 / (double)A.kappa);
   prm.nc_rcp = (float)(1.0 / (double)(float)A.nc);
   prm.nr_rcp = (float)(1.0 / (double)(float)A.nr);
-  prm.norm_eps = 1e-9;
   prm.max_iters = A.max_iters;
   prm.stop_every = A.stop_every;
   prm.stop_le = A.stop_le;

@@ -88,11 +88,10 @@ struct SolveParams {
   float nc_rcp;        // RN(1 / float(nc))
   float nr_rcp;        // RN(1 / float(nr))
   float lambda;        // GL threshold
-  float eps;           // absolute residual tolerance
   double res2_stop;    // stop when the squared residual (FP64) is below this:
                        // the exact image of the "< eps" / "<= eps" test on
-                       // its square root (set by the host)
-  double norm_eps;     // GL: constant added to the group norm (1e-9)
+                       // its square root of the absolute tolerance eps
+                       // (set by the host)
   int max_iters;
   int stop_every;      // QR: test every iteration (numpy-API loop), not only even ones
   int stop_le;         // QR: stop on residual <= eps (numpy-API loop) instead of < eps
@@ -224,25 +223,6 @@ __device__ __forceinline__ fpair block_sum_fp(fpair v, fpair* scratch) {
   }
   __syncthreads();
   return scratch[nw];
-}
-
-// Sum of v[0..n) (FP64) over one warp: every lane issues its first 16
-// strided loads at once (grids up to 512 CTAs take one round trip), then a
-// fixed add tree and a shuffle tree; all lanes get the same result.
-__device__ __forceinline__ double warp_sum_strided(const double* v, int n, int lane) {
-  double a[16];
-#pragma unroll
-  for (int u = 0; u < 16; ++u) {
-    const int i = lane + 32 * u;
-    a[u] = i < n ? __ldcg(v + i) : 0.0;
-  }
-#pragma unroll
-  for (int w = 8; w > 0; w >>= 1)
-#pragma unroll
-    for (int u = 0; u < w; ++u) a[u] += a[u + w];
-  double t = a[0];
-  for (int i = lane + 512; i < n; i += 32) t += __ldcg(v + i);
-  return warp_sum_d(t);
 }
 
 // Grid barrier.  Returns false when the run was aborted (time limit hit here
