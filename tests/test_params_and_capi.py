@@ -176,6 +176,9 @@ def test_batch_plan_rejects_bad_descriptors_on_the_host(solver_lib):
     solver_lib.drot_batch_plan_destroy(None)
     assert solver_lib.drot_qr_batch_launch(None, None, 0, None, None, None, 10, None, 0,
                                            None) == 1
+    # the profile log needs a plan, and buffers whenever cap > 0
+    assert solver_lib.drot_batch_set_iteration_log(None, None, None, 0) == 1
+    assert solver_lib.drot_batch_set_iteration_log(None, None, None, -1) == 1
 
 
 def test_cost_and_adjoint_reject_bad_arguments_on_the_host(solver_lib):
