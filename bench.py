@@ -701,13 +701,66 @@ def run_diff_case(n_inst, iters):
     return 0
 
 
+def run_batch_timeline():
+    """Timeline of one solve of the batched workload (256 instances): CTA 0's
+    device clock at four points of every iteration (QRBatch.iteration_log),
+    summarised per iteration range as mean stage times (--case batchlog)."""
+    import torch
+    from reg_drot.batch import QRBatch
+    dev = torch.device("cuda", 0)
+    shapes, costs, ps, qs, eps = make_batch_problem(dev)
+    B = QRBatch(shapes, RHO, ALPHA, eps, device=dev)
+    c = B.pack_c(costs)
+    p, q = B.pack_marginals(ps, qs)
+    cpt = B.autotune(c, p, q, iters=200)
+    x = B.empty_x()
+    B.launch(c, p, q, x, 10 ** 6)
+    times, _ = B.iteration_log(30000, cpt)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    B.launch(c, p, q, x, 10 ** 6)
+    b.record()
+    b.synchronize()
+    B.iteration_log(0, cpt)
+    info = B.results()
+    it = np.array([r["n_iter"] for r in info])
+    elems = np.array([m * n for m, n in shapes], dtype=np.float64)
+    n = min(int(it.max()) - 1, 30000)
+    t = times[:n].cpu().numpy().astype(np.float64) / 1e3  # us
+    total = np.append(np.diff(t[:, 0]), np.nan)
+    rest = np.append(t[1:, 0] - t[:-1, 3], np.nan)
+    rows = []
+    edges = [0, 2000, 3000, 4000, 6000, 10000, n]
+    for lo, hi in zip(edges[:-1], edges[1:]):
+        if hi <= lo:
+            continue
+        sl = slice(lo, hi)
+        ev = np.arange(lo, hi) % 2 == 0
+        rows.append({"iterations": [lo, hi],
+                     "active_elements_M": float(elems[it > lo].sum() / 1e6),
+                     "us_per_iteration": float(np.nanmean(total[sl])),
+                     "fused_update_us": float(np.mean(t[sl, 1] - t[sl, 0])),
+                     "barrier1_wait_us": float(np.mean(t[sl, 2] - t[sl, 1])),
+                     "dual_update_us": float(np.mean(t[sl, 3] - t[sl, 2])),
+                     "rest_even_us": float(np.nanmean(rest[sl][ev])),
+                     "rest_odd_us": float(np.nanmean(rest[sl][~ev])),
+                     "seconds": float(np.nansum(total[sl]) / 1e6)})
+    print(json.dumps({"case": "batchlog", "cols_per_tile": cpt, "tiles": B.tiles(cpt),
+                      "s_per_batch": a.elapsed_time(b) / 1e3,
+                      "n_iter_max": int(it.max()), "ranges": rows}), flush=True)
+    return 0
+
+
 def run_case(spec):
     """One solve of the headline workload at size n for a fixed iteration count
     (for profiler captures): --case n:iters[:gl][:bf16]; --case diff:n_inst:iters
-    for the differentiable workload's kernels."""
+    for the differentiable workload's kernels; --case batchlog for the
+    batched solver's per-iteration timeline."""
     import torch
     import reg_drot
     parts = spec.split(":")
+    if parts[0] == "batchlog":
+        return run_batch_timeline()
     if parts[0] == "diff":
         return run_diff_case(int(parts[1]), int(parts[2]))
     n, iters = int(parts[0]), int(parts[1])
