@@ -319,7 +319,8 @@ size_t drot_batch_plan_workspace_bytes(drot_batch_plan plan);
  * the start of iteration it, after its fused-update tiles, after the first
  * grid barrier and after its dual-update items in times[4 it + 0..3] (4 cap
  * entries), and the coarse tiles of unconverged instances at the start in
- * active_tiles[it] (cap entries).  cap = 0 switches the record off. */
+ * active_tiles[it] (cap entries).  cap = 0 switches the record off.  The
+ * buffers must stay allocated while the record is on. */
 int drot_batch_set_iteration_log(drot_batch_plan plan, unsigned long long *times,
                                  unsigned *active_tiles, int cap);
 /* Number of tiles (work units of one iteration). */
