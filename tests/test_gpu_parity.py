@@ -8,7 +8,8 @@ or the device-pointer loops drot_qr_solve / drot_gl_solve
 Tolerances (FP32 solver vs the FP32 oracle on the same inputs): the element
 operations are the same FP32 operations in the same order, but the row,
 column, norm and mass sums are accumulated in a different order (per-lane
-FP32 partials, FP64 across lanes, warps and CTAs, vs the oracle's FP64), so
+FP32 partials, float pairs across lanes, warps and CTAs, vs the oracle's
+FP64), so
 the iterates agree to FP32 rounding:
   * ||X - X_o||_F <= 1e-5 * ||X_o||_F  (the 1e-5 relative bar on X),
   * max|X - X_o| <= 1e-4 * max|X_o|    (single entries; the GL shrink factor
