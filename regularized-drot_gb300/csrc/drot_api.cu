@@ -57,12 +57,15 @@ static SolveFn kernel_kv(int vec, int kv) {
   return nullptr;
 }
 
-// Single-barrier (LDU) instances: QR, register path, 4-wide vectors.
-template <typename CT>
+// Single-barrier (LDU) instances: register path, 4-wide vectors.
+template <int MODE, typename CT>
 static SolveFn kernel_ldu(int kv) {
-  if (kv == 1) return drot_solve_kernel<MODE_QR, 4, 1, false, CT, true>;
-  if (kv == 2) return drot_solve_kernel<MODE_QR, 4, 2, false, CT, true>;
-  if (kv == 4) return drot_solve_kernel<MODE_QR, 4, 4, false, CT, true>;
+  if (kv == 1) return drot_solve_kernel<MODE, 4, 1, false, CT, true>;
+  if (kv == 2) return drot_solve_kernel<MODE, 4, 2, false, CT, true>;
+  if (kv == 4) return drot_solve_kernel<MODE, 4, 4, false, CT, true>;
+  if constexpr (MODE == MODE_GL) {
+    if (kv == 8) return drot_solve_kernel<MODE, 4, 8, false, CT, true>;
+  }
   return nullptr;
 }
 
@@ -71,8 +74,12 @@ static SolveFn kernel_ldu(int kv) {
 static SolveFn kernel_for(int mode, int vec, int kv, bool tma, int ctype = DROT_C_F32,
                           bool ldu = false) {
   if (ldu) {
-    if (mode != MODE_QR || tma || vec != 4) return nullptr;
-    return ctype == DROT_C_BF16 ? kernel_ldu<__nv_bfloat16>(kv) : kernel_ldu<float>(kv);
+    if (tma || vec != 4) return nullptr;
+    if (mode == MODE_QR)
+      return ctype == DROT_C_BF16 ? kernel_ldu<MODE_QR, __nv_bfloat16>(kv)
+                                  : kernel_ldu<MODE_QR, float>(kv);
+    return ctype == DROT_C_BF16 ? kernel_ldu<MODE_GL, __nv_bfloat16>(kv)
+                                : kernel_ldu<MODE_GL, float>(kv);
   }
   if (ctype == DROT_C_BF16) {
     if (tma) return nullptr;
@@ -192,7 +199,7 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
                               Plan& pl, const int* ubounds, bool ldu = false) {
   if (nr <= 0 || nc <= 0) return DROT_ERR_INVALID_ARG;
   if (tma && vec != 4) return DROT_ERR_UNSUPPORTED;
-  if (ldu && (mode != MODE_QR || tma || vec != 4)) return DROT_ERR_UNSUPPORTED;
+  if (ldu && (tma || vec != 4)) return DROT_ERR_UNSUPPORTED;
   const DeviceInfo dev = device_info();
   if (!dev.ok) return DROT_ERR_CUDA;
   pl = Plan();
@@ -445,9 +452,10 @@ static int path_override() {
 // part the fused update is bound by per-warp instruction latency, and two
 // 8-warp CTAs per SM with register-resident segments beat one 16-warp CTA
 // fed by the shared-memory TMA ring.  DROT_PATH=tma selects the ring.
-// DROT_LDU=1 asks for the single-barrier QR kernels (one grid barrier per
+// DROT_LDU=1 asks for the single-barrier kernels (one grid barrier per
 // iteration, every CTA reducing its own band's and chunk's partials); they
-// are used where their plan fits, else the two-barrier kernels.
+// are used where their plan fits (one warp per band or group), else the
+// two-barrier kernels.
 static bool ldu_requested() {
   const char* e = getenv("DROT_LDU");
   return e && atoi(e) == 1;
@@ -460,7 +468,7 @@ static int choose_plan(int mode, int nr, int nc, int G, bool aligned4, Plan& pl,
     if (!aligned4) return DROT_ERR_UNSUPPORTED;
     return make_plan(mode, nr, nc, G, 4, true, pl, DROT_C_F32, ubounds);
   }
-  if (mode == MODE_QR && aligned4 && ldu_requested() &&
+  if (aligned4 && ldu_requested() &&
       make_plan(mode, nr, nc, G, 4, false, pl, ctype, ubounds, true) == DROT_OK)
     return DROT_OK;
   return make_plan(mode, nr, nc, G, aligned4 ? 4 : 1, false, pl, ctype, ubounds);
@@ -475,7 +483,7 @@ static size_t scratch_bytes(int mode, int nr, int nc, int G, const int* ubounds 
     best = std::max(best, pl.total);
   if (make_plan(mode, nr, nc, G, 1, false, pl, DROT_C_F32, ubounds) == DROT_OK)
     best = std::max(best, pl.total);
-  if (mode == MODE_QR && ldu_requested() &&
+  if (ldu_requested() &&
       make_plan(mode, nr, nc, G, 4, false, pl, DROT_C_F32, ubounds, true) == DROT_OK)
     best = std::max(best, pl.total);
   return best;

@@ -568,7 +568,7 @@ template <int MODE, int VEC, int KV, bool TMA, typename CT = float, bool LDU = f
 __global__ void __launch_bounds__(512, 1)
 drot_solve_kernel(const SolveParams P) {
   static_assert(!TMA || VEC == 4, "the TMA path moves 16-byte vectors");
-  static_assert(!LDU || (MODE == MODE_QR && !TMA && VEC == 4), "LDU: QR register path");
+  static_assert(!LDU || (!TMA && VEC == 4), "LDU: register path, 4-wide vectors");
   static_assert(!TMA || std::is_same<CT, float>::value, "the TMA path streams float costs");
   const CT* const cbase = reinterpret_cast<const CT*>(P.c);
   constexpr int SV = 32 * VEC;        // rows per vector slot of a warp

@@ -1,4 +1,4 @@
-"""GPU: the single-barrier QR kernels (DROT_LDU=1) against the oracle.
+"""GPU: the single-barrier kernels (DROT_LDU=1, QR and GL) against the oracle.
 
 These kernels are opt-in and not yet measured, so this module runs only when
 DROT_TEST_LDU=1 is set.  The bars are those of the default kernels
@@ -87,3 +87,22 @@ def test_ldu_is_deterministic_and_matches_two_barrier_kernels(cuda, solver_lib, 
     assert abs(i1["n_iter"] - i3["n_iter"]) <= 2
     if i1["n_iter"] == i3["n_iter"]:
         _close(x1.cpu().numpy(), x3.cpu().numpy())
+
+
+@pytest.mark.parametrize("nr,nc,G", [(1500, 1000, 2), (600, 300, 2), (1001, 200, 3)])
+def test_ldu_group_lasso_matches_fp64_oracle(cuda, solver_lib, monkeypatch, nr, nc, G):
+    # The bar of the default GL kernels: within max(1e-5, 2 x the FP32
+    # oracle's own error) of the FP64 oracle on X and the objective.
+    import reg_drot
+    monkeypatch.setenv("DROT_LDU", "1")
+    c, p, q = _problem(nr, nc, nr * 11 + nc + G)
+    x, info, _ = reg_drot.solve_gl(c.to(cuda), p.to(cuda), q.to(cuda), G, 2.0, 1e-3, 20000, 1e-4)
+    o32 = O.group_lasso_drot(c.numpy(), p.numpy(), q.numpy(), G, 2.0, 1e-3, 20000, 1e-4)
+    o64 = O.group_lasso_drot(c.numpy(), p.numpy(), q.numpy(), G, 2.0, 1e-3, 20000, 1e-4,
+                             dtype=np.float64)
+    assert info["status"] == 0 and info["converged"] == 1
+    assert abs(info["n_iter"] - o32["n_iter"]) <= max(1, o32["n_iter"] // 50)
+    x64 = o64["x"]
+    ref_err = np.linalg.norm(o32["x"] - x64) / np.linalg.norm(x64)
+    err = np.linalg.norm(x.cpu().numpy().astype(np.float64) - x64) / np.linalg.norm(x64)
+    assert err <= max(RTOL_X, 2.0 * ref_err), (err, ref_err)
