@@ -57,17 +57,8 @@ static SolveFn kernel_kv(int vec, int kv) {
   return nullptr;
 }
 
-// Single-barrier (LDU) instances: register path, 4-wide vectors.
-template <int MODE, typename CT>
-static SolveFn kernel_ldu(int kv) {
-  if (kv == 1) return drot_solve_kernel<MODE, 4, 1, false, CT, true>;
-  if (kv == 2) return drot_solve_kernel<MODE, 4, 2, false, CT, true>;
-  if (kv == 4) return drot_solve_kernel<MODE, 4, 4, false, CT, true>;
-  if constexpr (MODE == MODE_GL) {
-    if (kv == 8) return drot_solve_kernel<MODE, 4, 8, false, CT, true>;
-  }
-  return nullptr;
-}
+// Single-barrier (LDU) instances, in drot_solve_ldu.cu.
+SolveFn solve_kernel_ldu(int mode, int kv, bool bf16);
 
 // Kernel instance for (mode, vector width, vectors per lane, data path, cost
 // type).  The TMA ring exists for float costs only.
@@ -75,11 +66,7 @@ static SolveFn kernel_for(int mode, int vec, int kv, bool tma, int ctype = DROT_
                           bool ldu = false) {
   if (ldu) {
     if (tma || vec != 4) return nullptr;
-    if (mode == MODE_QR)
-      return ctype == DROT_C_BF16 ? kernel_ldu<MODE_QR, __nv_bfloat16>(kv)
-                                  : kernel_ldu<MODE_QR, float>(kv);
-    return ctype == DROT_C_BF16 ? kernel_ldu<MODE_GL, __nv_bfloat16>(kv)
-                                : kernel_ldu<MODE_GL, float>(kv);
+    return solve_kernel_ldu(mode, kv, ctype == DROT_C_BF16);
   }
   if (ctype == DROT_C_BF16) {
     if (tma) return nullptr;
