@@ -1,29 +1,49 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 DROT solver.
 
-Headline workload (one step = one full solve):
-  quadratic-regularised DROT, m = n = 3000, C ~ U[0,1) float32, p, q ~
-  Dirichlet(1), r_weight (alpha) = 1e-3, rho = 2, warm start, stop at a
-  relative marginal residual ||(X1-p, X^T1-q)||_2 / ||(p;q)||_2 < 1e-4.
-  Metric: solves/s (whole job).
+Headline -- the metric "solves/s at marginal error 1e-4, batched + adjoint
+against the plain solver; X-update HBM GB/s against the peak".  One step =
+forward + backward of the differentiable OT loss over one batch:
 
-  value  solves with C, p, q resident in HBM, through reg_drot.solve_qr (the
-         drop-in operator's C-ABI entry point); L2 flushed between solves.
-  e2e    the same solve through the host-buffer C-ABI wrapper
-         (drot_qr_wrapper, the reference's quadratic_regularizer_drot_wrapper):
-         device allocation, H2D of C/p/q, solve, D2H of X per step.
-  roofline  the solve kernel: algorithmic bytes (12 B/element on iterations
-         that read C, 8 B on the others, 12 B for the final unfold) over its
-         measured time, against the measured HBM copy bandwidth.
-  cpu_baseline  the oracle (C restatement of the reference loop, OpenMP on all
-         host cores) timed on a bounded number of iterations of the same
-         solve and scaled to the iterations a solve takes.
+  64 quadratic-regularised DROT instances, m, n ~ U{512..4096}, points
+  x (m x 16), y (n x 16) ~ N(0, 1) (numpy default_rng(1239)), C = |x - y|^2
+  / 64 built on the tensor cores, uniform p, q, alpha = 1e-3, rho = 2, warm
+  start, every instance stopped at its relative marginal residual 1e-4
+  (||(X1 - p, X^T1 - q)||_2 / ||(p; q)||_2); loss = sum_k <C_k, X_k> +
+  w ||X_k||_F^2 with a fixed random w; backward = the implicit adjoint
+  (support masks, batched Jacobi-PCG) and the chain rule to x and y.
+  Seeded synthetic clouds stand in for the reference's data.
 
-`--impl reference` times that CPU implementation alone (the reference's
-solver is CUDA and its CPU implementation is numpy; neither runs on the GPU
-host, so the oracle port stands in for it).
+  value        instances solved with gradient per second: 64 x steps over
+               the device time of the steps (CUDA events; point clouds
+               resident in HBM; the solve streams 3.0 GB of X and C per
+               iteration, far beyond L2, and L2 is flushed before every step).
+  e2e          the same step through the public API from pinned host point
+               clouds: H2D of x and y, the step, D2H of dL/dx, dL/dy and the
+               loss, by wall clock.
+  plain        the same 64 instances one at a time with the drop-in
+               operator's entry point (reg_drot.solve_qr: FP32, forward
+               only); batched_over_plain = value / plain.
+  roofline     batch_solve_kernel, the dominant kernel of the step:
+               algorithmic bytes of its launch (12 B per element on the
+               iterations that read C, 8 B on the others, 12 B for the final
+               unfold) over its measured time, against the measured HBM copy
+               bandwidth; x_update_10000 inside it: the single-instance fused
+               X-update at 10000^2 (X + C = 800 MB, HBM resident), 400
+               iterations.
+  cpu_baseline the oracle (C restatement of the reference loop, OpenMP on
+               every host core) solving instances of the same workload one
+               at a time to the same stop -- forward only: the reference has
+               no backward.
 
-Multi-GPU: the solve does not shard; N ranks run N independent replicas.
+`--impl reference` times that CPU implementation alone.  The reference's own
+CPU solver is numpy, whose sources do not reach the GPU host; the oracle port
+stands in for it (on the reference's CPU-runnable 1000^2 case the numpy
+solver takes 42.6 ms per iteration and the port 0.80 ms on the same 8 cores:
+oracle/time_reference_numpy.py).
+
+Multi-GPU: the instances are independent and a step does not shard; N ranks
+run N independent replicas (weak scaling).
 """
 import argparse
 import ctypes
@@ -44,19 +64,52 @@ for _p in (REPO, PKG):
 
 import numpy as np  # noqa: E402
 
-N = 3000
 ALPHA = 1e-3
 RHO = 2.0
 REL_EPS = 1e-4
 SEED = 1234
-# DR iterations one solve of this workload takes (measured on the GPU solver;
-# the CPU restatement runs the same iteration map).  Used to scale the
-# bounded CPU samples to a full solve.
-ITERS_PER_SOLVE = 113831
-WORKLOAD = (f"QR-DROT {N}x{N}, C~U[0,1) fp32, p,q~Dirichlet(1), alpha={ALPHA}, rho={RHO}, "
-            f"warm start, stop at relative marginal residual {REL_EPS}")
-METRIC = f"solves/s at relative marginal error {REL_EPS} (QR-DROT {N}x{N}, alpha={ALPHA})"
+N = 3000              # the dense single-instance workload (extra.qr_3000)
 L2_FLUSH_BYTES = 512 << 20
+MAX_ITERS = 10 ** 6
+
+DIFF_INSTANCES = 64
+DIFF_MIN, DIFF_MAX = 512, 4096
+DIFF_DIM = 16
+DIFF_SCALE = 1.0 / (4 * DIFF_DIM)  # C = |x - y|^2 / 64: mean cost 0.5 for N(0, I_16) clouds
+DIFF_SEED = SEED + 5
+
+WORKLOAD = (f"differentiable QR-DROT loss, {DIFF_INSTANCES} instances, m,n ~ U{{{DIFF_MIN}..{DIFF_MAX}}}, "
+            f"x,y ~ N(0,I_{DIFF_DIM}), C = |x-y|^2/64 (tcgen05 split-TF32), alpha={ALPHA}, "
+            f"rho={RHO}, uniform marginals, relative eps {REL_EPS}, loss = sum <C,X*> + w|X*|^2, "
+            "forward + backward per step")
+METRIC = (f"solves/s at marginal error {REL_EPS:g}, batched forward+backward "
+          f"({DIFF_INSTANCES} differentiable QR-DROT instances)")
+CONFIG = {"workload": WORKLOAD, "instances": DIFF_INSTANCES, "m_n_range": [DIFF_MIN, DIFF_MAX],
+          "dim": DIFF_DIM, "alpha": ALPHA, "rho": RHO, "rel_eps": REL_EPS, "seed": DIFF_SEED,
+          "l2": "flushed (512 MB write) before every timed step; X + C = 3.0 GB streamed per iteration"}
+
+
+def diff_workload(seed=DIFF_SEED):
+    """Shapes, concatenated point clouds (host, float32), the loss weight w
+    and the absolute stop tolerance of every instance."""
+    rng = np.random.default_rng(seed)
+    shapes = [(int(a), int(b)) for a, b in
+              rng.integers(DIFF_MIN, DIFF_MAX + 1, size=(DIFF_INSTANCES, 2))]
+    xs = rng.standard_normal((sum(m for m, _ in shapes), DIFF_DIM), dtype=np.float32)
+    ys = rng.standard_normal((sum(n for _, n in shapes), DIFF_DIM), dtype=np.float32)
+    w = float(rng.random())
+    eps = [REL_EPS * math.sqrt(1.0 / m + 1.0 / n) for m, n in shapes]
+    return shapes, xs, ys, w, eps
+
+
+def instance_slices(shapes):
+    xo = yo = 0
+    out = []
+    for m, n in shapes:
+        out.append((slice(xo, xo + m), slice(yo, yo + n)))
+        xo += m
+        yo += n
+    return out
 
 
 def make_problem(n, seed=SEED):
@@ -78,16 +131,27 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profile_traffic_per_iteration():
-    """DRAM bytes per DR iteration of the solve kernel from the committed ncu summary."""
-    path = os.path.join(REPO, "profiles", "drot_solve_qr_3000.md")
+def profile_value(name, key):
+    """A `key: value` line of a committed ncu summary under profiles/."""
     try:
-        for line in open(path):
-            if line.startswith("dram_bytes_per_iteration:"):
+        for line in open(os.path.join(REPO, "profiles", name)):
+            if line.startswith(key + ":"):
                 return float(line.split(":")[1])
-    except OSError:
+    except (OSError, ValueError):
         pass
     return None
+
+
+def solve_bytes(shapes, info, cbytes=4):
+    """Algorithmic bytes of one batched solve launch: per instance, elements
+    x (12 B on the iterations that read C, 8 B on the others, 12 B for the
+    final unfold of a converged instance) with cbytes-byte C."""
+    tot = 0.0
+    for (m, n), r in zip(shapes, info):
+        t = int(r["iters_run"])
+        tot += float(m) * n * ((8 + cbytes) * ((t + 1) // 2) + 8 * (t // 2) +
+                               ((8 + cbytes) if r["converged"] else 0))
+    return tot
 
 
 # --------------------------------------------------------------------------- clocks
@@ -151,86 +215,85 @@ class ClockSampler:
 
 # --------------------------------------------------------------------------- CPU legs
 
-def cpu_sample(budget_s=12.0, threads=None):
-    """Time the oracle on a bounded number of iterations of the workload."""
+def cpu_cost(xk, yk):
+    """C = |x - y|^2 / 64 of one instance ([n, m] float32, FP64 arithmetic)."""
+    x = xk.astype(np.float64)
+    y = yk.astype(np.float64)
+    c = (y * y).sum(1)[:, None] + (x * x).sum(1)[None, :] - 2.0 * (y @ x.T)
+    return (np.maximum(c, 0.0) * DIFF_SCALE).astype(np.float32)
+
+
+def cpu_solve_instance(k, shapes, xs, ys, eps, threads=None):
+    """The oracle (FP32 restatement of the reference loop) solving instance k
+    of the headline workload to its stop; returns (seconds, n_iter)."""
     from oracle import oracle as O
-    c, p, q, eps = make_problem(N)  # c is [n_cols, n_rows], the operator's layout
-    s = O.step_size(RHO, N, N)
-    kappa = O.qr_scale(s, ALPHA, N, N, "torch")
-    threads = threads or O.lib().oracle_max_threads()
-    O.qr_solve(c, p, q, s, kappa, 2, eps, threads=threads)  # page in, spin up threads
-    iters, spent = 0, 0.0
-    chunk = 10
-    while spent < budget_s:
-        t0 = time.perf_counter()
-        O.qr_solve(c, p, q, s, kappa, chunk, eps, threads=threads)
-        spent += time.perf_counter() - t0
-        iters += chunk
-        chunk = min(chunk * 2, 400)
-    per_iter = spent / iters
-    value = 1.0 / (per_iter * ITERS_PER_SOLVE)
-    return {"value": value, "unit": "solves/s", "cores": int(threads), "kind": "port",
-            "sample": (f"{iters} DR iterations of the {N}x{N} QR solve from the warm start "
-                       f"(FP32 oracle, {threads} OpenMP threads, {spent:.1f} s), scaled to the "
-                       f"{ITERS_PER_SOLVE} iterations of a full solve"),
-            "s_per_iteration": per_iter}
+    m, n = shapes[k]
+    sx, sy = instance_slices(shapes)[k]
+    c = cpu_cost(xs[sx], ys[sy])
+    p = np.full(m, 1.0 / m, np.float32)
+    q = np.full(n, 1.0 / n, np.float32)
+    t0 = time.perf_counter()
+    o = O.quadratic_drot(c, p, q, RHO, ALPHA, MAX_ITERS, eps[k], threads=threads)
+    return time.perf_counter() - t0, int(o["n_iter"])
+
+
+def cpu_sample(budget_s=15.0):
+    """cpu_baseline: instances of the headline workload solved one at a time
+    by the oracle on every host core, in workload order, until budget_s."""
+    from oracle import oracle as O
+    shapes, xs, ys, _, eps = diff_workload()
+    threads = int(O.lib().oracle_max_threads())
+    small = int(np.argmin([m * n for m, n in shapes]))
+    cpu_solve_instance(small, shapes, xs, ys, eps, threads)  # page in, spin up threads
+    spent, done, iters = 0.0, 0, []
+    while spent < budget_s and done < len(shapes):
+        t, it = cpu_solve_instance(done, shapes, xs, ys, eps, threads)
+        spent += t
+        iters.append(it)
+        done += 1
+    return {"value": done / spent, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": (f"instances 0..{done - 1} of the {len(shapes)} solved to their stop one at "
+                       f"a time by the FP32 oracle ({threads} OpenMP threads, {spent:.1f} s, "
+                       f"{sum(iters)} iterations); forward only -- the reference has no backward")}
 
 
 def run_reference(args):
+    """The reference arm: the oracle port solving instances of the headline
+    workload one at a time on the host cores, one full solve per step."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return 0
+    from oracle import oracle as O
+    shapes, xs, ys, _, eps = diff_workload()
+    threads = int(O.lib().oracle_max_threads())
+    small = int(np.argmin([m * n for m, n in shapes]))
     for _ in range(args.warmup):
-        cpu_sample(budget_s=0.5)
-    vals = [cpu_sample(budget_s=10.0) for _ in range(args.steps)]
-    value = statistics.median(v["value"] for v in vals)
-    base = dict(vals[0])
-    base["value"] = value
+        cpu_solve_instance(small, shapes, xs, ys, eps, threads)
+    times, iters = [], []
+    for i in range(args.steps):
+        t, it = cpu_solve_instance(i % len(shapes), shapes, xs, ys, eps, threads)
+        times.append(t)
+        iters.append(it)
+    total = sum(times)
+    value = args.steps / total
+    sample = (f"one full solve per step: instances 0..{min(args.steps, len(shapes)) - 1} of the "
+              f"{len(shapes)} (warm-up: the smallest), FP32 oracle on {threads} OpenMP threads, "
+              f"{sum(iters)} iterations in {total:.1f} s; forward only -- the reference has no "
+              "backward")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_rows": N, "n_cols": N, "alpha": ALPHA, "rho": RHO,
-                   "rel_eps": REL_EPS, "seed": SEED},
-        "cpu_baseline": base,
+        "ms_per_step": 1000.0 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": CONFIG,
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": sample},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
 
-
-# --------------------------------------------------------------------------- GPU legs
-
-def e2e_wrapper(c, p, q, eps, steps):
-    """Solves through drot_qr_wrapper with pinned host buffers (host in, host out)."""
-    import torch
-    from reg_drot import _lib
-    L = _lib.lib()
-    ct = torch.from_numpy(c).pin_memory()  # column-major n_rows x n_cols
-    pt = torch.from_numpy(p).pin_memory()
-    qt = torch.from_numpy(q).pin_memory()
-    s = float(np.float32(RHO) / (np.float32(N) + np.float32(N)))
-    dur, prep = ctypes.c_float(), ctypes.c_float()
-    nit, obj = ctypes.c_int(), ctypes.c_float()
-
-    def once():
-        ptr = L.drot_qr_wrapper(ct.data_ptr(), pt.data_ptr(), qt.data_ptr(), N, N, s, ALPHA,
-                                10 ** 9, eps, ctypes.byref(dur), ctypes.byref(prep),
-                                ctypes.byref(nit), ctypes.byref(obj), 1, 1)
-        if not ptr:
-            raise RuntimeError(f"drot_qr_wrapper failed: {_lib.status_string(L.drot_last_status())}")
-        L.drot_free_host(ptr)
-
-    once()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        once()
-    wall = time.perf_counter() - t0
-    return {"value": steps / wall, "unit": "solves/s",
-            "h2d_bytes_per_step": (N * N + 2 * N) * 4, "d2h_bytes_per_step": N * N * 4,
-            "n_iter": nit.value, "wall_s_per_step": wall / steps}
 
 
 def hbm_point(dev, flush):
@@ -439,117 +502,168 @@ def batched_point(dev, flush, single_sample=16):
     return out
 
 
-DIFF_INSTANCES = 64
-DIFF_MIN, DIFF_MAX = 512, 4096
-DIFF_DIM = 16
-DIFF_SCALE = 1.0 / (4 * DIFF_DIM)  # C = |x - y|^2 / 64: mean cost 0.5 for N(0, I_16) clouds
+# --------------------------------------------------------------------------- GPU legs
+
+class DiffStep:
+    """The headline step on one device: plan, marginals and the step."""
+
+    def __init__(self, dev, shapes, eps, w):
+        import torch
+        from reg_drot.batch import QRBatch
+        self.dev = dev
+        self.shapes = shapes
+        self.w = w
+        self.B = QRBatch(shapes, RHO, ALPHA, eps, device=dev)
+        self.p, self.q = self.B.pack_marginals([torch.full((m,), 1.0 / m) for m, _ in shapes],
+                                               [torch.full((n,), 1.0 / n) for _, n in shapes])
+
+    def autotune(self, x, y):
+        import torch
+        from reg_drot.cost import packed_sqeuclidean_cost
+        with torch.no_grad():
+            return self.B.autotune(packed_sqeuclidean_cost(self.B, x, y, DIFF_SCALE),
+                                   self.p, self.q, iters=100)
+
+    def run(self, x, y, events=None):
+        """cost -> batched solve -> loss -> backward; x, y leaves with
+        requires_grad.  events: four CUDA events recorded around the stages.
+        Returns (loss, the solve's autograd node)."""
+        from reg_drot.autograd import batch_quadratic_drot_fn
+        from reg_drot.cost import packed_sqeuclidean_cost
+        if events:
+            events[0].record()
+        c = packed_sqeuclidean_cost(self.B, x, y, DIFF_SCALE)
+        if events:
+            events[1].record()
+        X = batch_quadratic_drot_fn(self.B, c, self.p, self.q, MAX_ITERS)
+        if events:
+            events[2].record()
+        loss = (c * X).sum() + self.w * (X * X).sum()
+        loss.backward()
+        if events:
+            events[3].record()
+        return loss.detach(), X.grad_fn
 
 
-def differentiable_point(dev, n_inst=DIFF_INSTANCES, gl_inst=4, single_sample=8, gl_iters=500):
-    """Differentiable OT loss: point clouds x_k (m x 16), y_k (n x 16) ~ N(0, 1),
-    m, n ~ U{512..4096}; C_k = |x - y|^2 / 64 on the tensor cores; loss =
-    sum_k <C_k, X_k*> + w ||X_k*||_F^2 (w fixed random); one step = cost +
-    batched QR solve (relative eps 1e-4, alpha 1e-3) + backward (implicit
-    adjoint + cost chain rule) for all instances.  GL part: the same loss with
-    the group-lasso plan (2 classes, lambda weight 1e-3) and the checkpointed
-    unrolled adjoint on the first `gl_inst` instances, `gl_iters` iterations
-    each (the GL solve does not reach the relative 1e-4 stop on these clouds
-    within 20000 iterations; the adjoint's cost is linear in the iterations)."""
+def e2e_point(step, xh, yh, steps):
+    """The headline step end to end through the public API: pinned host
+    point clouds -> H2D -> step -> D2H of dL/dx, dL/dy and the loss."""
+    import torch
+    dev = step.dev
+    xp = torch.from_numpy(xh).pin_memory()
+    yp = torch.from_numpy(yh).pin_memory()
+    gxh = torch.empty_like(xp).pin_memory()
+    gyh = torch.empty_like(yp).pin_memory()
+
+    def once():
+        x = xp.to(dev, non_blocking=True).requires_grad_(True)
+        y = yp.to(dev, non_blocking=True).requires_grad_(True)
+        loss, _ = step.run(x, y)
+        gxh.copy_(x.grad, non_blocking=True)
+        gyh.copy_(y.grad, non_blocking=True)
+        val = float(loss)  # D2H of the loss; synchronises
+        torch.cuda.synchronize(dev)
+        return val
+
+    once()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        once()
+    wall = time.perf_counter() - t0
+    return {"value": DIFF_INSTANCES * steps / wall, "unit": "solves/s",
+            "h2d_bytes_per_step": int(xp.nbytes + yp.nbytes),
+            "d2h_bytes_per_step": int(gxh.nbytes + gyh.nbytes + 4), "steps": steps}
+
+
+def plain_point(dev, shapes, xs, ys, eps, flush):
+    """The plain per-instance solver on the headline instances: each solved
+    alone with reg_drot.solve_qr (FP32, forward only), L2 flushed before
+    each; C from the tensor-core kernel (not timed)."""
     import torch
     import reg_drot
-    from reg_drot.autograd import batch_quadratic_drot_fn, group_lasso_drot_fn
-    from reg_drot.batch import QRBatch
-    from reg_drot.cost import packed_sqeuclidean_cost, sqeuclidean_cost
-    rng = np.random.default_rng(SEED + 5)
-    shapes = [(int(a), int(b)) for a, b in rng.integers(DIFF_MIN, DIFF_MAX + 1, size=(n_inst, 2))]
-    g = torch.Generator(device=dev).manual_seed(SEED + 5)
-    x_cat = torch.randn(sum(m for m, _ in shapes), DIFF_DIM, generator=g, device=dev,
-                        requires_grad=True)
-    y_cat = torch.randn(sum(n for _, n in shapes), DIFF_DIM, generator=g, device=dev,
-                        requires_grad=True)
-    w = float(torch.rand(1, generator=torch.Generator().manual_seed(SEED)).item())
-    eps = [REL_EPS * math.sqrt(1.0 / m + 1.0 / n) for m, n in shapes]
-    B = QRBatch(shapes, RHO, ALPHA, eps, device=dev)
-    p, q = B.pack_marginals([torch.full((m,), 1.0 / m) for m, _ in shapes],
-                            [torch.full((n,), 1.0 / n) for _, n in shapes])
+    from reg_drot.cost import sqeuclidean_cost
+    t_sum, iters = 0.0, []
+    sl = instance_slices(shapes)
     with torch.no_grad():
-        B.autotune(packed_sqeuclidean_cost(B, x_cat, y_cat, DIFF_SCALE), p, q, iters=100)
+        for k, (m, n) in enumerate(shapes):
+            xk = torch.from_numpy(xs[sl[k][0]]).to(dev)
+            yk = torch.from_numpy(ys[sl[k][1]]).to(dev)
+            ck = sqeuclidean_cost(xk, yk, DIFF_SCALE)
+            pk = torch.full((m,), 1.0 / m, device=dev)
+            qk = torch.full((n,), 1.0 / n, device=dev)
+            if k == 0:
+                reg_drot.solve_qr(ck, pk, qk, RHO, ALPHA, MAX_ITERS, eps[k])  # warm-up
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            _, info, _ = reg_drot.solve_qr(ck, pk, qk, RHO, ALPHA, MAX_ITERS, eps[k])
+            b.record()
+            b.synchronize()
+            t_sum += a.elapsed_time(b) / 1e3
+            iters.append(info["n_iter"])
+    return {"solves_per_s": len(shapes) / t_sum, "s_total": t_sum,
+            "n_iter_min_median_max": [int(min(iters)), float(np.median(iters)), int(max(iters))]}
 
-    def ev():
-        e = torch.cuda.Event(enable_timing=True)
-        e.record()
-        return e
 
-    def step():
-        x_cat.grad = None
-        y_cat.grad = None
-        e0 = ev()
-        c = packed_sqeuclidean_cost(B, x_cat, y_cat, DIFF_SCALE)
-        e1 = ev()
-        X = batch_quadratic_drot_fn(B, c, p, q, 10 ** 6)
-        e2 = ev()
-        loss = (c * X).sum() + w * (X * X).sum()
-        loss.backward()
-        e3 = ev()
-        e3.synchronize()
-        return (e0.elapsed_time(e1) / 1e3, e1.elapsed_time(e2) / 1e3, e2.elapsed_time(e3) / 1e3,
-                X.grad_fn, float(loss.detach()))
+def qr_3000_point(dev, flush):
+    """The dense single-instance workload: QR 3000^2, C ~ U[0,1) float32,
+    p, q ~ Dirichlet(1), alpha 1e-3, relative eps 1e-4 (X + C = 72 MB:
+    L2-resident for the whole solve)."""
+    import torch
+    import reg_drot
+    c, p, q, eps = make_problem(N, SEED)
+    cd, pd, qd = (torch.from_numpy(a).to(dev) for a in (c, p, q))
+    x, info, ws = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, 10 ** 9, eps)
+    flush.zero_()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    x, info, ws = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, 10 ** 9, eps, out=x, workspace=ws)
+    b.record()
+    b.synchronize()
+    t = a.elapsed_time(b) / 1e3
+    it = info["iters_run"]
+    nbytes = float(N) * N * (12 * ((it + 1) // 2) + 8 * (it // 2) + 12)
+    return {"solves_per_s": 1.0 / t, "n_iter": info["n_iter"],
+            "us_per_iteration": t / it * 1e6, "algorithmic_GBps": nbytes / t / 1e9,
+            "note": "X + C = 72 MB stays in the 129 MB L2 across iterations"}
 
-    step()  # warm-up
-    t_cost, t_fwd, t_bwd, fn, loss = step()
-    it = np.array([r["n_iter"] for r in fn.info])
-    total = t_cost + t_fwd + t_bwd
-    out = {"workload": (f"differentiable QR-DROT loss, {n_inst} instances, m,n ~ U{{{DIFF_MIN}..{DIFF_MAX}}}, "
-                        f"x,y ~ N(0,I_{DIFF_DIM}), C = |x-y|^2/64 (tcgen05 split-TF32 GEMM), "
-                        f"alpha={ALPHA}, relative eps {REL_EPS}, loss = sum <C,X*> + w|X*|^2"),
-           "elements": int(sum(m * n for m, n in shapes)),
-           "qr": {"s_per_step": total, "solves_with_grad_per_s": n_inst / total,
-                  "cost_s": t_cost, "forward_s": t_fwd, "backward_s": t_bwd,
-                  "converged": int(sum(r["converged"] for r in fn.info)),
-                  "n_iter_min_median_max": [int(it.min()), float(np.median(it)), int(it.max())],
-                  "cg_iters_min_median_max": [int(min(fn.cg_iters)), float(np.median(fn.cg_iters)),
-                                              int(max(fn.cg_iters))],
-                  "loss": loss}}
-    # plain per-instance FP32 solves, forward only (sample)
-    ks = list(range(0, n_inst, max(1, n_inst // single_sample)))
-    t_single = 0.0
-    with torch.no_grad():
-        for k in ks:
-            m, n = shapes[k]
-            xo = sum(a for a, _ in shapes[:k])
-            yo = sum(b for _, b in shapes[:k])
-            ck = sqeuclidean_cost(x_cat[xo:xo + m].detach(), y_cat[yo:yo + n].detach(), DIFF_SCALE)
-            pk, qk = torch.full((m,), 1.0 / m, device=dev), torch.full((n,), 1.0 / n, device=dev)
-            xk, _, ws = reg_drot.solve_qr(ck, pk, qk, RHO, ALPHA, 10 ** 6, eps[k])
-            e0 = ev()
-            reg_drot.solve_qr(ck, pk, qk, RHO, ALPHA, 10 ** 6, eps[k], out=xk, workspace=ws)
-            e1 = ev()
-            e1.synchronize()
-            t_single += e0.elapsed_time(e1) / 1e3
-    out["per_instance_forward_only_solves_per_s"] = len(ks) / t_single
-    out["per_instance_sample"] = f"{len(ks)} instances, reg_drot.solve_qr forward only"
-    # GL with the unrolled adjoint, one instance at a time
-    gl_times, gl_iters_run = [], []
+
+GL_LAST_K = 64
+
+
+def diff_gl_point(dev, shapes, xs, ys, w, eps, gl_inst=8, gl_iters=20000):
+    """The group-lasso half of the differentiable workload: 2 classes (the
+    row halves), GL weight 1e-3 in the C++ wrapper's convention (lambda =
+    r / sqrt(m / 2), core/drot_glr.hpp:385, as the domain-adaptation
+    benchmark), each solve run to its relative 1e-4 stop, backward = the
+    checkpointed unrolled adjoint of the last GL_LAST_K iterations; the first
+    gl_inst instances, one at a time."""
+    import torch
+    from reg_drot.autograd import group_lasso_drot_fn
+    from reg_drot.cost import sqeuclidean_cost
+    sl = instance_slices(shapes)
+    times, iters, conv = [], [], []
     for k in range(gl_inst):
         m, n = shapes[k]
-        xo = sum(a for a, _ in shapes[:k])
-        yo = sum(b for _, b in shapes[:k])
-        xk = x_cat[xo:xo + m].detach().clone().requires_grad_(True)
-        yk = y_cat[yo:yo + n].detach().clone().requires_grad_(True)
+        xk = torch.from_numpy(xs[sl[k][0]]).to(dev).requires_grad_(True)
+        yk = torch.from_numpy(ys[sl[k][1]]).to(dev).requires_grad_(True)
         pk, qk = torch.full((m,), 1.0 / m, device=dev), torch.full((n,), 1.0 / n, device=dev)
         for rep in range(2):
-            e0 = ev()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
             ck = sqeuclidean_cost(xk, yk, DIFF_SCALE)
-            Xk = group_lasso_drot_fn(ck, pk, qk, 2, RHO, ALPHA, gl_iters, eps[k])
+            Xk = group_lasso_drot_fn(ck, pk, qk, 2, RHO, ALPHA, gl_iters, eps[k],
+                                     convention="wrapper", last_k=GL_LAST_K)
             ((ck * Xk).sum() + w * (Xk * Xk).sum()).backward()
-            e1 = ev()
+            e1.record()
             e1.synchronize()
-        gl_times.append(e0.elapsed_time(e1) / 1e3)
-        gl_iters_run.append(Xk.grad_fn.info["n_iter"])
-    out["gl"] = {"instances": gl_inst, "s_per_instance_with_grad": statistics.mean(gl_times),
-                 "iterations": gl_iters_run, "segment": 32,
-                 "ms_per_iteration_with_grad": 1e3 * sum(gl_times) / sum(gl_iters_run)}
-    return out
+        times.append(e0.elapsed_time(e1) / 1e3)
+        iters.append(Xk.grad_fn.info["n_iter"])
+        conv.append(Xk.grad_fn.info["converged"])
+    return {"instances": gl_inst, "solves_with_grad_per_s": gl_inst / sum(times),
+            "iterations": iters, "converged": int(sum(conv)), "last_k": GL_LAST_K,
+            "lambda_convention": "wrapper"}
 
 
 def max_over_ranks(values, dist, device):
@@ -572,7 +686,6 @@ def replica_throughput(world, steps, slowest_total_s):
 
 def run_gpu(args):
     import torch
-    import reg_drot
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -584,87 +697,90 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
 
-    c, p, q, eps = make_problem(N, SEED)
-    cd = torch.from_numpy(c).to(dev)
-    pd = torch.from_numpy(p).to(dev)
-    qd = torch.from_numpy(q).to(dev)
+    shapes, xs, ys, w, eps = diff_workload()
+    step = DiffStep(dev, shapes, eps, w)
+    x = torch.from_numpy(xs).to(dev).requires_grad_(True)
+    y = torch.from_numpy(ys).to(dev).requires_grad_(True)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
-    x, info, ws = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, 10 ** 9, eps)
-    for _ in range(max(args.warmup - 1, 0)):
+    cpt = step.autotune(x, y)
+    for _ in range(args.warmup):
+        x.grad = y.grad = None
         flush.zero_()
-        x, info, ws = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, 10 ** 9, eps, out=x, workspace=ws)
+        step.run(x, y)
     torch.cuda.synchronize()
 
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    fn = None
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
-        # A short GPU-side wait ahead of the first timed step: the host
-        # enqueues every step while it runs, so a host stall cannot leave the
-        # GPU idle inside the timed events.
-        torch.cuda._sleep(100_000_000)
         for i in range(args.steps):
+            x.grad = y.grad = None
             flush.zero_()
-            starts[i].record()
-            x, _, ws = reg_drot.solve_qr(cd, pd, qd, RHO, ALPHA, 10 ** 9, eps, out=x,
-                                         workspace=ws, sync=False)
-            ends[i].record()
+            _, fn = step.run(x, y, evs[i])
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     if dist:
         dist.barrier()
-    info = reg_drot.read_result(ws)
-    step_s = [a.elapsed_time(b) / 1e3 for a, b in zip(starts, ends)]
+    step_s = [e[0].elapsed_time(e[3]) / 1e3 for e in evs]
+    solve_s = [e[1].elapsed_time(e[2]) / 1e3 for e in evs]
+    bwd_s = [e[2].elapsed_time(e[3]) / 1e3 for e in evs]
+    cost_s = [e[0].elapsed_time(e[1]) / 1e3 for e in evs]
     total = sum(step_s)
     total, wall = max_over_ranks([total, wall], dist, dev)
-    value = replica_throughput(world, args.steps, total)
+    value = replica_throughput(world, args.steps * DIFF_INSTANCES, total)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return 0
 
-    it = info["iters_run"]
-    n_even = (it + 1) // 2
-    kernel_bytes = float(N) * N * (12 * n_even + 8 * (it - n_even) + (12 if info["converged"] else 0))
-    kernel_s = total / args.steps
+    info = fn.info
+    it = np.array([r["iters_run"] for r in info])
     peak, peak_kind = measured_peak()
-    achieved = kernel_bytes / kernel_s / 1e9
-    traffic_it = profile_traffic_per_iteration()
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": traffic_it * it if traffic_it is not None else None,
-                "algorithmic_bytes_per_launch": kernel_bytes,
-                "note": ("X + C = 72 MB stays L2-resident across the iterations of a solve; "
-                         "the 10000^2 point in extra.hbm_point is the HBM-resident case")}
-
-    e2e = e2e_wrapper(c, p, q, eps, args.steps)
-    extra = {"hbm_point": hbm_point(dev, flush), "gl_da": gl_da_point(dev),
-             "gl_da_weight_5e-3": gl_da_point(dev, 5e-3), "configs": config_points(dev, flush),
-             "batched": batched_point(dev, flush), "differentiable": differentiable_point(dev)}
-    cpu = cpu_sample(budget_s=12.0) if world == 1 else None
+    kbytes = solve_bytes(shapes, info)
+    ksec = statistics.mean(solve_s)
+    ratio = profile_value("batch_solve_diff16.md", "traffic_over_algorithmic")
+    hbm = hbm_point(dev, flush)
+    roofline = {"bound": "hbm", "kernel": "batch_solve_kernel<float>",
+                "achieved": kbytes / ksec / 1e9, "peak": peak, "unit": "GB/s",
+                "frac": kbytes / ksec / 1e9 / peak, "peak_source": peak_kind,
+                "traffic": ratio * kbytes if ratio else None,
+                "algorithmic_bytes_per_launch": kbytes,
+                "traffic_basis": ("ncu DRAM bytes / algorithmic bytes of a 16-instance capture "
+                                  "of the same kernel, times this launch's algorithmic bytes"),
+                "x_update_10000": {"achieved": hbm["achieved_GBps"],
+                                   "frac": hbm["achieved_GBps"] / peak,
+                                   "us_per_iteration": hbm["us_per_iteration"]}}
+    e2e = e2e_point(step, xs, ys, min(args.steps, 5))
+    plain = plain_point(dev, shapes, xs, ys, eps, flush)
+    extra = {"qr_3000": qr_3000_point(dev, flush), "hbm_point": hbm,
+             "gl_da": gl_da_point(dev), "gl_da_weight_5e-3": gl_da_point(dev, 5e-3),
+             "configs": config_points(dev, flush), "batched_config4": batched_point(dev, flush),
+             "diff_gl": diff_gl_point(dev, shapes, xs, ys, w, eps)}
+    cpu = cpu_sample(budget_s=15.0) if world == 1 else None
+    cg = fn.cg_iters
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": kernel_s * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_rows": N, "n_cols": N, "alpha": ALPHA, "rho": RHO,
-                   "rel_eps": REL_EPS, "eps_abs": eps, "seed": SEED,
-                   "l2": "flushed (512 MB write) before every timed solve",
-                   "parallelism": f"replicas x{world}"},
-        "iterations_per_solve": it, "iterations_per_s": it / kernel_s,
-        "converged": info["converged"], "residual": info["residual"],
-        "phase_ms_per_solve_cta0": info["phase_ms"],
-        "roofline": roofline,
-        "cpu_baseline": cpu,
-        "e2e": {k: e2e[k] for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step")},
-        "e2e_detail": {"n_iter": e2e["n_iter"], "wall_s_per_step": e2e["wall_s_per_step"]},
-        "gpu_launches": 6 * args.steps,
-        "clocks": clk.summary(),
-        "wall_s_timed_region": wall,
+        "data": "synthetic (seeded N(0,1) point clouds)", "config": CONFIG,
+        "parallelism": f"replicas x{world}", "cols_per_tile": cpt,
+        "clocks": clk.summary(), "wall_s_timed_region": wall,
+        # our kernels per step: cost, batch init + solve, adjoint masks + PCG
+        "gpu_launches": 5 * args.steps,
         "extra": extra,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "roofline": roofline,
+        "stages_s_per_step": {"cost": statistics.mean(cost_s), "forward_solve": ksec,
+                              "backward": statistics.mean(bwd_s)},
+        "n_iter_min_median_max": [int(it.min()), float(np.median(it)), int(it.max())],
+        "cg_iters_min_median_max": [int(min(cg)), float(np.median(cg)), int(max(cg))],
+        "converged": int(sum(r["converged"] for r in info)),
+        "plain_per_instance": plain,
+        "batched_over_plain": value / plain["solves_per_s"],
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -673,9 +789,9 @@ def run_gpu(args):
 
 
 def run_diff_case(n_inst, iters):
-    """Profiler case: the differentiable workload's first n_inst instances,
-    one launch each of the cost kernel, the batched solve (iters iterations)
-    and the adjoint CG (--case diff:n_inst:iters)."""
+    """Profiler case: the headline workload's first n_inst instances, one
+    launch each of the cost kernel, the batched solve (iters iterations) and
+    the adjoint CG (--case diff:n_inst:iters)."""
     import warnings
     import torch
     from reg_drot.autograd import batch_quadratic_drot_fn
@@ -683,35 +799,61 @@ def run_diff_case(n_inst, iters):
     from reg_drot.cost import packed_sqeuclidean_cost
     warnings.simplefilter("ignore")
     dev = torch.device("cuda", 0)
-    rng = np.random.default_rng(SEED + 5)
-    shapes = [(int(a), int(b)) for a, b in rng.integers(DIFF_MIN, DIFF_MAX + 1, size=(n_inst, 2))]
-    g = torch.Generator(device=dev).manual_seed(SEED + 5)
-    x = torch.randn(sum(m for m, _ in shapes), DIFF_DIM, generator=g, device=dev, requires_grad=True)
-    y = torch.randn(sum(n for _, n in shapes), DIFF_DIM, generator=g, device=dev, requires_grad=True)
-    B = QRBatch(shapes, RHO, ALPHA, [REL_EPS * math.sqrt(1.0 / m + 1.0 / n) for m, n in shapes],
-                device=dev, cols_per_tile=256)
+    shapes, xs, ys, w, eps = diff_workload()
+    shapes, eps = shapes[:n_inst], eps[:n_inst]
+    sl = instance_slices(shapes)
+    x = torch.from_numpy(xs[:sl[-1][0].stop]).to(dev).requires_grad_(True)
+    y = torch.from_numpy(ys[:sl[-1][1].stop]).to(dev).requires_grad_(True)
+    B = QRBatch(shapes, RHO, ALPHA, eps, device=dev, cols_per_tile=256)
     p, q = B.pack_marginals([torch.full((m,), 1.0 / m) for m, _ in shapes],
                             [torch.full((n,), 1.0 / n) for _, n in shapes])
     c = packed_sqeuclidean_cost(B, x, y, DIFF_SCALE)
     X = batch_quadratic_drot_fn(B, c, p, q, iters)
-    ((c * X).sum() + 0.5 * (X * X).sum()).backward()
+    ((c * X).sum() + w * (X * X).sum()).backward()
     torch.cuda.synchronize()
+    # the forward launch alone, timed (inputs in HBM, all instances active)
+    with torch.no_grad():
+        xo = B.empty_x()
+        B.launch(c.detach(), p, q, xo, iters)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        B.launch(c.detach(), p, q, xo, iters)
+        b.record()
+        b.synchronize()
+    t = a.elapsed_time(b) / 1e3
+    info = B.results()
+    nbytes = solve_bytes(shapes, info)
+    peak, _ = measured_peak()
     print(json.dumps({"case": f"diff:{n_inst}:{iters}", "elements": sum(m * n for m, n in shapes),
-                      "cg_iters": X.grad_fn.cg_iters[:4]}), flush=True)
+                      "cg_iters": X.grad_fn.cg_iters[:4], "solve_s": t,
+                      "us_per_iteration": 1e6 * t / max(1, iters),
+                      "achieved_GBps": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / peak,
+                      "pf": os.environ.get("DROT_BATCH_PF", "0")}), flush=True)
     return 0
 
 
-def run_batch_timeline():
-    """Timeline of one solve of the batched workload (256 instances): CTA 0's
-    device clock at four points of every iteration (QRBatch.iteration_log),
-    summarised per iteration range as mean stage times (--case batchlog)."""
+def run_batch_timeline(workload="config4"):
+    """Timeline of one solve of a batched workload (config4: the 256-instance
+    batch; diff: the headline's 64 instances): CTA 0's device clock at four
+    points of every iteration (QRBatch.iteration_log), summarised per
+    iteration range as mean stage times (--case batchlog[:diff])."""
     import torch
     from reg_drot.batch import QRBatch
     dev = torch.device("cuda", 0)
-    shapes, costs, ps, qs, eps = make_batch_problem(dev)
-    B = QRBatch(shapes, RHO, ALPHA, eps, device=dev)
-    c = B.pack_c(costs)
-    p, q = B.pack_marginals(ps, qs)
+    if workload == "diff":
+        from reg_drot.cost import packed_sqeuclidean_cost
+        shapes, xs, ys, _, eps = diff_workload()
+        B = QRBatch(shapes, RHO, ALPHA, eps, device=dev)
+        with torch.no_grad():
+            c = packed_sqeuclidean_cost(B, torch.from_numpy(xs).to(dev),
+                                        torch.from_numpy(ys).to(dev), DIFF_SCALE)
+        p, q = B.pack_marginals([torch.full((m,), 1.0 / m) for m, _ in shapes],
+                                [torch.full((n,), 1.0 / n) for _, n in shapes])
+    else:
+        shapes, costs, ps, qs, eps = make_batch_problem(dev)
+        B = QRBatch(shapes, RHO, ALPHA, eps, device=dev)
+        c = B.pack_c(costs)
+        p, q = B.pack_marginals(ps, qs)
     cpt = B.autotune(c, p, q, iters=200)
     x = B.empty_x()
     B.launch(c, p, q, x, 10 ** 6)
@@ -745,7 +887,7 @@ def run_batch_timeline():
                      "rest_even_us": float(np.nanmean(rest[sl][ev])),
                      "rest_odd_us": float(np.nanmean(rest[sl][~ev])),
                      "seconds": float(np.nansum(total[sl]) / 1e6)})
-    print(json.dumps({"case": "batchlog", "cols_per_tile": cpt, "tiles": B.tiles(cpt),
+    print(json.dumps({"case": f"batchlog:{workload}", "cols_per_tile": cpt, "tiles": B.tiles(cpt),
                       "s_per_batch": a.elapsed_time(b) / 1e3,
                       "n_iter_max": int(it.max()), "ranges": rows}), flush=True)
     return 0
@@ -760,7 +902,7 @@ def run_case(spec):
     import reg_drot
     parts = spec.split(":")
     if parts[0] == "batchlog":
-        return run_batch_timeline()
+        return run_batch_timeline(parts[1] if len(parts) > 1 else "config4")
     if parts[0] == "diff":
         return run_diff_case(int(parts[1]), int(parts[2]))
     n, iters = int(parts[0]), int(parts[1])
@@ -787,7 +929,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--case", default=None,
                     help="n:iters[:gl][:bf16] -- one fixed-length solve; diff:n_inst:iters -- "
-                         "cost, batched solve and adjoint of the differentiable workload; "
+                         "cost, batched solve and adjoint of the headline workload; "
+                         "batchlog[:diff] -- per-iteration timeline of a batched solve; "
                          "for profiler captures")
     args = ap.parse_args()
     if args.case:

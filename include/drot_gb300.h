@@ -253,9 +253,10 @@ void drot_free_host(float *ptr);
  * is at most DROT_NOALLOC_WORKSPACE_BYTES (square problems up to about
  * 35 000); larger problems get DROT_ERR_WORKSPACE and nothing runs.  The
  * caller passes the inputs c, p, q and the output x (device pointers).
- * The first call on a device looks up that array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  All calls on a device share the one array:
+ * Every call looks up that array's device address (cudaGetSymbolAddress)
+ * with the calling thread's current device; the first call on a device also
+ * loads the library's device code there, so make that first call before any
+ * stream capture.  All calls on a device share the one array:
  * calls whose work overlaps on the GPU (other streams, other host threads)
  * race and corrupt each other; serialise them.  Each call re-initialises
  * everything it reads from the array. */
@@ -374,24 +375,26 @@ int drot_batch_state(drot_batch_plan plan, void *workspace, float **phi1,
  * positive entries of X off S that decay towards 0).
  *
  * drot_qr_adjoint_prepare builds the bit-packed support masks (and,
- * optionally, a byte mask in the layout of C for the caller's own
- * right-hand side and gradient assembly); drot_qr_adjoint_solve then solves
+ * optionally, a byte mask in the layout of C); drot_qr_adjoint_solve then
+ * forms the right-hand side from the upstream gradient and solves
  * the system of every instance with Jacobi-preconditioned conjugate
  * gradients in one persistent launch whose matvecs walk the mask bits.
  * ------------------------------------------------------------------------- */
 
 /* One instance: C is n_rows x n_cols column-major with leading dimension ld
- * at element c_offset of the C buffer; its phi1 (n_rows) and phi2 (n_cols)
- * start at phi1_offset / phi2_offset of the phi buffers; step_size is the s
- * of its solve; its right-hand side and solution [a (n_rows); b (n_cols)]
- * start at element v_offset of rhs / z. */
+ * at element c_offset of the C buffer (and of the upstream gradient and
+ * dL/dC buffers, which share its layout); its phi1 (n_rows) and phi2
+ * (n_cols) start at phi1_offset / phi2_offset of the phi buffers (and its
+ * dL/dp, dL/dq at the same offsets of grad_p / grad_q); step_size is the s
+ * of its solve and lambda = (scale - 1) / s its regularisation weight; its
+ * solution [a (n_rows); b (n_cols)] starts at element v_offset of z. */
 typedef struct {
   int n_rows, n_cols, ld, pad;
   long long c_offset, v_offset, phi1_offset, phi2_offset;
-  float step_size, pad2;
+  float step_size, lambda;
 } drot_adjoint_instance;
 
-/* Workspace of the prepare + solve pair (the same for both calls). */
+/* Workspace of the prepare + solve + grad calls (the same for all three). */
 size_t drot_qr_adjoint_workspace_bytes(int n_inst, const drot_adjoint_instance *inst);
 
 /* Support masks of every instance into the workspace; mask (may be NULL)
@@ -403,14 +406,37 @@ int drot_qr_adjoint_prepare(int n_inst, const drot_adjoint_instance *inst,
                             void *workspace, size_t workspace_bytes,
                             drot_stream_t stream);
 
-/* After drot_qr_adjoint_prepare on the same workspace and instances: solves
- * until ||r|| <= tol * ||r_0|| per instance or max_iters; writes z and, when
- * iters != NULL, the CG iterations of each instance (host array of n_inst).
- * Synchronises `stream`. */
+/* After drot_qr_adjoint_prepare on the same workspace and instances: the
+ * right-hand side [rowsum(g o M); colsum(g o M)] from the upstream gradient
+ * g = dL/dX (float, layout of C), then Jacobi-preconditioned CG in FP64
+ * until ||r|| <= tol * ||r_0|| per instance or max_iters; writes z (FP64,
+ * the [a; b] of every instance at its v_offset) and, when iters != NULL,
+ * the CG iterations of each instance (host array of n_inst).  Lines per
+ * instance: n_rows + n_cols <= 25 600.  Synchronises `stream`. */
 int drot_qr_adjoint_solve(int n_inst, const drot_adjoint_instance *inst,
-                          const float *rhs, float *z, float tol, int max_iters,
+                          const float *g, double *z, double tol, int max_iters,
                           void *workspace, size_t workspace_bytes, int *iters,
                           drot_stream_t stream);
+
+/* After drot_qr_adjoint_solve: the gradients of every instance --
+ * grad_c = (a_i + b_j - g_ij) / lambda on the support and 0 elsewhere
+ * (every element of the n_rows x n_cols block; padding rows untouched),
+ * grad_p = a + t, grad_q = b - t with t = (sum b - sum a) / (n_rows +
+ * n_cols) (the gauge sum(dL/dp) = sum(dL/dq)); FP64 arithmetic, rounded
+ * once.  Asynchronous (one kernel on `stream`). */
+int drot_qr_adjoint_grad(int n_inst, const drot_adjoint_instance *inst,
+                         const float *g, const double *z, float *grad_c,
+                         float *grad_p, float *grad_q, void *workspace,
+                         size_t workspace_bytes, drot_stream_t stream);
+
+/* After drot_qr_adjoint_solve on the same workspace and instances: the
+ * final relative residual ||r|| / ||r_0|| of each instance's CG (host array
+ * rel_residual[n_inst]; 0 for a zero right-hand side).  An instance stops
+ * the first time it is at or below tol and stays stopped.  Synchronises
+ * `stream`. */
+int drot_qr_adjoint_residuals(int n_inst, const drot_adjoint_instance *inst,
+                              const void *workspace, size_t workspace_bytes,
+                              double *rel_residual, drot_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * Unrolled adjoint of the group-lasso iteration (autograd backward)
@@ -474,6 +500,24 @@ typedef struct {
 int drot_sqeuclidean_cost(int n_inst, const drot_cost_instance *inst,
                           const float *x, const float *y, int dim, float scale,
                           int clamp, float *c, drot_stream_t stream);
+
+/* Backward of drot_sqeuclidean_cost (no counterpart in the reference): for
+ * grad_c = dL/dC of every instance (layout of C), the chain rule
+ *     grad_x_i = 2 scale (x_i sum_j G_ij - sum_j G_ij y_j)
+ *     grad_y_j = 2 scale (y_j sum_i G_ij - sum_i G_ij x_i)
+ * with G = grad_c, zeroed where c <= 0 when c != NULL (the clamp of the
+ * forward); grad_x / grad_y in the layout of x / y.  FP32 sums in a fixed
+ * order (deterministic), one pass over grad_c (and c).  workspace: the
+ * per-band partials of grad_y, drot_sqeuclidean_cost_grad_workspace_bytes.
+ * grad_c, c 16-byte aligned.  Asynchronous (two kernels on `stream`). */
+size_t drot_sqeuclidean_cost_grad_workspace_bytes(int n_inst,
+                                                  const drot_cost_instance *inst,
+                                                  int dim);
+int drot_sqeuclidean_cost_grad(int n_inst, const drot_cost_instance *inst,
+                               const float *x, const float *y, int dim,
+                               float scale, const float *c, const float *grad_c,
+                               float *grad_x, float *grad_y, void *workspace,
+                               size_t workspace_bytes, drot_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -66,6 +66,51 @@ def implicit_adjoint(M, G, lam):
     return gc, a, b
 
 
+def implicit_adjoint_sparse(M, G, lam, rtol=1e-13):
+    """implicit_adjoint for large supports: the same system, FP64, as a
+    sparse matrix solved by conjugate gradients (it is positive
+    semidefinite and the right-hand side is consistent, so CG converges to
+    a solution; the gauge a + t, b - t is fixed as in implicit_adjoint)."""
+    from scipy.sparse import bmat, coo_matrix, diags
+    from scipy.sparse.linalg import cg
+    nc, nr = M.shape
+    Mf = M.astype(np.float64)
+    j, i = np.nonzero(M)
+    off = coo_matrix((np.ones(len(i)), (i, j)), shape=(nr, nc)).tocsr()
+    A = bmat([[diags(Mf.sum(0)), off], [off.T, diags(Mf.sum(1))]], format="csr")
+    Gm = G * Mf
+    rhs = np.concatenate([Gm.sum(0), Gm.sum(1)])
+    deg = np.asarray(A.diagonal())
+    pre = diags(np.where(deg > 0, 1.0 / np.maximum(deg, 1.0), 0.0))
+    try:
+        z, info = cg(A, rhs, rtol=rtol, atol=0.0, maxiter=100000, M=pre)
+    except TypeError:  # scipy before 1.12 names the relative tolerance `tol`
+        z, info = cg(A, rhs, tol=rtol, atol=0.0, maxiter=100000, M=pre)
+    if info != 0:
+        raise RuntimeError(f"implicit_adjoint_sparse: CG did not converge ({info})")
+    a, b = z[:nr], z[nr:]
+    t = (b.sum() - a.sum()) / (nr + nc)
+    a, b = a + t, b - t
+    gc = np.where(M, (a[None, :] + b[:, None] - G) / lam, 0.0)
+    return gc, a, b
+
+
+def grads_at_state(o, c, rho, r_weight, w, sparse=True):
+    """Loss L = <C, X> + w ||X||_F^2 and its implicit gradients (dL/dC, dL/dp,
+    dL/dq), FP64, at the plan and duals of a finished solve `o` (the support
+    read off o's duals): the gradient the implicit adjoint gives for that
+    solve."""
+    X = np.asarray(o["x"], np.float64)
+    c = np.asarray(c, np.float64)
+    nc, nr = X.shape
+    lam = qr_lambda(rho, r_weight, nr, nc)
+    L = float((c * X).sum() + w * (X * X).sum())
+    G = c + 2.0 * w * X
+    M = support(o, c, O.step_size(rho, nr, nc))
+    gi, a, b = (implicit_adjoint_sparse if sparse else implicit_adjoint)(M, G, lam)
+    return L, X + gi, a, b
+
+
 def loss_and_grads(c, p, q, rho, r_weight, w, eps=1e-13):
     """L = <C, X*> + w ||X*||_F^2 and its FP64 gradients w.r.t. C, p, q."""
     o = solve64(c, p, q, rho, r_weight, eps)
@@ -93,17 +138,23 @@ def point_grads(xs, yt, gc):
     return gx, gy
 
 
-def gl_unrolled(c, p, q, n_class, rho, r_weight, iters, norm_eps=1e-9):
+def gl_unrolled(c, p, q, n_class, rho, r_weight, iters, norm_eps=1e-9, convention="torch",
+                last_k=None, c_last=None):
     """X after `iters` GL iterations from the warm start, in FP64 torch (CPU)
     so that autograd gives the exact gradient of the unrolled map.  Restates
     the oracle's GL loop (oracle_gl_solve: core/drot_glr.hpp:242-355,
     kernel_glr.hpp:59-161, 461-526) with the operator's parameters
-    (pytorch/src/glr_drot_cuda_kernel.cu:255-257).  c, p, q: torch float64
-    tensors ([n_cols, n_rows], [n_rows], [n_cols])."""
+    (pytorch/src/glr_drot_cuda_kernel.cu:255-257; convention="wrapper": the
+    C++ wrapper's threshold, core/drot_glr.hpp:385).  last_k: the first
+    iters - last_k iterations run without autograd, so the gradient is that
+    of the last last_k steps with the state before them held fixed (the
+    truncated unrolled adjoint); c_last, if given, is the cost those last
+    steps use (c the earlier ones).  c, p, q: torch float64 tensors
+    ([n_cols, n_rows], [n_rows], [n_cols])."""
     import torch
     nc, nr = c.shape
     s = O.step_size(rho, nr, nc)
-    lam = O.gl_lambda(r_weight, nr, n_class, "torch")
+    lam = O.gl_lambda(r_weight, nr, n_class, convention)
     w = O.warm_start(s, nr, nc)
     bounds = [int(v) for v in O.group_bounds(nr, n_class)]
     f64 = dict(dtype=torch.float64)
@@ -113,8 +164,12 @@ def gl_unrolled(c, p, q, n_class, rho, r_weight, iters, norm_eps=1e-9):
     a = torch.full((nr,), float(w["a"]), **f64)
     b = torch.full((nc,), float(w["b"]), **f64)
     alpha = torch.tensor(float(w["alpha"]), **f64)
-    for _ in range(iters):
-        y = (X + phi1[None, :] + phi2[:, None] - s * c).clamp_min(0.0)
+    t_free = iters - last_k if last_k is not None else 0
+    for it in range(iters):
+        if it == t_free and last_k is not None:
+            X, phi1, phi2, a, b, alpha = (v.detach() for v in (X, phi1, phi2, a, b, alpha))
+        cc = c_last if (c_last is not None and it >= t_free) else c
+        y = (X + phi1[None, :] + phi2[:, None] - s * cc).clamp_min(0.0)
         parts = []
         for g in range(n_class):
             yg = y[:, bounds[g]:bounds[g + 1]]

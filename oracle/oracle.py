@@ -173,6 +173,45 @@ def quadratic_drot(c, p, q, rho, r_weight, max_iters, eps, dtype=np.float32, thr
     return qr_solve(c, p, q, s, kappa, max_iters, eps, dtype=dtype, threads=threads)
 
 
+def qr_solve_stopped_at(c, p, q, s, kappa, n_iter, dtype=np.float32, threads=None):
+    """The QR loop as though its stop test had passed at iteration n_iter - 1.
+
+    The reference tests even iterations only and reports the last index + 1
+    (core/drot_qr.hpp:200-233), so n_iter - 1 must be even.  The loop runs
+    iterations 0 .. n_iter - 1 with the test disabled, then applies fix_x
+    (kernel_qr.hpp:469-482: X <- max(X + sC, 0), one rounding of s*C + X):
+    the state, objective and residual the reference returns when its test
+    passes there.  A solve whose stop moved by one check (a tie at the
+    threshold between two summation orders) is compared with this."""
+    k = int(n_iter) - 1
+    if k < 0 or k % 2:
+        raise ValueError("n_iter - 1 must be a non-negative even iteration index")
+    st = qr_solve(c, p, q, s, kappa, k + 1, -1.0, dtype=dtype, threads=threads)
+    dt = np.dtype(dtype)
+    sv = float(np.asarray(s, dtype=dt))
+    x = st["x"].astype(np.float64) + sv * np.asarray(c, dtype=dt).astype(np.float64)
+    st["x"] = np.maximum(x, 0.0).astype(dt)
+    st["n_iter"] = int(n_iter)
+    return st
+
+
+def quadratic_drot_at(c, p, q, rho, r_weight, n_iter, dtype=np.float32, threads=None):
+    """quadratic_drot stopped (converged) at the reference count n_iter."""
+    nc, nr = c.shape
+    s = step_size(rho, nr, nc)
+    kappa = qr_scale(s, r_weight, nr, nc, "torch")
+    return qr_solve_stopped_at(c, p, q, s, kappa, n_iter, dtype=dtype, threads=threads)
+
+
+def quadratic_drot_matching(n_iter, o, c, p, q, rho, r_weight, dtype=np.float32, threads=None):
+    """The oracle solve `o` when it stopped at n_iter, else the oracle
+    stopped at n_iter (quadratic_drot_at): the reference result to compare a
+    converged solve that reported n_iter with."""
+    if o["n_iter"] == n_iter:
+        return o
+    return quadratic_drot_at(c, p, q, rho, r_weight, n_iter, dtype=dtype, threads=threads)
+
+
 def group_lasso_drot(c, p, q, n_class, rho, r_weight, max_iters, eps, dtype=np.float32,
                      threads=None):
     """Oracle of reg_drot.group_lasso_drot (pytorch/src/glr_drot_cuda_kernel.cu:299-381)."""

@@ -23,7 +23,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 OUT = os.path.join(PKG, "reg_drot", "libdrot_gb300.so")
 SOURCES = [os.path.join(CSRC, f)
-           for f in ("drot_api.cu", "drot_solve_ldu.cu", "drot_batch.cu", "drot_adjoint.cu",
+           for f in ("drot_api.cu", "drot_batch.cu", "drot_adjoint.cu",
                      "drot_gl_adjoint.cu", "drot_cost.cu")]
 DEPS = SOURCES + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))] + \
     [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]

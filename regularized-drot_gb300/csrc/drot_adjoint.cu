@@ -58,6 +58,7 @@ struct AdjInst {
   int seg0, nseg;    // its segments (contiguous)
   int owner;         // CTA that counts its convergence
   float s;           // step size of the solve
+  float lam;         // regularisation weight lambda = (kappa - 1) / s
 };
 
 struct AdjSeg {
@@ -69,9 +70,9 @@ struct AdjParams {
   int c_bf16;
   const float *phi1, *phi2;
   unsigned char* mask;  // byte mask, layout of C (may be null)
-  const float* rhs;
-  float* z;  // solution [a; b]
-  float *r, *d0, *d1, *q, *invdiag, *deg;
+  const float* g;       // upstream gradient dL/dX, layout of C
+  double* z;            // solution [a; b]
+  double *r, *d0, *d1, *q, *invdiag, *deg;
   unsigned *mcol, *mrow;
   const AdjInst* inst;
   const AdjSeg* seg;
@@ -82,12 +83,13 @@ struct AdjParams {
   double* slot_rr0;     // per segment: initial r.r
   int* iters;           // per instance: CG iterations run
   int* conv;            // per instance: converged flag (owner CTA only)
+  double* relres;       // per instance: final relative residual ||r|| / ||r0||
   unsigned* conv_count;
   unsigned* bar;
   int* abort_flag;
   long long timeout_ns;
   int n_inst, n_seg, max_iters;
-  float tol;
+  double tol;
 };
 
 // ---------------------------------------------------------------------------
@@ -130,7 +132,7 @@ __global__ void adj_mask_kernel(const AdjParams A) {
 }
 
 // ---------------------------------------------------------------------------
-// batched PCG
+// batched PCG (FP64 vectors)
 // ---------------------------------------------------------------------------
 
 // Lines per warp step and 32-word blocks per line held in registers: a
@@ -143,10 +145,10 @@ constexpr int kAdjWords = 4;
 // (rows sum the column half, columns the row half); lanes split the words,
 // bits are walked in order, then a shuffle tree.  Deterministic.
 __device__ __forceinline__ void lines_dot(const AdjParams& A, const AdjInst& I, int l0, int l1,
-                                          const float* sv, int lane, float (&out)[kAdjLines]) {
-  float s[kAdjLines];
+                                          const double* sv, int lane, double (&out)[kAdjLines]) {
+  double s[kAdjLines];
 #pragma unroll
-  for (int u = 0; u < kAdjLines; ++u) s[u] = 0.0f;
+  for (int u = 0; u < kAdjLines; ++u) s[u] = 0.0;
   const int nwmax = max(I.nwr, I.nwc);
   for (int w0 = 0; w0 < nwmax; w0 += 32 * kAdjWords) {
     unsigned wd[kAdjLines][kAdjWords];
@@ -165,11 +167,11 @@ __device__ __forceinline__ void lines_dot(const AdjParams& A, const AdjInst& I, 
     }
 #pragma unroll
     for (int u = 0; u < kAdjLines; ++u) {
-      const float* base = (l0 + u < I.nr) ? sv + I.nr : sv;
+      const double* base = (l0 + u < I.nr) ? sv + I.nr : sv;
 #pragma unroll
       for (int kk = 0; kk < kAdjWords; ++kk) {
         unsigned m = wd[u][kk];
-        const float* b0 = base + (w0 + kk * 32 + lane) * 32;
+        const double* b0 = base + (w0 + kk * 32 + lane) * 32;
         while (m) {
           const int b = __ffs(m) - 1;
           s[u] += b0[b];
@@ -179,15 +181,47 @@ __device__ __forceinline__ void lines_dot(const AdjParams& A, const AdjInst& I, 
     }
   }
 #pragma unroll
-  for (int u = 0; u < kAdjLines; ++u) out[u] = warp_sum(s[u]);
+  for (int u = 0; u < kAdjLines; ++u) out[u] = warp_sum_d(s[u]);
 }
 
-__device__ __forceinline__ int popc_line(const unsigned* words, int nw, int lane) {
+// Degree of line l and the right-hand side entry of the adjoint system: the
+// sum of the upstream gradient g over the line's support (rowsum(g o M) for
+// a row, colsum(g o M) for a column), in FP64.  Lanes split the mask words;
+// fixed shuffle trees, so the result is deterministic.
+__device__ __forceinline__ void line_degree_rhs(const AdjParams& A, const AdjInst& I, int l,
+                                                int lane, int& deg, double& rhs) {
   int c = 0;
-  for (int w = lane; w < nw; w += 32) c += __popc(__ldcg(words + w));
+  double s = 0.0;
+  const float* g = A.g + I.c_off;
+  if (l < I.nr) {  // row i = l: set bits are columns j, g at j * ld + i (strided gather)
+    const unsigned* words = A.mrow + I.mr_off + (long long)l * I.nwc;
+    for (int w = lane; w < I.nwc; w += 32) {
+      unsigned m = __ldcg(words + w);
+      c += __popc(m);
+      while (m) {
+        const int j = 32 * w + __ffs(m) - 1;
+        s += (double)__ldg(g + (long long)j * I.ld + l);
+        m &= m - 1u;
+      }
+    }
+  } else {  // column j = l - nr: set bits are rows i, g contiguous down the column
+    const int j = l - I.nr;
+    const unsigned* words = A.mcol + I.mc_off + (long long)j * I.nwr;
+    const float* gc = g + (long long)j * I.ld;
+    for (int w = lane; w < I.nwr; w += 32) {
+      unsigned m = __ldcg(words + w);
+      c += __popc(m);
+      while (m) {
+        const int i = 32 * w + __ffs(m) - 1;
+        s += (double)__ldg(gc + i);
+        m &= m - 1u;
+      }
+    }
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-  return c;
+  deg = c;
+  rhs = warp_sum_d(s);
 }
 
 // Sum over the segments of an instance of slot[] (fixed order).
@@ -197,34 +231,40 @@ __device__ __forceinline__ double inst_sum(const double* slot, const AdjInst& I)
   return s;
 }
 
+// Vectors (r, d, q, z) and the staged direction are FP64: the adjoint system
+// is a graph Laplacian whose support graph is often close to a forest (as
+// many edges as vertices), so it is badly conditioned, and an FP32 CG stops
+// at a solution error far above its residual.  The FP64 work is one add per
+// set mask bit and O(lines) vector updates -- small beside the mask traffic.
 __global__ void __launch_bounds__(256, 2) adj_pcg_kernel(const AdjParams A) {
-  extern __shared__ __align__(16) float sv[];  // the staged direction of one instance
+  extern __shared__ __align__(16) double sv[];  // the staged direction of one instance
   __shared__ int s_flag;
   __shared__ double s_red[32 + 1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
   const int sg0 = A.cta_seg0[blockIdx.x], sg1 = A.cta_seg0[blockIdx.x + 1];
-  const double tol2 = (double)A.tol * (double)A.tol;
+  const double tol2 = A.tol * A.tol;
   unsigned epoch = 0;
 
-  // Prologue: degrees, r = rhs, z = 0; parity-0 slots r.y and r.r.
+  // Prologue: degrees, the right-hand side from g, r = rhs, z = 0; parity-0
+  // slots r.y and r.r.
   for (int sg = sg0; sg < sg1; ++sg) {
     const AdjSeg S = A.seg[sg];
     const AdjInst I = A.inst[S.inst];
     double ry = 0.0, rr = 0.0;
     for (int l = S.l0 + warp; l < S.l1; l += W) {
       int dg;
-      if (l < I.nr) dg = popc_line(A.mrow + I.mr_off + (long long)l * I.nwc, I.nwc, lane);
-      else dg = popc_line(A.mcol + I.mc_off + (long long)(l - I.nr) * I.nwr, I.nwr, lane);
+      double rhs;
+      line_degree_rhs(A, I, l, lane, dg, rhs);
       if (lane == 0) {
-        const int g = I.v_off + l;
-        const float inv = dg > 0 ? 1.0f / (float)dg : 0.0f;
-        const float r0 = dg > 0 ? A.rhs[g] : 0.0f;  // a line off the support has rhs 0
-        A.invdiag[g] = inv;
-        A.deg[g] = (float)dg;
-        A.r[g] = r0;
-        A.z[g] = 0.0f;
-        ry += (double)r0 * (double)(inv * r0);
-        rr += (double)r0 * (double)r0;
+        const int gi = I.v_off + l;
+        const double inv = dg > 0 ? 1.0 / (double)dg : 0.0;
+        const double r0 = dg > 0 ? rhs : 0.0;
+        A.invdiag[gi] = inv;
+        A.deg[gi] = (double)dg;
+        A.r[gi] = r0;
+        A.z[gi] = 0.0;
+        ry += r0 * (inv * r0);
+        rr += r0 * r0;
       }
     }
     ry = block_sum_d(ry, s_red);
@@ -237,10 +277,11 @@ __global__ void __launch_bounds__(256, 2) adj_pcg_kernel(const AdjParams A) {
   }
   if (!grid_barrier(A.bar, A.abort_flag, A.timeout_ns, epoch, &s_flag)) return;
 
-  for (int it = 0; it < A.max_iters; ++it) {
+  int it = 0;
+  for (; it < A.max_iters; ++it) {
     const int par = it & 1;
-    float* dcur = par ? A.d1 : A.d0;
-    const float* dold = par ? A.d0 : A.d1;
+    double* dcur = par ? A.d1 : A.d0;
+    const double* dold = par ? A.d0 : A.d1;
     const double* ry_cur = A.slot_ry + (size_t)par * A.n_seg;
     const double* ry_prev = A.slot_ry + (size_t)(par ^ 1) * A.n_seg;
     const double* rr_cur = A.slot_rr + (size_t)par * A.n_seg;
@@ -258,27 +299,27 @@ __global__ void __launch_bounds__(256, 2) adj_pcg_kernel(const AdjParams A) {
         }
         continue;
       }
-      const float beta = it == 0 ? 0.0f : (float)(inst_sum(ry_cur, I) / inst_sum(ry_prev, I));
+      const double beta = it == 0 ? 0.0 : inst_sum(ry_cur, I) / inst_sum(ry_prev, I);
       const int nv = I.nr + I.nc;
       __syncthreads();
       // Stage d = M^-1 r + beta d_old for the whole instance: a thread takes
       // 4 entries and issues their 12 loads before using any.
       for (int t0 = threadIdx.x; t0 < nv; t0 += 4 * blockDim.x) {
-        float iv[4], rv[4], dv0[4];
+        double iv[4], rv[4], dv0[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const int t = t0 + u * blockDim.x;
-          const int g = I.v_off + (t < nv ? t : 0);
-          iv[u] = __ldcg(A.invdiag + g);
-          rv[u] = __ldcg(A.r + g);
-          dv0[u] = it == 0 ? 0.0f : __ldcg(dold + g);
+          const int gi = I.v_off + (t < nv ? t : 0);
+          iv[u] = __ldcg(A.invdiag + gi);
+          rv[u] = __ldcg(A.r + gi);
+          dv0[u] = it == 0 ? 0.0 : __ldcg(dold + gi);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
           const int t = t0 + u * blockDim.x;
           if (t >= nv) break;
-          const float y = iv[u] * rv[u];
-          const float dv = it == 0 ? y : fmaf(beta, dv0[u], y);
+          const double y = iv[u] * rv[u];
+          const double dv = it == 0 ? y : fma(beta, dv0[u], y);
           sv[t] = dv;
           if (t >= S.l0 && t < S.l1) dcur[I.v_off + t] = dv;
         }
@@ -286,18 +327,18 @@ __global__ void __launch_bounds__(256, 2) adj_pcg_kernel(const AdjParams A) {
       __syncthreads();
       double dq = 0.0;
       for (int l0 = S.l0 + warp * kAdjLines; l0 < S.l1; l0 += W * kAdjLines) {
-        float s[kAdjLines];
+        double s[kAdjLines];
         lines_dot(A, I, l0, S.l1, sv, lane, s);
         if (lane == 0) {
 #pragma unroll
           for (int u = 0; u < kAdjLines; ++u) {
             const int l = l0 + u;
             if (l < S.l1) {
-              const int g = I.v_off + l;
-              const float dl = sv[l];
-              const float qv = fmaf(__ldcg(A.deg + g), dl, s[u]);
-              A.q[g] = qv;
-              dq += (double)dl * (double)qv;
+              const int gi = I.v_off + l;
+              const double dl = sv[l];
+              const double qv = fma(__ldcg(A.deg + gi), dl, s[u]);
+              A.q[gi] = qv;
+              dq += dl * qv;
             }
           }
         }
@@ -314,19 +355,30 @@ __global__ void __launch_bounds__(256, 2) adj_pcg_kernel(const AdjParams A) {
     for (int sg = sg0; sg < sg1; ++sg) {
       const AdjSeg S = A.seg[sg];
       const AdjInst I = A.inst[S.inst];
-      if (!(inst_sum(rr_cur, I) > tol2 * inst_sum(A.slot_rr0, I))) continue;
+      if (!(inst_sum(rr_cur, I) > tol2 * inst_sum(A.slot_rr0, I))) {
+        // Converged: carry this segment's r.y and r.r into the next parity's
+        // slots, so the instance reads the same (converged) sums on every
+        // later iteration and stays stopped.  Without the copy the next
+        // iteration would read the slots of two iterations back, find the
+        // instance unconverged and step it again with stale CG scalars.
+        if (threadIdx.x == 0) {
+          ry_next[sg] = __ldcg(ry_cur + sg);
+          rr_next[sg] = __ldcg(rr_cur + sg);
+        }
+        continue;
+      }
       const double dq = inst_sum(A.slot_dq, I);
-      const float alpha = dq > 0.0 ? (float)(inst_sum(ry_cur, I) / dq) : 0.0f;
+      const double alpha = dq > 0.0 ? inst_sum(ry_cur, I) / dq : 0.0;
       double ry = 0.0, rr = 0.0;
       for (int l = S.l0 + threadIdx.x; l < S.l1; l += blockDim.x) {
-        const int g = I.v_off + l;
-        const float zl = fmaf(alpha, __ldcg(dcur + g), A.z[g]);
-        const float rl = fmaf(-alpha, __ldcg(A.q + g), A.r[g]);
-        A.z[g] = zl;
-        A.r[g] = rl;
-        const float yl = __ldcg(A.invdiag + g) * rl;
-        ry += (double)rl * (double)yl;
-        rr += (double)rl * (double)rl;
+        const int gi = I.v_off + l;
+        const double zl = fma(alpha, __ldcg(dcur + gi), A.z[gi]);
+        const double rl = fma(-alpha, __ldcg(A.q + gi), A.r[gi]);
+        A.z[gi] = zl;
+        A.r[gi] = rl;
+        const double yl = __ldcg(A.invdiag + gi) * rl;
+        ry += rl * yl;
+        rr += rl * rl;
       }
       ry = block_sum_d(ry, s_red);
       rr = block_sum_d(rr, s_red);
@@ -337,6 +389,77 @@ __global__ void __launch_bounds__(256, 2) adj_pcg_kernel(const AdjParams A) {
       }
     }
     if (!grid_barrier(A.bar, A.abort_flag, A.timeout_ns, epoch, &s_flag)) return;
+  }
+  // Final relative residual of each instance, from the slots of the parity
+  // the last phase A read (written, and made visible by a grid barrier,
+  // before the loop ended); the CTA of the instance's first segment writes it.
+  const double* rr_fin = A.slot_rr + (size_t)(it & 1) * A.n_seg;
+  for (int sg = sg0; sg < sg1; ++sg) {
+    const AdjSeg S = A.seg[sg];
+    const AdjInst I = A.inst[S.inst];
+    if (sg == I.seg0 && threadIdx.x == 0) {
+      const double r0 = inst_sum(A.slot_rr0, I);
+      A.relres[S.inst] = r0 > 0.0 ? sqrt(inst_sum(rr_fin, I) / r0) : 0.0;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// gradient assembly
+// ---------------------------------------------------------------------------
+
+// dL/dC = (a_i + b_j - g_ij) / lambda on the support, 0 elsewhere (FP64
+// arithmetic on the support entries, rounded once), for every element of an
+// instance's n_rows x n_cols block; grid (column blocks, instances), a warp
+// per column, a lane per 4 rows (one 128-row chunk per step).  Off-support
+// groups of 4 rows are written as zeros without reading g.  Block 0 of each
+// instance also writes dL/dp = a + t, dL/dq = b - t with the gauge t =
+// (sum b - sum a) / (n_rows + n_cols) (FP64 sums in a fixed order).
+__global__ void __launch_bounds__(256) adj_grad_kernel(const AdjParams A, float* __restrict__ gc,
+                                                       float* __restrict__ gp,
+                                                       float* __restrict__ gq) {
+  __shared__ double s_red[32 + 1];
+  const int k = blockIdx.y;
+  const AdjInst I = A.inst[k];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+  const double* za = A.z + I.v_off;
+  const double* zb = za + I.nr;
+  const double inv_lam = 1.0 / (double)I.lam;
+  for (int j = blockIdx.x * W + warp; j < I.nc; j += gridDim.x * W) {
+    const unsigned* words = A.mcol + I.mc_off + (long long)j * I.nwr;
+    const float* gcol = A.g + I.c_off + (long long)j * I.ld;
+    float* ocol = gc + I.c_off + (long long)j * I.ld;
+    const double bj = __ldcg(zb + j);
+    for (int i0 = 0; i0 < I.nr; i0 += 128) {
+      const int i = i0 + 4 * lane;
+      if (i >= I.nr) continue;
+      const unsigned wd = __ldcg(words + (i >> 5));
+      const unsigned m4 = (wd >> (i & 31)) & 0xfu;
+      float o[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      if (m4) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (((m4 >> e) & 1u) && i + e < I.nr)
+            o[e] = (float)(((__ldcg(za + i + e) + bj) - (double)__ldg(gcol + i + e)) * inv_lam);
+      }
+      if (i + 4 <= I.nr && (((I.c_off + (long long)j * I.ld + i) & 3) == 0)) {
+        *reinterpret_cast<float4*>(ocol + i) = make_float4(o[0], o[1], o[2], o[3]);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          if (i + e < I.nr) ocol[i + e] = o[e];
+      }
+    }
+  }
+  if (blockIdx.x == 0) {
+    double sa = 0.0, sb = 0.0;
+    for (int i = threadIdx.x; i < I.nr; i += blockDim.x) sa += __ldcg(za + i);
+    for (int j = threadIdx.x; j < I.nc; j += blockDim.x) sb += __ldcg(zb + j);
+    sa = block_sum_d(sa, s_red);
+    sb = block_sum_d(sb, s_red);
+    const double t = (sb - sa) / (double)(I.nr + I.nc);
+    for (int i = threadIdx.x; i < I.nr; i += blockDim.x) gp[I.f1_off + i] = (float)(za[i] + t);
+    for (int j = threadIdx.x; j < I.nc; j += blockDim.x) gq[I.f2_off + j] = (float)(zb[j] - t);
   }
 }
 
@@ -358,7 +481,7 @@ struct AdjLayout {
   std::vector<int> cta_seg0;
   long long mcol_words = 0, mrow_words = 0;
   size_t off_ctrl = 0, off_inst = 0, off_seg = 0, off_cta = 0, off_mcol = 0, off_mrow = 0,
-         off_vec = 0, off_slots = 0, off_iters = 0, off_conv = 0, total = 0;
+         off_vec = 0, off_slots = 0, off_iters = 0, off_conv = 0, off_relres = 0, total = 0;
 };
 
 size_t al256(size_t v) { return (v + 255) / 256 * 256; }
@@ -372,6 +495,7 @@ int adj_layout(int n_inst, const drot_adjoint_instance* d, AdjLayout& L) {
     const drot_adjoint_instance& a = d[k];
     if (a.n_rows <= 0 || a.n_cols <= 0 || a.ld < a.n_rows || a.c_offset < 0 ||
         a.v_offset < 0 || a.phi1_offset < 0 || a.phi2_offset < 0 || !(a.step_size > 0.0f) ||
+        !(a.lambda > 0.0f) ||
         (long long)a.n_rows + a.n_cols > (1 << 24))
       return DROT_ERR_INVALID_ARG;
     AdjInst& I = L.inst[k];
@@ -385,6 +509,7 @@ int adj_layout(int n_inst, const drot_adjoint_instance* d, AdjLayout& L) {
     I.f1_off = a.phi1_offset;
     I.f2_off = a.phi2_offset;
     I.s = a.step_size;
+    I.lam = a.lambda;
     I.v_off = (int)a.v_offset;
     I.mc_off = mc;
     I.mr_off = mr;
@@ -398,7 +523,7 @@ int adj_layout(int n_inst, const drot_adjoint_instance* d, AdjLayout& L) {
   L.V = (int)V;
   L.mcol_words = mc;
   L.mrow_words = mr;
-  L.smem = sizeof(float) * (size_t)maxv;
+  L.smem = sizeof(double) * (size_t)maxv;
   if (L.smem > 200 * 1024) return DROT_ERR_UNSUPPORTED;
 
   int dev = 0, sms = 0, coop = 0, occ = 0;
@@ -458,10 +583,11 @@ int adj_layout(int n_inst, const drot_adjoint_instance* d, AdjLayout& L) {
   L.off_cta = off;   off = al256(off + sizeof(int) * (L.grid + 1));
   L.off_mcol = off;  off = al256(off + sizeof(unsigned) * (size_t)mc);
   L.off_mrow = off;  off = al256(off + sizeof(unsigned) * (size_t)mr);
-  L.off_vec = off;   off = al256(off + sizeof(float) * (size_t)V * 6);
+  L.off_vec = off;   off = al256(off + sizeof(double) * (size_t)V * 6);
   L.off_slots = off; off = al256(off + sizeof(double) * (size_t)L.n_seg * 6);
   L.off_iters = off; off = al256(off + sizeof(int) * n_inst);
   L.off_conv = off;  off = al256(off + sizeof(int) * n_inst);
+  L.off_relres = off; off = al256(off + sizeof(double) * n_inst);
   L.total = off;
   return DROT_OK;
 }
@@ -471,7 +597,7 @@ int adj_layout(int n_inst, const drot_adjoint_instance* d, AdjLayout& L) {
 // Device pointers of a workspace laid out by L.
 static void adj_params(const AdjLayout& L, char* ws, AdjParams& A) {
   memset(&A, 0, sizeof(A));
-  float* vec = (float*)(ws + L.off_vec);
+  double* vec = (double*)(ws + L.off_vec);
   A.r = vec;
   A.d0 = vec + (size_t)L.V;
   A.d1 = vec + 2 * (size_t)L.V;
@@ -490,6 +616,7 @@ static void adj_params(const AdjLayout& L, char* ws, AdjParams& A) {
   A.slot_rr0 = slots + 5 * (size_t)L.n_seg;
   A.iters = (int*)(ws + L.off_iters);
   A.conv = (int*)(ws + L.off_conv);
+  A.relres = (double*)(ws + L.off_relres);
   A.bar = (unsigned*)(ws + L.off_ctrl);
   A.abort_flag = (int*)(ws + L.off_ctrl + 64);
   A.conv_count = (unsigned*)(ws + L.off_ctrl + 128);
@@ -543,10 +670,10 @@ int drot_qr_adjoint_prepare(int n_inst, const drot_adjoint_instance* inst, const
   return cudaStreamSynchronize(st) == cudaSuccess ? DROT_OK : DROT_ERR_CUDA;
 }
 
-int drot_qr_adjoint_solve(int n_inst, const drot_adjoint_instance* inst, const float* rhs,
-                          float* z, float tol, int max_iters, void* workspace,
+int drot_qr_adjoint_solve(int n_inst, const drot_adjoint_instance* inst, const float* g,
+                          double* z, double tol, int max_iters, void* workspace,
                           size_t workspace_bytes, int* iters, drot_stream_t stream) {
-  if (!rhs || !z || !workspace || max_iters < 0 || !(tol >= 0.0f)) return DROT_ERR_INVALID_ARG;
+  if (!g || !z || !workspace || max_iters < 0 || !(tol >= 0.0)) return DROT_ERR_INVALID_ARG;
   AdjLayout L;
   int rc = adj_layout(n_inst, inst, L);
   if (rc != DROT_OK) return rc;
@@ -555,7 +682,7 @@ int drot_qr_adjoint_solve(int n_inst, const drot_adjoint_instance* inst, const f
   cudaStream_t st = (cudaStream_t)stream;
   AdjParams A;
   adj_params(L, ws, A);
-  A.rhs = rhs;
+  A.g = g;
   A.z = z;
   A.n_inst = n_inst;
   A.max_iters = max_iters;
@@ -577,6 +704,43 @@ int drot_qr_adjoint_solve(int n_inst, const drot_adjoint_instance* inst, const f
       cudaStreamSynchronize(st) != cudaSuccess)
     return DROT_ERR_CUDA;
   return abort_flag ? DROT_ERR_BARRIER_TIMEOUT : DROT_OK;
+}
+
+int drot_qr_adjoint_grad(int n_inst, const drot_adjoint_instance* inst, const float* g,
+                         const double* z, float* grad_c, float* grad_p, float* grad_q,
+                         void* workspace, size_t workspace_bytes, drot_stream_t stream) {
+  if (!g || !z || !grad_c || !grad_p || !grad_q || !workspace) return DROT_ERR_INVALID_ARG;
+  AdjLayout L;
+  int rc = adj_layout(n_inst, inst, L);
+  if (rc != DROT_OK) return rc;
+  if (workspace_bytes < L.total || ((uintptr_t)workspace & 255u)) return DROT_ERR_WORKSPACE;
+  AdjParams A;
+  adj_params(L, (char*)workspace, A);
+  A.g = g;
+  A.z = const_cast<double*>(z);
+  A.n_inst = n_inst;
+  int maxc = 1;
+  for (const AdjInst& I : L.inst) maxc = std::max(maxc, I.nc);
+  const int blocks = std::min((maxc + 7) / 8, 1024);
+  adj_grad_kernel<<<dim3(blocks, n_inst), 256, 0, (cudaStream_t)stream>>>(A, grad_c, grad_p,
+                                                                        grad_q);
+  return cudaGetLastError() == cudaSuccess ? DROT_OK : DROT_ERR_CUDA;
+}
+
+int drot_qr_adjoint_residuals(int n_inst, const drot_adjoint_instance* inst,
+                              const void* workspace, size_t workspace_bytes, double* rel_residual,
+                              drot_stream_t stream) {
+  if (!workspace || !rel_residual) return DROT_ERR_INVALID_ARG;
+  AdjLayout L;
+  int rc = adj_layout(n_inst, inst, L);
+  if (rc != DROT_OK) return rc;
+  if (workspace_bytes < L.total || ((uintptr_t)workspace & 255u)) return DROT_ERR_WORKSPACE;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(rel_residual, (const char*)workspace + L.off_relres,
+                      sizeof(double) * n_inst, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return DROT_ERR_CUDA;
+  return DROT_OK;
 }
 
 }  // extern "C"

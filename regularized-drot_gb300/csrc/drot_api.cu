@@ -57,17 +57,9 @@ static SolveFn kernel_kv(int vec, int kv) {
   return nullptr;
 }
 
-// Single-barrier (LDU) instances, in drot_solve_ldu.cu.
-SolveFn solve_kernel_ldu(int mode, int kv, bool bf16);
-
 // Kernel instance for (mode, vector width, vectors per lane, data path, cost
 // type).  The TMA ring exists for float costs only.
-static SolveFn kernel_for(int mode, int vec, int kv, bool tma, int ctype = DROT_C_F32,
-                          bool ldu = false) {
-  if (ldu) {
-    if (tma || vec != 4) return nullptr;
-    return solve_kernel_ldu(mode, kv, ctype == DROT_C_BF16);
-  }
+static SolveFn kernel_for(int mode, int vec, int kv, bool tma, int ctype = DROT_C_F32) {
   if (ctype == DROT_C_BF16) {
     if (tma) return nullptr;
     return mode == MODE_QR ? kernel_kv<MODE_QR, false, __nv_bfloat16>(vec, kv)
@@ -114,18 +106,14 @@ static inline size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAl
 //   rowpart      P * nr floats
 //   colpart      nsb * nc floats
 //   cta_sum/obj/res  grid float pairs (8 bytes) each
-//   LDU plans add: rowpart, colpart, cta_sum, cta_obj for odd iterations,
-//                  and grid residual flags (uint32)
 struct Plan {
   int mode = 0, vec = 4, kv = 4, wt = 1, threads = 256, nbands = 1, P = 1, grid = 1, nsb = 1;
   int band_h = 0, ns = 1, p2_smem = 0, p2_cap_r = 0, p2_cap_c = 0, ctype = DROT_C_F32;
   bool tma = false;
-  bool ldu = false;  // single-barrier kernels (second partial buffers, residual flags)
   size_t smem = 0;
   std::vector<int> bounds;
   size_t off_stats = 0, off_ctrl = 256, off_rowpart = 0, off_colpart = 0, off_sum = 0,
          off_obj = 0, off_res = 0, total = 0;
-  size_t off_rowpart1 = 0, off_colpart1 = 0, off_sum1 = 0, off_obj1 = 0, off_flag = 0;
 };
 
 struct DeviceInfo {
@@ -183,10 +171,9 @@ static int reg_warps() {
 // Build the launch plan for one data path (tma: shared-memory TMA ring, else
 // register loads).  Returns a drot_status.
 static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma, int ctype,
-                              Plan& pl, const int* ubounds, bool ldu = false) {
+                              Plan& pl, const int* ubounds) {
   if (nr <= 0 || nc <= 0) return DROT_ERR_INVALID_ARG;
   if (tma && vec != 4) return DROT_ERR_UNSUPPORTED;
-  if (ldu && (tma || vec != 4)) return DROT_ERR_UNSUPPORTED;
   const DeviceInfo dev = device_info();
   if (!dev.ok) return DROT_ERR_CUDA;
   pl = Plan();
@@ -242,10 +229,9 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
     }
   }
   const int S = SV * pl.kv;
-  SolveFn fn = kernel_for(mode, vec, pl.kv, tma, ctype, ldu);
+  SolveFn fn = kernel_for(mode, vec, pl.kv, tma, ctype);
   if (!fn) return DROT_ERR_UNSUPPORTED;
   pl.ctype = ctype;
-  pl.ldu = ldu;
   // TMA ring: DROT_TMA_CTAS (1 or 2) CTAs per SM share the shared memory.
   const int tma_ctas = tma ? std::max(1, std::min(2, getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1)) : 1;
   const size_t budget = (size_t)std::max(dev.smem_optin, 48 * 1024) / tma_ctas - 1024;
@@ -310,46 +296,25 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
   }
   if (pl.grid <= 0 || pl.nbands <= 0) return DROT_ERR_UNSUPPORTED;
 
-  if (ldu) {
-    // The band rows' p, a and the chunk columns' q, b, phi2 live in shared
-    // memory (the layout's p2 slices, sized to the band cover and the widest
-    // chunk); the plan fails when that does not fit with the same occupancy.
-    if (pl.wt != 1) return DROT_ERR_UNSUPPORTED;
-    const int capr = pl.wt * S;
-    const int capc = ((nc + pl.P - 1) / pl.P + 3) & ~3;
-    const int p2f = 3 * (capr + capc);
-    const size_t smem2 = solve_smem_bytes(pl.threads / 32, pl.wt, S, pl.ns, false, p2f);
-    if (smem2 > budget) return DROT_ERR_UNSUPPORTED;
-    if (smem2 > 48 * 1024 &&
-        cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem2) != cudaSuccess)
-      return DROT_ERR_CUDA;
-    if (occupancy(fn, pl.threads, smem2) * dev.sms < pl.grid) return DROT_ERR_UNSUPPORTED;
-    pl.p2_smem = 1;
-    pl.p2_cap_r = capr;
-    pl.p2_cap_c = capc;
-    pl.smem = smem2;
-  } else {
-    // Phase-2 state of each CTA's row / column slice in shared memory when
-    // it is small and the CTAs stay co-resident with it.
-    const int capr = ((nr + pl.grid - 1) / pl.grid + 3) & ~3;
-    const int capc = ((nc + pl.grid - 1) / pl.grid + 3) & ~3;
-    const int p2f = 3 * (capr + capc);
-    const int warps = pl.threads / 32;
-    const size_t smem2 = solve_smem_bytes(warps, pl.wt, S, pl.ns, tma, p2f);
-    pl.p2_smem = 0;
-    pl.p2_cap_r = pl.p2_cap_c = 0;
-    if ((size_t)p2f * sizeof(float) <= 48 * 1024 && smem2 <= budget) {
-      bool ok = true;
-      if (smem2 > 48 * 1024)
-        ok = cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem2) == cudaSuccess;
-      if (ok && occupancy(fn, pl.threads, smem2) * dev.sms >= pl.grid) {
-        pl.p2_smem = 1;
-        pl.p2_cap_r = capr;
-        pl.p2_cap_c = capc;
-        pl.smem = smem2;
-      }
+  // Phase-2 state of each CTA's row / column slice in shared memory when
+  // it is small and the CTAs stay co-resident with it.
+  const int capr = ((nr + pl.grid - 1) / pl.grid + 3) & ~3;
+  const int capc = ((nc + pl.grid - 1) / pl.grid + 3) & ~3;
+  const int p2f = 3 * (capr + capc);
+  const int warps = pl.threads / 32;
+  const size_t smem2 = solve_smem_bytes(warps, pl.wt, S, pl.ns, tma, p2f);
+  pl.p2_smem = 0;
+  pl.p2_cap_r = pl.p2_cap_c = 0;
+  if ((size_t)p2f * sizeof(float) <= 48 * 1024 && smem2 <= budget) {
+    bool ok = true;
+    if (smem2 > 48 * 1024)
+      ok = cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem2) == cudaSuccess;
+    if (ok && occupancy(fn, pl.threads, smem2) * dev.sms >= pl.grid) {
+      pl.p2_smem = 1;
+      pl.p2_cap_r = capr;
+      pl.p2_cap_c = capc;
+      pl.smem = smem2;
     }
   }
 
@@ -366,18 +331,6 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
   off = align_up(off + sizeof(float2) * pl.grid);
   pl.off_res = off;
   off = align_up(off + sizeof(float2) * pl.grid);
-  if (ldu) {
-    pl.off_rowpart1 = off;
-    off = align_up(off + sizeof(float) * (size_t)pl.P * nr);
-    pl.off_colpart1 = off;
-    off = align_up(off + sizeof(float) * (size_t)pl.nsb * nc);
-    pl.off_sum1 = off;
-    off = align_up(off + sizeof(float2) * pl.grid);
-    pl.off_obj1 = off;
-    off = align_up(off + sizeof(float2) * pl.grid);
-    pl.off_flag = off;
-    off = align_up(off + sizeof(unsigned) * pl.grid);
-  }
   pl.total = off;
   return DROT_OK;
 }
@@ -388,11 +341,10 @@ struct PlanKey {
   int dev, mode, nr, nc, G, vec, tma, warps, ctas, ctype;
   std::vector<int> ubounds;  // caller's GL group boundaries (empty: the reference's)
   int qr_kv;                 // DROT_QR_KV and DROT_GL_KV knobs
-  int ldu;                   // single-barrier kernels
   bool operator==(const PlanKey& o) const {
     return dev == o.dev && mode == o.mode && nr == o.nr && nc == o.nc && G == o.G &&
            vec == o.vec && tma == o.tma && warps == o.warps && ctas == o.ctas &&
-           ctype == o.ctype && ubounds == o.ubounds && qr_kv == o.qr_kv && ldu == o.ldu;
+           ctype == o.ctype && ubounds == o.ubounds && qr_kv == o.qr_kv;
   }
 };
 
@@ -400,15 +352,14 @@ static std::mutex g_plan_mu;
 static std::vector<std::pair<PlanKey, Plan>> g_plans;
 
 static int make_plan(int mode, int nr, int nc, int G, int vec, bool tma, Plan& pl,
-                     int ctype = DROT_C_F32, const int* ubounds = nullptr, bool ldu = false) {
+                     int ctype = DROT_C_F32, const int* ubounds = nullptr) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return DROT_ERR_CUDA;
   PlanKey key = {dev, mode, nr, nc, mode == MODE_GL ? G : 0, vec, tma ? 1 : 0,
                  tma ? tma_warps() : reg_warps(),
                  tma && getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1, ctype, {},
                  (getenv("DROT_QR_KV") ? atoi(getenv("DROT_QR_KV")) : 0) +
-                     16 * (getenv("DROT_GL_KV") ? atoi(getenv("DROT_GL_KV")) : 0),
-                 ldu ? 1 : 0};
+                     16 * (getenv("DROT_GL_KV") ? atoi(getenv("DROT_GL_KV")) : 0)};
   if (mode == MODE_GL && ubounds) key.ubounds.assign(ubounds, ubounds + G + 1);
   {
     std::lock_guard<std::mutex> lk(g_plan_mu);
@@ -416,7 +367,7 @@ static int make_plan(int mode, int nr, int nc, int G, int vec, bool tma, Plan& p
       if (e.first == key) { pl = e.second; return DROT_OK; }
   }
   const int rc = make_plan_uncached(mode, nr, nc, G, vec, tma, ctype, pl,
-                                    mode == MODE_GL ? ubounds : nullptr, ldu);
+                                    mode == MODE_GL ? ubounds : nullptr);
   if (rc == DROT_OK) {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     if (g_plans.size() >= 64) g_plans.erase(g_plans.begin());
@@ -439,14 +390,6 @@ static int path_override() {
 // part the fused update is bound by per-warp instruction latency, and two
 // 8-warp CTAs per SM with register-resident segments beat one 16-warp CTA
 // fed by the shared-memory TMA ring.  DROT_PATH=tma selects the ring.
-// DROT_LDU=1 asks for the single-barrier kernels (one grid barrier per
-// iteration, every CTA reducing its own band's and chunk's partials); they
-// are used where their plan fits (one warp per band or group), else the
-// two-barrier kernels.
-static bool ldu_requested() {
-  const char* e = getenv("DROT_LDU");
-  return e && atoi(e) == 1;
-}
 
 static int choose_plan(int mode, int nr, int nc, int G, bool aligned4, Plan& pl,
                        int ctype = DROT_C_F32, const int* ubounds = nullptr) {
@@ -455,9 +398,6 @@ static int choose_plan(int mode, int nr, int nc, int G, bool aligned4, Plan& pl,
     if (!aligned4) return DROT_ERR_UNSUPPORTED;
     return make_plan(mode, nr, nc, G, 4, true, pl, DROT_C_F32, ubounds);
   }
-  if (aligned4 && ldu_requested() &&
-      make_plan(mode, nr, nc, G, 4, false, pl, ctype, ubounds, true) == DROT_OK)
-    return DROT_OK;
   return make_plan(mode, nr, nc, G, aligned4 ? 4 : 1, false, pl, ctype, ubounds);
 }
 
@@ -470,9 +410,6 @@ static size_t scratch_bytes(int mode, int nr, int nc, int G, const int* ubounds 
     best = std::max(best, pl.total);
   if (make_plan(mode, nr, nc, G, 1, false, pl, DROT_C_F32, ubounds) == DROT_OK)
     best = std::max(best, pl.total);
-  if (ldu_requested() &&
-      make_plan(mode, nr, nc, G, 4, false, pl, DROT_C_F32, ubounds, true) == DROT_OK)
-    best = std::max(best, pl.total);
   return best;
 }
 
@@ -483,6 +420,15 @@ static long long barrier_timeout_ns() {
     if (ms > 0) return ms * 1000000LL;
   }
   return 10000LL * 1000000LL;  // 10 s
+}
+
+// DROT_TEST_STALL_CTA=k: CTA k skips its first grid-barrier arrival, so the
+// launch's bounded waits run out and it returns DROT_ERR_BARRIER_TIMEOUT
+// (with DROT_BARRIER_TIMEOUT_MS set low, quickly).  Failure-detection test
+// hook; off (-1) by default.
+static int stall_cta_hook() {
+  const char* e = getenv("DROT_TEST_STALL_CTA");
+  return (e && *e) ? atoi(e) : -1;
 }
 
 static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
@@ -563,13 +509,6 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
   prm.cta_sum = (float2*)(ws + pl.off_sum);
   prm.cta_obj = (float2*)(ws + pl.off_obj);
   prm.cta_res = (float2*)(ws + pl.off_res);
-  if (pl.ldu) {
-    prm.rowpart1 = (float*)(ws + pl.off_rowpart1);
-    prm.colpart1 = (float*)(ws + pl.off_colpart1);
-    prm.cta_sum1 = (float2*)(ws + pl.off_sum1);
-    prm.cta_obj1 = (float2*)(ws + pl.off_obj1);
-    prm.res_flag = (unsigned*)(ws + pl.off_flag);
-  }
   prm.bar = (unsigned int*)(ws + pl.off_ctrl);
   prm.abort_flag = (int*)(ws + pl.off_ctrl + 64);
   prm.stats = (DeviceStats*)(ws + pl.off_stats);
@@ -578,12 +517,10 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
   prm.timer_cta = getenv("DROT_TIMER_CTA") ? atoi(getenv("DROT_TIMER_CTA")) : 0;
   if (prm.timer_cta < 0 || prm.timer_cta >= pl.grid) prm.timer_cta = 0;
   prm.timeout_ns = barrier_timeout_ns();
+  prm.stall_cta = stall_cta_hook();
 
   if (cudaMemsetAsync(ws, 0, 512, A.stream) != cudaSuccess) return DROT_ERR_CUDA;
-  if (pl.ldu && cudaMemsetAsync(prm.res_flag, 0, sizeof(unsigned) * pl.grid, A.stream) !=
-                    cudaSuccess)
-    return DROT_ERR_CUDA;
-  SolveFn fn = kernel_for(A.mode, pl.vec, pl.kv, pl.tma, pl.ctype, pl.ldu);
+  SolveFn fn = kernel_for(A.mode, pl.vec, pl.kv, pl.tma, pl.ctype);
   if (pl.smem > 48 * 1024 &&
       cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)pl.smem) != cudaSuccess)
@@ -1002,26 +939,18 @@ namespace drot {
 // Workspace of the allocation-free entry point, one per device.
 static __device__ __align__(256) unsigned char g_noalloc_ws[DROT_NOALLOC_WORKSPACE_BYTES];
 
-static std::mutex g_noalloc_mu;
-static void* g_noalloc_ptr[64];  // device address of g_noalloc_ws per device ordinal
-
 // The array's name in host code is only a host-side handle; the kernels need
-// its device address, which the runtime gives per device.  Looked up once per
-// device, with that device current.
+// its device address, which the runtime gives per device.  Looked up on every
+// call, with the call's device current: the lookup is a host-side table read
+// once the library's device code is loaded, and no address is kept that a
+// cudaDeviceReset (a new context, possibly a new address) could leave stale.
 static int noalloc_workspace(void** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return DROT_ERR_CUDA;
-  if (dev < 0 || dev >= 64) return DROT_ERR_UNSUPPORTED;
-  std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* ptr = nullptr;
-    if (cudaGetSymbolAddress(&ptr, g_noalloc_ws) != cudaSuccess || !ptr) {
-      cudaGetLastError();
-      return DROT_ERR_CUDA;
-    }
-    g_noalloc_ptr[dev] = ptr;
+  void* ptr = nullptr;
+  if (cudaGetSymbolAddress(&ptr, g_noalloc_ws) != cudaSuccess || !ptr) {
+    cudaGetLastError();
+    return DROT_ERR_CUDA;
   }
-  *out = g_noalloc_ptr[dev];
+  *out = ptr;
   return DROT_OK;
 }
 

@@ -102,6 +102,8 @@ struct BatchParams {
   unsigned* bar;
   int* abort_flag;
   long long timeout_ns;
+  int stall_cta;       // test hook of the bounded waits (grid_barrier); -1 off
+  int pf_dist;         // L2 prefetch distance of the fused update, in warp steps (0 off)
   // Optional profile of CTA 0 for iterations it < iter_log_cap: globaltimer
   // at the start of the iteration, after its fused-update tiles, after the
   // first barrier and after its dual-update items (iter_log[4 it + 0..3]),
@@ -163,6 +165,26 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
   const int lo = T.lo, hi = T.hi, c1 = T.c1;
   const float s = I.s, kappa = I.kappa, krcp = I.kappa_rcp;
   for (int j0 = T.c0 + warp * NCOL; j0 < c1; j0 += W * NCOL) {
+    // L2 prefetch of this warp's step pf_dist steps ahead (its X segment,
+    // and C on even iterations): one 128-byte line per lane, no registers
+    // held, so more of the tile's bytes are in flight from DRAM than the
+    // register-resident loads of the 16 warps of an SM alone keep.
+    if (P.pf_dist > 0) {
+      const int jn = j0 + P.pf_dist * W * NCOL;
+      if (jn < c1) {
+        constexpr int RPC = 128 * KVR;  // rows per column of a warp step
+        if (lane < 16) {
+          const int cc = lane / (4 * KVR), r = lo + (lane % (4 * KVR)) * 32;
+          if (jn + cc < c1 && r < hi) prefetch_l2(P.x + I.x_off + (long long)(jn + cc) * I.ld + r);
+        } else if constexpr (EV && DIM == 0) {
+          constexpr int EPL = 128 / (int)sizeof(CT);  // elements per line
+          constexpr int LPC = (RPC + EPL - 1) / EPL;  // lines per column
+          const int li = lane - 16, cc = li / LPC, r = lo + (li % LPC) * EPL;
+          if (cc < NCOL && jn + cc < c1 && r < hi)
+            prefetch_l2(cbase + I.c_off + (long long)(jn + cc) * I.ld + r);
+        }
+      }
+    }
     float xv[4][VEC], cv[4][VEC], f2[NCOL];
     // All loads of the step first (nothing consumes them before the last
     // one is issued).
@@ -535,7 +557,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
   // the current one leaves CTAs idle.  False when the run was aborted.
   auto rebuild = [&]() -> bool {
     if (blockIdx.x == 0) build_active_lists(P, reinterpret_cast<int*>(smem_raw));
-    if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag)) return false;
+    if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag, P.stall_cta)) return false;
 #pragma unroll
     for (int l = 0; l < 5; ++l) n_act[l] = (int)__ldcg(P.counters + 8 + l);
     conv_seen = __ldcg(P.counters + 2);
@@ -651,7 +673,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
     }
 
     if (logit) P.iter_log[4 * it + 1] = globaltimer_ns();
-    if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag)) {
+    if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag, P.stall_cta)) {
       aborted = true;
       break;
     }
@@ -717,7 +739,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
     }
 
     if (logit) P.iter_log[4 * it + 3] = globaltimer_ns();
-    if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag)) {
+    if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag, P.stall_cta)) {
       aborted = true;
       break;
     }
@@ -760,7 +782,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
           P.stats[k] = st;
         }
       }
-      if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag)) {
+      if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag, P.stall_cta)) {
         aborted = true;
         break;
       }
@@ -862,10 +884,27 @@ static int fine_cols() {
   const int v = e ? atoi(e) : 0;
   return v > 0 ? v : 128;
 }
-static int fine_divisor() {
+// L2 prefetch distance of the fused update in warp steps (DROT_BATCH_PF,
+// 0..8; 0 switches the prefetch off).
+static int prefetch_distance() {
+  const char* e = getenv("DROT_BATCH_PF");
+  const int d = (e && *e) ? atoi(e) : 0;
+  return d < 0 ? 0 : (d > 8 ? 8 : d);
+}
+
+// Active tiles of a level below which the solve moves to the next finer
+// level, in quarters of the grid: DROT_BATCH_FINE_QUARTERS (default 2, i.e.
+// half the CTAs; 0 never moves).  DROT_BATCH_FINE_DIV=d, the older knob,
+// sets the threshold to grid / d.
+static long long fine_threshold(int grid) {
+  if (const char* e = getenv("DROT_BATCH_FINE_QUARTERS")) {
+    const int v = atoi(e);
+    return v <= 0 ? 0 : (long long)grid * v / 4;
+  }
   const char* e = getenv("DROT_BATCH_FINE_DIV");
   const int v = e ? atoi(e) : -1;
-  return v >= 0 ? (v == 0 ? 1 << 30 : v) : 2;
+  if (v == 0) return 0;
+  return grid / (v > 0 ? v : 2);
 }
 static int item_lines() {  // lines per dual-update item (DROT_BATCH_ITEM_LINES overrides)
   const char* e = getenv("DROT_BATCH_ITEM_LINES");
@@ -1155,7 +1194,7 @@ static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, 
   B.n_tiles_f = P.n_tiles_f;
   B.n_tiles_x = P.n_tiles_x;
   B.n_items_x = P.n_items_x;
-  B.fine_threshold = P.grid / fine_divisor();
+  B.fine_threshold = (int)fine_threshold(P.grid);
   B.items = (const BatchItem*)(ws + P.off_items);
   B.n_items = P.n_items;
   B.res_slot = (float2*)(ws + P.off_res);
@@ -1180,6 +1219,11 @@ static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, 
   const char* e = getenv("DROT_BARRIER_TIMEOUT_MS");
   const long long ms = (e && atoll(e) > 0) ? atoll(e) : 10000LL;
   B.timeout_ns = ms * 1000000LL;
+  // DROT_TEST_STALL_CTA=k: CTA k skips its first grid-barrier arrival (the
+  // failure-detection test hook of the bounded waits; off by default).
+  const char* sc = getenv("DROT_TEST_STALL_CTA");
+  B.stall_cta = (sc && *sc) ? atoi(sc) : -1;
+  B.pf_dist = prefetch_distance();
   if (cudaMemsetAsync(ws + P.off_ctrl, 0, 512, st) != cudaSuccess) return DROT_ERR_CUDA;
   batch_init_kernel<<<dim3(64, P.n_inst), 256, 0, st>>>(B);
   if (cudaGetLastError() != cudaSuccess) return DROT_ERR_CUDA;

@@ -238,11 +238,261 @@ static size_t cost_smem_bytes(int dim) {
   return (size_t)(kCostM + kCostN) * dim * 4 * 2 + sizeof(float) * (kCostM + kCostN);
 }
 
+// ---------------------------------------------------------------------------
+// chain rule of the cost to the points (autograd backward of the cost)
+// ---------------------------------------------------------------------------
+//
+// For G = dL/dC of one instance (column-major m x n, the layout of C),
+//     dL/dx_i = 2 scale (x_i sum_j G_ij - sum_j G_ij y_j)
+//     dL/dy_j = 2 scale (y_j sum_i G_ij - sum_i G_ij x_i)
+// (G zeroed where C = 0 when the cost was clamped).  CTA (band b, instance
+// k) owns rows [256 b, 256 b + 256) and walks the columns in tiles of 64:
+// the G tile goes to shared memory (row pitch 65: conflict-free both ways),
+// thread t accumulates row t's sums over the columns (its dL/dx, written at
+// the end), and thread (column c, k-group) the column sums of the tile over
+// the band's rows, written as the band's partial of dL/dy; a second kernel
+// adds the bands' partials in band order.  No atomics: deterministic.
+
+constexpr int kGradRows = 256;  // rows per CTA (= threads)
+constexpr int kGradCols = 64;   // columns per tile
+constexpr int kGradPitch = kGradCols + 1;
+
+struct GradInst {
+  long long x_off, y_off, c_off;  // element offsets: x (m x d), y (n x d), G / C (ld x n)
+  long long part_off;             // float offset of its partials [bands][n][d + 1]
+  int m, n, ld, bands, aligned;
+  int pad;
+};
+
+struct GradParams {
+  const float* x;
+  const float* y;
+  const float* g;
+  const float* c;  // null: no clamp mask
+  float* gx;
+  float* gy;
+  float* part;
+  int n_inst;
+  float scale2;  // 2 * scale
+  GradInst inst[kCostMaxInst];
+};
+
+template <int DIM>
+__global__ void __launch_bounds__(kGradRows, 2) cost_grad_kernel(const GradParams P) {
+  extern __shared__ __align__(16) float gsm[];
+  float* gt = gsm;                               // [kGradRows][kGradPitch]
+  float* xs = gt + kGradRows * kGradPitch;       // [kGradRows][DIM]
+  float* ys = xs + kGradRows * DIM;              // [kGradCols][DIM]
+  const GradInst I = P.inst[blockIdx.y];
+  const int b = blockIdx.x;
+  if (b >= I.bands) return;
+  const int t = threadIdx.x;
+  const int r0 = b * kGradRows;
+  constexpr int KG = DIM / 4;  // k values per column thread
+  for (int e = t; e < kGradRows * DIM; e += kGradRows) {
+    const int r = e / DIM, k = e - r * DIM;
+    xs[e] = r0 + r < I.m ? __ldg(P.x + I.x_off + (long long)(r0 + r) * DIM + k) : 0.0f;
+  }
+  float ax[DIM], rs = 0.0f;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) ax[k] = 0.0f;
+  const int cc = t % kGradCols, kg = t / kGradCols;
+  const float* gbase = P.g + I.c_off;
+  const float* cbase = P.c ? P.c + I.c_off : nullptr;
+  for (int c0 = 0; c0 < I.n; c0 += kGradCols) {
+    __syncthreads();  // the previous tile's readers are done
+    for (int e = t; e < kGradCols * DIM; e += kGradRows) {
+      const int c = e / DIM, k = e - c * DIM;
+      ys[e] = c0 + c < I.n ? __ldg(P.y + I.y_off + (long long)(c0 + c) * DIM + k) : 0.0f;
+    }
+    // G tile: a column is 256 contiguous rows; 64 threads per column, 4 rows each.
+    for (int pass = 0; pass < kGradCols / 4; ++pass) {
+      const int c = pass * 4 + t / 64, rr = 4 * (t % 64);
+      const int j = c0 + c, i = r0 + rr;
+      float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      if (j < I.n && i < I.m) {
+        const long long off = (long long)j * I.ld + i;
+        if (I.aligned && i + 4 <= I.m) {
+          const float4 q = __ldg(reinterpret_cast<const float4*>(gbase + off));
+          v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+          if (cbase) {
+            const float4 cq = __ldg(reinterpret_cast<const float4*>(cbase + off));
+            v[0] = cq.x > 0.0f ? v[0] : 0.0f;
+            v[1] = cq.y > 0.0f ? v[1] : 0.0f;
+            v[2] = cq.z > 0.0f ? v[2] : 0.0f;
+            v[3] = cq.w > 0.0f ? v[3] : 0.0f;
+          }
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (i + e < I.m) {
+              const float gv = __ldg(gbase + off + e);
+              v[e] = (!cbase || __ldg(cbase + off + e) > 0.0f) ? gv : 0.0f;
+            }
+        }
+      }
+#pragma unroll
+      for (int e = 0; e < 4; ++e) gt[(rr + e) * kGradPitch + c] = v[e];
+    }
+    __syncthreads();
+    // row t: sums over the tile's columns
+    {
+      const float* grow = gt + t * kGradPitch;
+#pragma unroll 4
+      for (int c = 0; c < kGradCols; ++c) {
+        const float gv = grow[c];
+        rs += gv;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) ax[k] = fmaf(gv, ys[c * DIM + k], ax[k]);
+      }
+    }
+    // column cc, k-group kg: sums over the band's rows -> the band's partial
+    {
+      float ay[KG], cs = 0.0f;
+#pragma unroll
+      for (int k = 0; k < KG; ++k) ay[k] = 0.0f;
+#pragma unroll 4
+      for (int r = 0; r < kGradRows; ++r) {
+        const float gv = gt[r * kGradPitch + cc];
+        cs += gv;
+#pragma unroll
+        for (int k = 0; k < KG; ++k) ay[k] = fmaf(gv, xs[r * DIM + kg * KG + k], ay[k]);
+      }
+      const int j = c0 + cc;
+      if (j < I.n) {
+        float* pp = P.part + I.part_off + ((long long)b * I.n + j) * (DIM + 1);
+#pragma unroll
+        for (int k = 0; k < KG; ++k) pp[kg * KG + k] = ay[k];
+        if (kg == 0) pp[DIM] = cs;
+      }
+    }
+  }
+  const int i = r0 + t;
+  if (i < I.m) {
+    float* o = P.gx + I.x_off + (long long)i * DIM;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) o[k] = P.scale2 * fmaf(xs[t * DIM + k], rs, -ax[k]);
+  }
+}
+
+// dL/dy_j from the bands' partials, added in band order.
+template <int DIM>
+__global__ void cost_grad_reduce_kernel(const GradParams P) {
+  const GradInst I = P.inst[blockIdx.y];
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < I.n; j += gridDim.x * blockDim.x) {
+    float a[DIM + 1];
+#pragma unroll
+    for (int k = 0; k <= DIM; ++k) a[k] = 0.0f;
+    for (int b = 0; b < I.bands; ++b) {
+      const float* pp = P.part + I.part_off + ((long long)b * I.n + j) * (DIM + 1);
+#pragma unroll
+      for (int k = 0; k <= DIM; ++k) a[k] += __ldcg(pp + k);
+    }
+    const float* yj = P.y + I.y_off + (long long)j * DIM;
+    float* o = P.gy + I.y_off + (long long)j * DIM;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) o[k] = P.scale2 * fmaf(__ldg(yj + k), a[DIM], -a[k]);
+  }
+}
+
+static size_t grad_smem_bytes(int dim) {
+  return sizeof(float) * ((size_t)kGradRows * kGradPitch + (size_t)kGradRows * dim +
+                          (size_t)kGradCols * dim);
+}
+
+// Partials layout; returns the floats they need (0: invalid descriptors).
+static long long grad_layout(int n_inst, const drot_cost_instance* inst, int dim, GradParams* P) {
+  long long part = 0;
+  for (int k = 0; k < n_inst; ++k) {
+    const drot_cost_instance& a = inst[k];
+    if (a.m <= 0 || a.n <= 0 || a.ld < a.m || a.x_offset < 0 || a.y_offset < 0 || a.c_offset < 0)
+      return 0;
+    const int bands = (a.m + kGradRows - 1) / kGradRows;
+    if (P) {
+      GradInst& I = P->inst[k];
+      I.x_off = a.x_offset * dim;
+      I.y_off = a.y_offset * dim;
+      I.c_off = a.c_offset;
+      I.part_off = part;
+      I.m = a.m;
+      I.n = a.n;
+      I.ld = a.ld;
+      I.bands = bands;
+      I.aligned = (a.ld % 4 == 0) && (a.c_offset % 4 == 0);
+    }
+    part += (long long)bands * a.n * (dim + 1);
+  }
+  return part;
+}
+
 }  // namespace drot
 
 using namespace drot;
 
 extern "C" {
+
+size_t drot_sqeuclidean_cost_grad_workspace_bytes(int n_inst, const drot_cost_instance* inst,
+                                                  int dim) {
+  if (n_inst <= 0 || n_inst > kCostMaxInst || !inst || dim <= 0 || dim > 32 || (dim & 7))
+    return 0;
+  const long long f = grad_layout(n_inst, inst, dim, nullptr);
+  return f > 0 ? (size_t)f * sizeof(float) : 0;
+}
+
+int drot_sqeuclidean_cost_grad(int n_inst, const drot_cost_instance* inst, const float* x,
+                               const float* y, int dim, float scale, const float* c,
+                               const float* grad_c, float* grad_x, float* grad_y,
+                               void* workspace, size_t workspace_bytes, drot_stream_t stream) {
+  if (n_inst <= 0 || n_inst > kCostMaxInst || !inst || !x || !y || !grad_c || !grad_x ||
+      !grad_y || !workspace)
+    return DROT_ERR_INVALID_ARG;
+  if (dim <= 0 || dim > 32 || (dim & 7) != 0) return DROT_ERR_UNSUPPORTED;
+  if (((uintptr_t)grad_c & 15u) || (c && ((uintptr_t)c & 15u))) return DROT_ERR_INVALID_ARG;
+  static GradParams P;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  memset(&P, 0, sizeof(P));
+  const long long nf = grad_layout(n_inst, inst, dim, &P);
+  if (nf <= 0) return DROT_ERR_INVALID_ARG;
+  if (workspace_bytes < (size_t)nf * sizeof(float)) return DROT_ERR_WORKSPACE;
+  int max_bands = 0, max_n = 0;
+  for (int k = 0; k < n_inst; ++k) {
+    max_bands = std::max(max_bands, P.inst[k].bands);
+    max_n = std::max(max_n, P.inst[k].n);
+  }
+  P.x = x;
+  P.y = y;
+  P.g = grad_c;
+  P.c = c;
+  P.gx = grad_x;
+  P.gy = grad_y;
+  P.part = (float*)workspace;
+  P.n_inst = n_inst;
+  P.scale2 = 2.0f * scale;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t smem = grad_smem_bytes(dim);
+  const void* k1 = dim == 8 ? (const void*)cost_grad_kernel<8>
+                 : dim == 16 ? (const void*)cost_grad_kernel<16>
+                 : dim == 24 ? (const void*)cost_grad_kernel<24>
+                             : (const void*)cost_grad_kernel<32>;
+  const void* k2 = dim == 8 ? (const void*)cost_grad_reduce_kernel<8>
+                 : dim == 16 ? (const void*)cost_grad_reduce_kernel<16>
+                 : dim == 24 ? (const void*)cost_grad_reduce_kernel<24>
+                             : (const void*)cost_grad_reduce_kernel<32>;
+  if (cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return DROT_ERR_CUDA;
+  void* args[] = {(void*)&P};
+  if (cudaLaunchKernel(k1, dim3(max_bands, n_inst), dim3(kGradRows), args, smem, st) !=
+          cudaSuccess ||
+      cudaLaunchKernel(k2, dim3(std::min((max_n + 255) / 256, 64), n_inst), dim3(256), args, 0,
+                       st) != cudaSuccess) {
+    cudaGetLastError();
+    return DROT_ERR_CUDA;
+  }
+  return DROT_OK;
+}
+
 
 int drot_sqeuclidean_cost(int n_inst, const drot_cost_instance* inst, const float* x,
                           const float* y, int dim, float scale, int clamp, float* c,

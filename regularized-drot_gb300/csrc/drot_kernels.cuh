@@ -113,16 +113,9 @@ struct SolveParams {
   int* abort_flag;     // zeroed before launch
   DeviceStats* stats;
   int timer_cta;       // CTA whose stage times are recorded (phase_ns)
+  int stall_cta;       // test hook of the bounded waits (grid_barrier); -1 off
   long long timeout_ns;
   int gbounds[kMaxGroups + 1];  // GL: group row boundaries
-  // Single-barrier iteration (LDU kernels): the partials of odd iterations
-  // go to these second buffers, and res_flag[cta] = it + 1 publishes the
-  // residual partial of a CTA that owns a band's rows or a chunk's columns.
-  float* rowpart1;
-  float* colpart1;
-  float2* cta_sum1;
-  float2* cta_obj1;
-  unsigned* res_flag;  // [grid], zeroed before launch
 };
 
 
@@ -146,8 +139,9 @@ __device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
 }
 
-__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+// Hint: fetch the 128-byte line holding p into L2 (no register, no wait).
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" :: "l"(p));
 }
 
 __device__ __forceinline__ int ld_volatile_i32(const int* p) {
@@ -238,18 +232,22 @@ __device__ __forceinline__ fpair block_sum_fp(fpair v, fpair* scratch) {
 }
 
 // Grid barrier.  Returns false when the run was aborted (time limit hit here
-// or in another CTA).  `epoch` counts barriers passed by this CTA.  The CTA
+// or in another CTA).  `epoch` counts barriers passed by this CTA.
+// stall_cta >= 0 is the failure-detection test hook: that CTA does not
+// arrive at its first barrier, so every CTA's bounded wait runs out and the
+// launch ends with the time-limit status (no fault, no unbounded wait).  The
+// CTA
 // barrier orders every thread's writes before thread 0's release add, and
 // thread 0's acquire load before every thread's later reads (the release /
 // acquire pattern needs no separate fences: 1.5 us per barrier at 300 CTAs
 // against 1.8 us with a fence on each side).
 __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* abort_flag, long long timeout_ns,
-                                             unsigned& epoch, int* s_flag) {
+                                             unsigned& epoch, int* s_flag, int stall_cta = -1) {
   __syncthreads();
   if (threadIdx.x == 0) {
     epoch += 1u;
     const unsigned target = epoch * gridDim.x;
-    red_release_add_u32(bar, 1u);
+    if (!(epoch == 1u && (int)blockIdx.x == stall_cta)) red_release_add_u32(bar, 1u);
     int ok = 1;
     const unsigned long long t0 = globaltimer_ns();
     unsigned spins = 0;
@@ -270,7 +268,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, int* abort_flag, lon
 }
 
 __device__ __forceinline__ bool grid_barrier(const SolveParams& P, unsigned& epoch, int* s_flag) {
-  return grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, s_flag);
+  return grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, s_flag, P.stall_cta);
 }
 
 // ---- shared-memory addresses, mbarriers and TMA bulk copies -------------
@@ -489,52 +487,6 @@ __device__ __forceinline__ void reduce_partials(int r0, int r1, int k0, int k1,
   }
 }
 
-// Row sums of the band rows [lo, hi) (np_r partials each, partial k of row
-// i at rp[k * nr + i]) and column sums of the chunk columns [c0, c1) (np_c
-// partials at cp[k * nc + j]) for the LDU kernels.  A thread takes two lines
-// at a time and issues 8 loads of each before adding any (16 per line spill
-// at the register cap); per line the partials are added in a fixed order (a
-// tree within each group of 8, the groups in index order), so every CTA of
-// a band (of a chunk) gets bitwise the same sums.  fin_r(i, sum) /
-// fin_c(j, sum) consume them.
-__device__ __forceinline__ float tree8(const float (&a)[8]) {
-  return ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
-}
-
-template <typename FinR, typename FinC>
-__device__ __forceinline__ void ldu_reduce(const float* rp, const float* cp, int lo, int hi, int c0,
-                                           int c1, long long nr, long long nc, int np_r, int np_c,
-                                           FinR fin_r, FinC fin_c) {
-  const int R = hi - lo, items = R + (c1 - c0), nt = blockDim.x;
-  for (int i0 = threadIdx.x; i0 < items; i0 += 2 * nt) {
-    const int i1 = i0 + nt;
-    const bool live1 = i1 < items;
-    const bool row0 = i0 < R, row1 = i1 < R;
-    const float* p0 = row0 ? rp + lo + i0 : cp + c0 + (i0 - R);
-    const float* p1 = live1 ? (row1 ? rp + lo + i1 : cp + c0 + (i1 - R)) : p0;
-    const long long s0 = row0 ? nr : nc, s1 = row1 ? nr : nc;
-    const int n0 = row0 ? np_r : np_c;
-    const int n1 = live1 ? (row1 ? np_r : np_c) : 0;
-    float t0 = 0.0f, t1 = 0.0f;
-    for (int k0 = 0; k0 < max(n0, n1); k0 += 8) {
-      float a[8], b[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        a[u] = k0 + u < n0 ? __ldcg(p0 + (long long)(k0 + u) * s0) : 0.0f;
-        b[u] = k0 + u < n1 ? __ldcg(p1 + (long long)(k0 + u) * s1) : 0.0f;
-      }
-      t0 += tree8(a);
-      t1 += tree8(b);
-    }
-    if (row0) fin_r(lo + i0, t0);
-    else fin_c(c0 + i0 - R, t0);
-    if (live1) {
-      if (row1) fin_r(lo + i1, t1);
-      else fin_c(c0 + i1 - R, t1);
-    }
-  }
-}
-
 // Dynamic shared memory of the solve kernel (must match the device layout).
 //   ring    TMA: W * ns * 2 * S floats (stage: X segment, C segment)
 //           reg: W * S floats (row-partial staging only)
@@ -555,20 +507,10 @@ __host__ __device__ constexpr size_t solve_smem_bytes(int warps, int wt, int S, 
 // The solve kernel
 // ---------------------------------------------------------------------------
 
-// LDU (local dual update): one grid barrier per iteration instead of two.
-// Every CTA reduces the row partials of its own band and the column partials
-// of its own chunk itself (the same sums, in the same order, in every CTA of
-// the band or chunk) and keeps a, phi1 of its band rows and b, phi2 of its
-// columns in shared memory; partial buffers alternate by iteration parity so
-// the next iteration's writes never meet this iteration's reads.  On
-// stop-test iterations the CTAs that own a band's rows (chunk 0) or a
-// chunk's columns (band 0) publish their residual partial with a flag, and
-// every CTA waits (bounded) for those flags only.
-template <int MODE, int VEC, int KV, bool TMA, typename CT = float, bool LDU = false>
+template <int MODE, int VEC, int KV, bool TMA, typename CT = float>
 __global__ void __launch_bounds__(512, 1)
 drot_solve_kernel(const SolveParams P) {
   static_assert(!TMA || VEC == 4, "the TMA path moves 16-byte vectors");
-  static_assert(!LDU || (!TMA && VEC == 4), "LDU: register path, 4-wide vectors");
   static_assert(!TMA || std::is_same<CT, float>::value, "the TMA path streams float costs");
   const CT* const cbase = reinterpret_cast<const CT*>(P.c);
   constexpr int SV = 32 * VEC;        // rows per vector slot of a warp
@@ -663,22 +605,7 @@ drot_solve_kernel(const SolveParams P) {
   const int r_hi = (int)(((long long)P.nr * (blockIdx.x + 1)) / G);
   const int k_lo = (int)(((long long)P.nc * blockIdx.x) / G);
   const int k_hi = (int)(((long long)P.nc * (blockIdx.x + 1)) / G);
-  if constexpr (LDU) {
-    // p, a, phi1 of the band rows and q, b, phi2 of the chunk columns stay
-    // in shared memory for the whole solve (capr >= Wt * S, capc >= c1 - c0).
-    for (int idx = threadIdx.x; idx < Wt * S; idx += blockDim.x) {
-      const int r = base + idx;
-      const bool in = r >= lo && r < hi;
-      s_p[idx] = in ? P.p[r] : 0.0f;
-      s_a[idx] = in ? P.a[r] : 0.0f;
-      f1s[idx] = in ? P.phi1[r] : 0.0f;
-    }
-    for (int j = threadIdx.x; j < c1 - c0; j += blockDim.x) {
-      s_q[j] = P.q[c0 + j];
-      s_b[j] = P.b[c0 + j];
-      s_t2[j] = P.phi2[c0 + j];
-    }
-  } else if (P.p2_smem) {
+  if (P.p2_smem) {
     for (int i = threadIdx.x; i < r_hi - r_lo; i += blockDim.x) {
       s_p[i] = P.p[r_lo + i];
       s_a[i] = P.a[r_lo + i];
@@ -702,7 +629,6 @@ drot_solve_kernel(const SolveParams P) {
   bool aborted = false;
   double last_obj = 0.0;
   int obj_valid = 0;
-  int obj_par = 0;  // LDU: parity of the last objective-bearing iteration
   double last_res = -1.0;
   double last_sigma = 0.0;
 
@@ -732,15 +658,10 @@ drot_solve_kernel(const SolveParams P) {
     stamp(0);
 
     // ------------------------------------------------------------ phase 1
-    // Partial buffers of this iteration: LDU kernels alternate by parity
-    // (odd_buf is a compile-time false in the others).
-    const bool odd_buf = LDU && (it & 1);
-    // phi1 of the band rows -> shared memory (LDU: already there).
-    if constexpr (!LDU) {
-      for (int idx = threadIdx.x; idx < Wt * S; idx += blockDim.x) {
-        const int r = base + idx;
-        f1s[idx] = (r >= lo && r < hi) ? __ldcg(P.phi1 + r) : 0.0f;
-      }
+    // phi1 of the band rows -> shared memory.
+    for (int idx = threadIdx.x; idx < Wt * S; idx += blockDim.x) {
+      const int r = base + idx;
+      f1s[idx] = (r >= lo && r < hi) ? __ldcg(P.phi1 + r) : 0.0f;
     }
     __syncthreads();
     float acc[KV][VEC];
@@ -837,7 +758,7 @@ drot_solve_kernel(const SolveParams P) {
 
       // Prox, store and partial sums of column j (segment in xv / cv).
       auto finish = [&](int j, float (&xv)[KV][VEC], const float (&cv)[KV][VEC], int par) {
-        const float f2 = LDU ? s_t2[j - c0] : __ldcg(P.phi2 + j);
+        const float f2 = __ldcg(P.phi2 + j);
         float* xcol = P.x + (long long)j * ld;
         float f1[KV][VEC];
 #pragma unroll
@@ -995,7 +916,7 @@ drot_solve_kernel(const SolveParams P) {
           ob_lo += e1;
         }
         colp = warp_sum(colp);
-        if (lane == 0) (odd_buf ? P.colpart1 : P.colpart)[(long long)sb * P.nc + j] = colp;
+        if (lane == 0) P.colpart[(long long)sb * P.nc + j] = colp;
       };
 
       if constexpr (TMA) {
@@ -1072,7 +993,7 @@ drot_solve_kernel(const SolveParams P) {
           const int kk = idx / S, r = idx - kk * S;
           float t = 0.0f;
           for (int tm = 0; tm < nteams; ++tm) t += red[(size_t)(tm * Wt + kk) * S + r];
-          (odd_buf ? P.rowpart1 : P.rowpart)[(long long)chunk * P.nr + row] = t;
+          P.rowpart[(long long)chunk * P.nr + row] = t;
         }
       }
     }
@@ -1082,8 +1003,8 @@ drot_solve_kernel(const SolveParams P) {
       t = warp_sum_fp(t);
       if (with_c) o = warp_sum_fp(o);
       if (lane == 0) {
-        (odd_buf ? P.cta_sum1 : P.cta_sum)[blockIdx.x] = make_float2(t.hi, t.lo);
-        if (with_c) (odd_buf ? P.cta_obj1 : P.cta_obj)[blockIdx.x] = make_float2(o.hi, o.lo);
+        P.cta_sum[blockIdx.x] = make_float2(t.hi, t.lo);
+        if (with_c) P.cta_obj[blockIdx.x] = make_float2(o.hi, o.lo);
       }
     }
 
@@ -1099,217 +1020,95 @@ drot_solve_kernel(const SolveParams P) {
     //     the duals a, b; (dual - residual) is staged until gamma is known;
     // (c) one block sync, then phi = (staged + gamma) / n_cols (or n_rows).
     const bool check = (MODE == MODE_GL) || even || P.stop_every;
-    if constexpr (!LDU) {
-      if (warp == 0) {
-        const fpair ts = warp_sum_strided_fp(P.cta_sum, G, lane);
-        if (lane == 0) {
-          // The float total mass: RN(hi + lo) of the normalised pair.
-          const float sigma = ts.hi + ts.lo;
-          const double t = fp_value(ts);
-          s_misc_f[0] = (float)((2.0 * ((double)sigma - 1.0) - (double)alpha) /
-                                (double)(P.nr + P.nc));
-          alpha = (float)(((double)alpha + 1.0) - (double)sigma);
-          s_misc_d[0] = t;
-        }
+    if (warp == 0) {
+      const fpair ts = warp_sum_strided_fp(P.cta_sum, G, lane);
+      if (lane == 0) {
+        // The float total mass: RN(hi + lo) of the normalised pair.
+        const float sigma = ts.hi + ts.lo;
+        const double t = fp_value(ts);
+        s_misc_f[0] = (float)((2.0 * ((double)sigma - 1.0) - (double)alpha) /
+                              (double)(P.nr + P.nc));
+        alpha = (float)(((double)alpha + 1.0) - (double)sigma);
+        s_misc_d[0] = t;
       }
-      fpair res = fp_make(0.0f);
-      const bool sm2 = P.p2_smem != 0;
-      reduce_partials(
-          r_lo, r_hi, k_lo, k_hi, P.rowpart, P.colpart, P.nr, P.nc, P.P, P.nsb,
-          [&](int i, float t) {
-            const int li = i - r_lo;
-            const float rs = t - (sm2 ? s_p[li] : __ldg(P.p + i));
-            const float ab = (sm2 ? s_a[li] : P.a[i]) - rs;
-            if (sm2) {
-              s_a[li] = ab;
-              s_t1[li] = ab - rs;
-            } else {
-              P.a[i] = ab;
-              P.phi1[i] = ab - rs;
-            }
-            res = fp_add(res, fp_sqr(rs));
-          },
-          [&](int j, float t) {
-            const int lj = j - k_lo;
-            const float cs = t - (sm2 ? s_q[lj] : __ldg(P.q + j));
-            const float ab = (sm2 ? s_b[lj] : P.b[j]) - cs;
-            if (sm2) {
-              s_b[lj] = ab;
-              s_t2[lj] = ab - cs;
-            } else {
-              P.b[j] = ab;
-              P.phi2[j] = ab - cs;
-            }
-            res = fp_add(res, fp_sqr(cs));
-          });
-      if (check) {
-        res = warp_sum_fp(res);
-        if (lane == 0) dscr[warp] = res;
-      }
-      __syncthreads();
-      {
-        const float gamma = s_misc_f[0];
-        for (int i = threadIdx.x; i < r_hi - r_lo; i += blockDim.x) {
-          const float t = sm2 ? s_t1[i] : __ldcg(P.phi1 + r_lo + i);
-          P.phi1[r_lo + i] = div_rn_by(t + gamma, nc_f, nc_rcp);
-        }
-        for (int j = threadIdx.x; j < k_hi - k_lo; j += blockDim.x) {
-          const float t = sm2 ? s_t2[j] : __ldcg(P.phi2 + k_lo + j);
-          P.phi2[k_lo + j] = div_rn_by(t + gamma, nr_f, nr_rcp);
-        }
-      }
-      if (check && warp == 0) {
-        fpair t = lane < W ? dscr[lane] : fp_make(0.0f);
-        t = warp_sum_fp(t);
-        if (lane == 0) P.cta_res[blockIdx.x] = make_float2(t.hi, t.lo);
-      }
-      last_sigma = s_misc_d[0];
-      if (with_c) obj_valid = 1;
-
-      stamp(3);
-      if (!grid_barrier(P, epoch, &s_flag)) { aborted = true; break; }
-
-      if (check) {
-        // One thread turns the squared residual into the decision; the square
-        // root is taken once, after the loop.
-        if (warp == 0) {
-          const fpair t = warp_sum_strided_fp(P.cta_res, G, lane);
-          if (lane == 0) {
-            const double r2 = fp_value(t);
-            s_misc_d[1] = r2;
-            s_stop = r2 < P.res2_stop ? 1 : 0;
-          }
-        }
-        __syncthreads();
-        last_res = s_misc_d[1];  // squared until the epilogue
-        if (s_stop) {
-          converged = true;
-          stamp(4);
-          break;
-        }
-      }
-      stamp(4);
-    } else {
-      // (a) warp 0: sigma, gamma and the next alpha as above;
-      // (b) every thread: row sums of the band rows and column sums of the
-      //     chunk columns (partials of this iteration's parity), duals and
-      //     staged phi in shared memory;
-      // (c) phi = (staged + gamma) / n;
-      // (d) stop-test iterations: owners publish their residual partial,
-      //     every CTA waits for the owners' flags and decides.
-      const bool odd_r = (it & 1) != 0;
-      const float2* const cs_r = odd_r ? P.cta_sum1 : P.cta_sum;
-      const float* const rp_r = odd_r ? P.rowpart1 : P.rowpart;
-      const float* const cp_r = odd_r ? P.colpart1 : P.colpart;
-      if (warp == 0) {
-        const fpair ts = warp_sum_strided_fp(cs_r, G, lane);
-        if (lane == 0) {
-          const float sigma = ts.hi + ts.lo;
-          const double t = fp_value(ts);
-          s_misc_f[0] = (float)((2.0 * ((double)sigma - 1.0) - (double)alpha) /
-                                (double)(P.nr + P.nc));
-          alpha = (float)(((double)alpha + 1.0) - (double)sigma);
-          s_misc_d[0] = t;
-        }
-      }
-      const bool own_rows = chunk == 0, own_cols = band == 0;
-      fpair res = fp_make(0.0f);
-      ldu_reduce(rp_r, cp_r, lo, hi, c0, c1, P.nr, P.nc, P.P, P.nsb,
-                 [&](int i, float t) {
-                   const int li = i - base;
-                   const float rs = t - s_p[li];
-                   const float ab = s_a[li] - rs;
-                   s_a[li] = ab;
-                   f1s[li] = ab - rs;
-                   if (own_rows) res = fp_add(res, fp_sqr(rs));
-                 },
-                 [&](int j, float t) {
-                   const int lj = j - c0;
-                   const float cs = t - s_q[lj];
-                   const float ab = s_b[lj] - cs;
-                   s_b[lj] = ab;
-                   s_t2[lj] = ab - cs;
-                   if (own_cols) res = fp_add(res, fp_sqr(cs));
-                 });
-      if (check) {
-        res = warp_sum_fp(res);
-        if (lane == 0) dscr[warp] = res;
-      }
-      __syncthreads();
-      {
-        const float gamma = s_misc_f[0];
-        for (int i = lo + threadIdx.x; i < hi; i += blockDim.x)
-          f1s[i - base] = div_rn_by(f1s[i - base] + gamma, nc_f, nc_rcp);
-        for (int j = threadIdx.x; j < c1 - c0; j += blockDim.x)
-          s_t2[j] = div_rn_by(s_t2[j] + gamma, nr_f, nr_rcp);
-      }
-      last_sigma = s_misc_d[0];
-      if (with_c) {
-        obj_valid = 1;
-        obj_par = it & 1;
-      }
-      stamp(3);
-      if (check) {
-        if (warp == 0) {
-          fpair t = lane < W ? dscr[lane] : fp_make(0.0f);
-          t = warp_sum_fp(t);
-          const unsigned want = (unsigned)(it + 1);
-          if (lane == 0 && (own_rows || own_cols)) {
-            P.cta_res[blockIdx.x] = make_float2(t.hi, t.lo);
-            st_release_u32(P.res_flag + blockIdx.x, want);
-          }
-          // Owners: chunk 0 of every band, then chunks 1.. of band 0.
-          const int nown = P.nbands + P.P - 1;
-          auto owner = [&](int d) { return d < P.nbands ? d * P.P : d - P.nbands + 1; };
-          int ok = 1;
-          const unsigned long long t0 = globaltimer_ns();
-          unsigned spins = 0;
-          for (;;) {
-            bool mine = true;
-            for (int d = lane; d < nown; d += 32)
-              mine &= (int)(ld_acquire_u32(P.res_flag + owner(d)) - want) >= 0;
-            if (__all_sync(0xffffffffu, mine)) break;
-            if ((++spins & 15u) == 0u) {
-              int bad = 0;
-              if (lane == 0)
-                bad = ld_volatile_i32(P.abort_flag) ||
-                      (long long)(globaltimer_ns() - t0) > P.timeout_ns;
-              if (__shfl_sync(0xffffffffu, bad, 0)) {
-                if (lane == 0) atomicExch(P.abort_flag, 1);
-                ok = 0;
-                break;
-              }
-            }
-          }
-          fpair r2 = fp_make(0.0f);
-          if (ok) {
-            for (int d = lane; d < nown; d += 32) {
-              const float2 u = __ldcg(P.cta_res + owner(d));
-              r2 = fp_add(r2, fpair{u.x, u.y});
-            }
-          }
-          r2 = warp_sum_fp(r2);
-          if (lane == 0) {
-            const double v = fp_value(r2);
-            s_flag = ok;
-            s_misc_d[1] = v;
-            s_stop = v < P.res2_stop ? 1 : 0;
-          }
-        }
-        __syncthreads();
-        if (!s_flag) {
-          aborted = true;
-          break;
-        }
-        last_res = s_misc_d[1];
-        if (s_stop) {
-          converged = true;
-          stamp(4);
-          break;
-        }
-      }
-      stamp(4);
     }
+    fpair res = fp_make(0.0f);
+    const bool sm2 = P.p2_smem != 0;
+    reduce_partials(
+        r_lo, r_hi, k_lo, k_hi, P.rowpart, P.colpart, P.nr, P.nc, P.P, P.nsb,
+        [&](int i, float t) {
+          const int li = i - r_lo;
+          const float rs = t - (sm2 ? s_p[li] : __ldg(P.p + i));
+          const float ab = (sm2 ? s_a[li] : P.a[i]) - rs;
+          if (sm2) {
+            s_a[li] = ab;
+            s_t1[li] = ab - rs;
+          } else {
+            P.a[i] = ab;
+            P.phi1[i] = ab - rs;
+          }
+          res = fp_add(res, fp_sqr(rs));
+        },
+        [&](int j, float t) {
+          const int lj = j - k_lo;
+          const float cs = t - (sm2 ? s_q[lj] : __ldg(P.q + j));
+          const float ab = (sm2 ? s_b[lj] : P.b[j]) - cs;
+          if (sm2) {
+            s_b[lj] = ab;
+            s_t2[lj] = ab - cs;
+          } else {
+            P.b[j] = ab;
+            P.phi2[j] = ab - cs;
+          }
+          res = fp_add(res, fp_sqr(cs));
+        });
+    if (check) {
+      res = warp_sum_fp(res);
+      if (lane == 0) dscr[warp] = res;
+    }
+    __syncthreads();
+    {
+      const float gamma = s_misc_f[0];
+      for (int i = threadIdx.x; i < r_hi - r_lo; i += blockDim.x) {
+        const float t = sm2 ? s_t1[i] : __ldcg(P.phi1 + r_lo + i);
+        P.phi1[r_lo + i] = div_rn_by(t + gamma, nc_f, nc_rcp);
+      }
+      for (int j = threadIdx.x; j < k_hi - k_lo; j += blockDim.x) {
+        const float t = sm2 ? s_t2[j] : __ldcg(P.phi2 + k_lo + j);
+        P.phi2[k_lo + j] = div_rn_by(t + gamma, nr_f, nr_rcp);
+      }
+    }
+    if (check && warp == 0) {
+      fpair t = lane < W ? dscr[lane] : fp_make(0.0f);
+      t = warp_sum_fp(t);
+      if (lane == 0) P.cta_res[blockIdx.x] = make_float2(t.hi, t.lo);
+    }
+    last_sigma = s_misc_d[0];
+    if (with_c) obj_valid = 1;
+
+    stamp(3);
+    if (!grid_barrier(P, epoch, &s_flag)) { aborted = true; break; }
+
+    if (check) {
+      // One thread turns the squared residual into the decision; the square
+      // root is taken once, after the loop.
+      if (warp == 0) {
+        const fpair t = warp_sum_strided_fp(P.cta_res, G, lane);
+        if (lane == 0) {
+          const double r2 = fp_value(t);
+          s_misc_d[1] = r2;
+          s_stop = r2 < P.res2_stop ? 1 : 0;
+        }
+      }
+      __syncthreads();
+      last_res = s_misc_d[1];  // squared until the epilogue
+      if (s_stop) {
+        converged = true;
+        stamp(4);
+        break;
+      }
+    }
+    stamp(4);
   }
 
   // ------------------------------------------------------------ epilogue
@@ -1341,19 +1140,7 @@ drot_solve_kernel(const SolveParams P) {
     }
   }
   // Duals of this CTA's slice back to global memory (the state outputs).
-  if constexpr (LDU) {
-    __syncthreads();
-    if (chunk == 0)
-      for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-        P.a[i] = s_a[i - base];
-        P.phi1[i] = f1s[i - base];
-      }
-    if (band == 0)
-      for (int j = threadIdx.x; j < c1 - c0; j += blockDim.x) {
-        P.b[c0 + j] = s_b[j];
-        P.phi2[c0 + j] = s_t2[j];
-      }
-  } else if (P.p2_smem) {
+  if (P.p2_smem) {
     __syncthreads();
     for (int i = threadIdx.x; i < r_hi - r_lo; i += blockDim.x) P.a[r_lo + i] = s_a[i];
     for (int j = threadIdx.x; j < k_hi - k_lo; j += blockDim.x) P.b[k_lo + j] = s_b[j];
@@ -1361,7 +1148,7 @@ drot_solve_kernel(const SolveParams P) {
   // <C, X> of the last objective-bearing iteration: the CTA partials of that
   // iteration are the last ones written (visible since its barriers).
   if (blockIdx.x == 0 && warp == 0 && obj_valid && !aborted)
-    last_obj = fp_value(warp_sum_strided_fp((LDU && obj_par) ? P.cta_obj1 : P.cta_obj, G, lane));
+    last_obj = fp_value(warp_sum_strided_fp(P.cta_obj, G, lane));
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     DeviceStats* st = P.stats;
     st->iters_run = converged ? it + 1 : it;

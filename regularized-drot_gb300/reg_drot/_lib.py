@@ -63,7 +63,7 @@ class DrotAdjointInstance(ctypes.Structure):
         ("n_rows", ctypes.c_int), ("n_cols", ctypes.c_int), ("ld", ctypes.c_int),
         ("pad", ctypes.c_int), ("c_offset", ctypes.c_longlong), ("v_offset", ctypes.c_longlong),
         ("phi1_offset", ctypes.c_longlong), ("phi2_offset", ctypes.c_longlong),
-        ("step_size", ctypes.c_float), ("pad2", ctypes.c_float),
+        ("step_size", ctypes.c_float), ("lambda_", ctypes.c_float),
     ]
 
 
@@ -144,8 +144,11 @@ SIGNATURES = {
     "drot_qr_adjoint_workspace_bytes": (_c_size, [_c_int, _AIP]),
     "drot_qr_adjoint_prepare": (_c_int, [_c_int, _AIP, _vp, _c_int, _vp, _vp, _vp, _vp,
                                          _c_size, _vp]),
-    "drot_qr_adjoint_solve": (_c_int, [_c_int, _AIP, _vp, _vp, _c_float, _c_int, _vp, _c_size,
-                                       _ip, _vp]),
+    "drot_qr_adjoint_solve": (_c_int, [_c_int, _AIP, _vp, _vp, ctypes.c_double, _c_int, _vp,
+                                       _c_size, _ip, _vp]),
+    "drot_qr_adjoint_grad": (_c_int, [_c_int, _AIP, _vp, _vp, _vp, _vp, _vp, _vp, _c_size, _vp]),
+    "drot_qr_adjoint_residuals": (_c_int, [_c_int, _AIP, _vp, _c_size,
+                                           ctypes.POINTER(ctypes.c_double), _vp]),
     "drot_gl_adjoint_workspace_bytes": (_c_size, [_c_int, _c_int, _c_int]),
     "drot_gl_adjoint_step": (_c_int, [_vp, _c_int, _c_int, _c_int, _c_int, _c_float, _c_float,
                                       _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _c_size, _vp]),
@@ -155,6 +158,9 @@ SIGNATURES = {
                                          _vp]),
     "drot_sqeuclidean_cost": (_c_int, [_c_int, _CIP, _vp, _vp, _c_int, _c_float, _c_int, _vp,
                                        _vp]),
+    "drot_sqeuclidean_cost_grad_workspace_bytes": (_c_size, [_c_int, _CIP, _c_int]),
+    "drot_sqeuclidean_cost_grad": (_c_int, [_c_int, _CIP, _vp, _vp, _c_int, _c_float, _vp, _vp,
+                                            _vp, _vp, _vp, _c_size, _vp]),
 }
 
 _lib = None

@@ -18,8 +18,9 @@ lambda = (kappa - 1) / s (= r_weight * (n_rows + n_cols) with the operator's
 parameters, pytorch/src/qr_drot_cuda_kernel.cu:100-102): on the support S,
     dL/dC = (a_i + b_j - G_ij) / lambda,  dL/dp = a,  dL/dq = b,
 where [a; b] solves the masked Laplacian system built from the support
-(drot_qr_adjoint_prepare / _solve: bit-packed masks, Jacobi-preconditioned
-CG in one persistent launch).  The support is S = {phi1_i + phi2_j - s C_ij
+(drot_qr_adjoint_prepare / _solve / _grad: bit-packed masks, the right-hand
+side from the upstream gradient, Jacobi-preconditioned CG in FP64 in one
+persistent launch, and one kernel for dL/dC, dL/dp, dL/dq).  The support is S = {phi1_i + phi2_j - s C_ij
 > 0} from the solve's final duals: a finite solve leaves tiny, geometrically
 decaying positive entries of X off S, so X > 0 would overstate it.  a and b
 are unique up to a + t, b - t (the marginals' masses are tied) -- one such
@@ -37,7 +38,7 @@ import torch
 from ._lib import DrotAdjointInstance, check, lib
 
 C_F32, C_BF16 = 0, 1
-CG_TOL = 1e-7
+CG_TOL = 1e-10
 CG_MAX_ITERS = 5000
 
 f32 = np.float32
@@ -60,50 +61,66 @@ def step_and_kappa(rho, r_weight, n_rows, n_cols):
 
 
 class _Adjoint:
-    """Support masks + CG solve of one or more instances (drot_qr_adjoint_*)."""
+    """Support masks, CG solve and gradient assembly of one or more instances
+    (drot_qr_adjoint_prepare / _solve / _grad / _residuals)."""
 
-    def __init__(self, c, phi1, phi2, descs):
-        # descs: (n_rows, n_cols, ld, c_offset, v_offset, phi1_offset, phi2_offset, s)
+    def __init__(self, c, phi1, phi2, descs, byte_mask=False):
+        # descs: (n_rows, n_cols, ld, c_offset, v_offset, phi1_offset, phi2_offset, s, lambda)
         n = len(descs)
         self.n = n
         self.arr = (DrotAdjointInstance * n)()
-        for k, (nr, nc, ld, co, vo, o1, o2, st) in enumerate(descs):
+        self.nv = 0
+        for k, (nr, nc, ld, co, vo, o1, o2, st, lam) in enumerate(descs):
             d = self.arr[k]
             d.n_rows, d.n_cols, d.ld, d.c_offset, d.v_offset = nr, nc, ld, co, vo
-            d.phi1_offset, d.phi2_offset, d.step_size = o1, o2, st
+            d.phi1_offset, d.phi2_offset, d.step_size, d.lambda_ = o1, o2, st, lam
+            self.nv = max(self.nv, vo + nr + nc)
         self.device = c.device
+        self.mask = None
         with torch.cuda.device(c.device):
             self.nbytes = int(lib().drot_qr_adjoint_workspace_bytes(n, self.arr))
             if self.nbytes == 0:
                 raise RuntimeError("drot_qr_adjoint_workspace_bytes: unsupported shapes")
             self.ws = torch.empty(self.nbytes + 256, dtype=torch.uint8, device=c.device)
             self.ptr = self.ws.data_ptr() + (-self.ws.data_ptr()) % 256
-            self.mask = torch.zeros(c.shape, dtype=torch.uint8, device=c.device)
+            if byte_mask:
+                self.mask = torch.zeros(c.shape, dtype=torch.uint8, device=c.device)
             rc = lib().drot_qr_adjoint_prepare(
                 n, self.arr, c.data_ptr(), C_BF16 if c.dtype == torch.bfloat16 else C_F32,
-                phi1.data_ptr(), phi2.data_ptr(), self.mask.data_ptr(), self.ptr, self.nbytes,
-                torch.cuda.current_stream(c.device).cuda_stream)
+                phi1.data_ptr(), phi2.data_ptr(),
+                self.mask.data_ptr() if byte_mask else None, self.ptr, self.nbytes,
+                self._stream())
         check(rc, "qr_adjoint_prepare")
-        self.mask = self.mask.bool()
+        if byte_mask:
+            self.mask = self.mask.bool()
 
-    def solve(self, rhs, tol, max_iters):
-        z = torch.empty_like(rhs)
+    def _stream(self):
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def solve(self, g, tol, max_iters):
+        """z = [a; b] (FP64) of every instance for the upstream gradient g
+        (float32, layout of C); returns (z, CG iterations, final relative
+        residuals)."""
+        z = torch.empty(self.nv, dtype=torch.float64, device=self.device)
         iters = (ctypes.c_int * self.n)()
+        rel = (ctypes.c_double * self.n)()
         with torch.cuda.device(self.device):
-            rc = lib().drot_qr_adjoint_solve(self.n, self.arr, rhs.data_ptr(), z.data_ptr(),
+            rc = lib().drot_qr_adjoint_solve(self.n, self.arr, g.data_ptr(), z.data_ptr(),
                                              float(tol), int(max_iters), self.ptr, self.nbytes,
-                                             iters, torch.cuda.current_stream(self.device).cuda_stream)
-        check(rc, "qr_adjoint_solve")
-        return z, list(iters)
+                                             iters, self._stream())
+            check(rc, "qr_adjoint_solve")
+            rc = lib().drot_qr_adjoint_residuals(self.n, self.arr, self.ptr, self.nbytes, rel,
+                                                 self._stream())
+        check(rc, "qr_adjoint_residuals")
+        return z, list(iters), list(rel)
 
-
-def _grads_from_z(G, mask, a, b, lam):
-    """dL/dC (implicit part), dL/dp, dL/dq of one instance ([n_cols, n_rows] layout)."""
-    t = (b.sum() - a.sum()) / (a.numel() + b.numel())
-    a = a + t
-    b = b - t
-    gc = torch.where(mask, (a[None, :] + b[:, None] - G) / lam, torch.zeros((), device=G.device))
-    return gc, a, b
+    def grad(self, g, z, gc, gp, gq):
+        """dL/dC into gc (layout of C), dL/dp into gp, dL/dq into gq."""
+        with torch.cuda.device(self.device):
+            rc = lib().drot_qr_adjoint_grad(self.n, self.arr, g.data_ptr(), z.data_ptr(),
+                                            gc.data_ptr(), gp.data_ptr(), gq.data_ptr(),
+                                            self.ptr, self.nbytes, self._stream())
+        check(rc, "qr_adjoint_grad")
 
 
 class QuadraticDROTFn(torch.autograd.Function):
@@ -152,13 +169,15 @@ class QuadraticDROTFn(torch.autograd.Function):
         c, phi1, phi2 = ctx.saved_tensors
         nr, nc, s, lam = ctx.meta
         G = gx.detach().float().contiguous()
-        adj = _Adjoint(c.detach(), phi1, phi2, [(nr, nc, nr, 0, 0, 0, 0, s)])
-        Gm = G * adj.mask
-        rhs = torch.cat([Gm.sum(0), Gm.sum(1)]).contiguous()
-        z, iters = adj.solve(rhs, *ctx.cg)
+        adj = _Adjoint(c.detach(), phi1, phi2, [(nr, nc, nr, 0, 0, 0, 0, s, lam)])
+        z, iters, rel = adj.solve(G, *ctx.cg)
         ctx.cg_iters = iters
-        gc, a, b = _grads_from_z(G, adj.mask, z[:nr], z[nr:], lam)
-        return gc.to(c.dtype), a, b, None, None, None, None, None, None
+        ctx.cg_residuals = rel
+        gc = torch.empty(c.shape, dtype=torch.float32, device=c.device)
+        gp = torch.empty(nr, dtype=torch.float32, device=c.device)
+        gq = torch.empty(nc, dtype=torch.float32, device=c.device)
+        adj.grad(G, z, gc, gp, gq)
+        return gc.to(c.dtype), gp, gq, None, None, None, None, None, None
 
 
 def quadratic_drot_fn(c, p, q, rho, r_weight, max_iters, eps, *, cg_tol=CG_TOL,
@@ -196,29 +215,20 @@ class BatchQuadraticDROTFn(torch.autograd.Function):
         steps = B.step_sizes()
         descs, vo, prow, pcol = [], 0, 0, 0
         for k, (nr, nc) in enumerate(B.shapes):
-            descs.append((nr, nc, B.lds[k], B.offsets[k], vo, prow, pcol, steps[k]))
+            lam = (step_and_kappa(B.rho[k], B.r_weight[k], nr, nc)[1] - 1.0) / steps[k]
+            descs.append((nr, nc, B.lds[k], B.offsets[k], vo, prow, pcol, steps[k], lam))
             vo += nr + nc
             prow += nr
             pcol += nc
         adj = _Adjoint(c.detach(), phi1, phi2, descs)
-        rhs_parts = []
-        for k in range(B.n):
-            Gm = B.view(G, k) * B.view(adj.mask, k)
-            rhs_parts += [Gm.sum(0), Gm.sum(1)]
-        rhs = torch.cat(rhs_parts).contiguous()
-        z, iters = adj.solve(rhs, *ctx.cg)
+        z, iters, rel = adj.solve(G, *ctx.cg)
         ctx.cg_iters = iters
-        gc = torch.zeros_like(G)
-        gp, gq = [], []
-        for k, (nr, nc) in enumerate(B.shapes):
-            vo = descs[k][4]
-            lam = (step_and_kappa(B.rho[k], B.r_weight[k], nr, nc)[1] - 1.0) / steps[k]
-            g, a, b = _grads_from_z(B.view(G, k), B.view(adj.mask, k), z[vo:vo + nr],
-                                    z[vo + nr:vo + nr + nc], lam)
-            B.view(gc, k).copy_(g)
-            gp.append(a)
-            gq.append(b)
-        return gc.to(c.dtype), torch.cat(gp), torch.cat(gq), None, None, None, None, None
+        ctx.cg_residuals = rel
+        gc = torch.zeros_like(G)  # the padding rows of every block stay zero
+        gp = torch.empty(prow, dtype=torch.float32, device=G.device)
+        gq = torch.empty(pcol, dtype=torch.float32, device=G.device)
+        adj.grad(G, z, gc, gp, gq)
+        return gc.to(c.dtype), gp, gq, None, None, None, None, None
 
 
 def batch_quadratic_drot_fn(batch, c, p, q, max_iters, *, cg_tol=CG_TOL,
@@ -235,11 +245,20 @@ def batch_quadratic_drot_fn(batch, c, p, q, max_iters, *, cg_tol=CG_TOL,
                                       int(cg_max_iters), points)
 
 
-def gl_step_and_lambda(rho, r_weight, n_rows, n_cols, n_class):
-    """s and the group threshold of the GL operator (glr_drot_cuda_kernel.cu:255-257)."""
+def gl_step_and_lambda(rho, r_weight, n_rows, n_cols, n_class, convention="operator"):
+    """s and the group threshold lambda: the GL operator's r * sqrt(n_rows //
+    n_class) (pytorch/src/glr_drot_cuda_kernel.cu:255-257) or, with
+    convention="wrapper", the C++ wrapper's r / sqrt(n_rows // n_class)
+    (core/drot_glr.hpp:385), both rounded from FP64 to FP32."""
     import math
     s = f32(rho) / (f32(n_rows) + f32(n_cols))
-    lam = f32(float(f32(r_weight)) * math.sqrt(n_rows // n_class))
+    k = math.sqrt(n_rows // n_class)
+    if convention == "operator":
+        lam = f32(float(f32(r_weight)) * k)
+    elif convention == "wrapper":
+        lam = f32(float(f32(r_weight)) / k)
+    else:
+        raise RuntimeError("convention must be 'operator' or 'wrapper'")
     return float(s), float(lam)
 
 
@@ -299,24 +318,32 @@ class _GLState:
 
 class GroupLassoDROTFn(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, c, p, q, n_class, rho, r_weight, max_iters, eps, segment):
+    def forward(ctx, c, p, q, n_class, rho, r_weight, max_iters, eps, segment, convention,
+                last_k):
         from . import _check_input, _check_shapes
         _check_input(c, "c", allow_bf16=True)
         for t, n in ((p, "p"), (q, "q")):
             _check_input(t, n)
         nr, nc = _check_shapes(c, p, q)
-        s, lam = gl_step_and_lambda(rho, r_weight, nr, nc, n_class)
+        s, lam = gl_step_and_lambda(rho, r_weight, nr, nc, n_class, convention)
         st = _GLState(c.detach(), p.detach(), q.detach(), n_class, s, lam)
         st.warm_start()
-        checkpoints, T, info = [], 0, None
+        # Checkpoints (segment index, state); with last_k only the newest
+        # ceil(last_k / segment) + 1 are kept -- those the truncated backward reads.
+        keep = None if last_k is None else (last_k + segment - 1) // segment + 1
+        checkpoints, T, info, si = [], 0, None, 0
         while T < max_iters:
-            checkpoints.append(st.snapshot())
+            checkpoints.append((si, st.snapshot()))
+            if keep is not None and len(checkpoints) > keep:
+                checkpoints.pop(0)
             info = st.run(min(segment, max_iters - T), eps)
             T += info["iters_run"]
+            si += 1
             if info["converged"] or info["iters_run"] == 0:
                 break
         ctx.save_for_backward(c, p, q)
-        ctx.meta = (nr, nc, int(n_class), s, lam, int(segment), T)
+        t_lo = 0 if last_k is None else max(0, T - int(last_k))
+        ctx.meta = (nr, nc, int(n_class), s, lam, int(segment), T, t_lo)
         ctx.checkpoints = checkpoints
         ctx.info = dict(info, n_iter=T, iters_run=T)  # totals over the segments
         return st.t["x"].clone()
@@ -324,7 +351,7 @@ class GroupLassoDROTFn(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gx):
         c, p, q = ctx.saved_tensors
-        nr, nc, G, s, lam, seg, T = ctx.meta
+        nr, nc, G, s, lam, seg, T, t_lo = ctx.meta
         dev = c.device
         st = _GLState(c.detach(), p.detach(), q.detach(), G, s, lam)
         xbar = gx.detach().float().contiguous().clone()
@@ -341,10 +368,16 @@ class GroupLassoDROTFn(torch.autograd.Function):
         cdt = C_BF16 if c.dtype == torch.bfloat16 else C_F32
         states = torch.empty(seg * (nr * nc + nr + nc), device=dev)
         t = st.t
-        for si in reversed(range(len(ctx.checkpoints))):
+        for si, snap in reversed(ctx.checkpoints):
             k0 = si * seg
             k1 = min(k0 + seg, T)
-            st.restore(ctx.checkpoints[si])
+            if k1 <= t_lo:
+                break
+            st.restore(snap)
+            if k0 < t_lo:
+                # truncated adjoint: advance to its first iteration without it
+                st.run(t_lo - k0, -1.0)
+                k0 = t_lo
             with torch.cuda.device(dev):
                 rc = lib().drot_gl_adjoint_segment(
                     c.data_ptr(), cdt, p.data_ptr(), q.data_ptr(), nr, nc, G, s, lam,
@@ -353,16 +386,25 @@ class GroupLassoDROTFn(torch.autograd.Function):
                     st.wptr, st.nbytes, xbar.data_ptr(), vbar.data_ptr(), cbar.data_ptr(),
                     pbar.data_ptr(), qbar.data_ptr(), aptr, abytes, st.stream())
             check(rc, "gl_adjoint_segment")
-        return cbar.to(c.dtype), pbar, qbar, None, None, None, None, None, None
+        return cbar.to(c.dtype), pbar, qbar, None, None, None, None, None, None, None, None
 
 
-def group_lasso_drot_fn(c, p, q, n_class, rho, r_weight, max_iters, eps, *, segment=32):
+def group_lasso_drot_fn(c, p, q, n_class, rho, r_weight, max_iters, eps, *, segment=32,
+                        convention="operator", last_k=None):
     """reg_drot.group_lasso_drot with a backward: the unrolled adjoint of the
     iterations the solve ran, recomputed from checkpoints taken every
     ``segment`` iterations (memory: one state per segment plus ``segment``
-    plans during the backward)."""
+    plans during the backward).  last_k: unroll only the last last_k
+    iterations (the truncated adjoint: the gradient of the last last_k steps
+    with the state before them held fixed; memory: ceil(last_k / segment) + 1
+    states).  convention: "operator" (lambda = r_weight * sqrt(n_rows //
+    n_class), the PyTorch operator) or "wrapper" (r_weight / sqrt(n_rows //
+    n_class), the C++ wrapper)."""
+    if last_k is not None and int(last_k) <= 0:
+        raise RuntimeError("last_k must be positive")
     return GroupLassoDROTFn.apply(c, p, q, int(n_class), float(rho), float(r_weight),
-                                  int(max_iters), float(eps), int(segment))
+                                  int(max_iters), float(eps), int(segment), str(convention),
+                                  None if last_k is None else int(last_k))
 
 
 __all__ = ["quadratic_drot_fn", "batch_quadratic_drot_fn", "group_lasso_drot_fn", "qr_lambda",

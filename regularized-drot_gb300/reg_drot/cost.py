@@ -13,7 +13,8 @@ q over the y points), with autograd:
     dL/dx_i = 2 scale (x_i sum_j G'_ji - sum_j G'_ji y_j)
     dL/dy_j = 2 scale (y_j sum_i G'_ji - sum_i G'_ji x_i)
 
-(G' = dL/dC where C > 0; two FP32 cuBLAS GEMMs per instance).
+(G' = dL/dC where C > 0; drot_sqeuclidean_cost_grad: one pass over G' and C,
+FP32 sums in a fixed order).
 ``sqeuclidean_cost(x, y)`` builds one cost; ``packed_sqeuclidean_cost(batch,
 x_cat, y_cat)`` builds every instance of a QRBatch straight into its packed
 C buffer (x_cat, y_cat: the instances' points concatenated in order).
@@ -49,10 +50,27 @@ def _launch(descs, x, y, scale, clamp, c):
     check(rc, "sqeuclidean_cost")
 
 
-def _point_grads(G, x, y, scale):
-    """Chain rule of C = scale * (|x|^2 + |y|^2 - 2 x.y) for G = dL/dC ([n, m])."""
-    gx = 2.0 * scale * (x * G.sum(0)[:, None] - G.t() @ y)
-    gy = 2.0 * scale * (y * G.sum(1)[:, None] - G @ x)
+def _chain_rule(descs, x, y, scale, c, g, clamp):
+    """dL/dx, dL/dy of C = scale * max(|x|^2 + |y|^2 - 2 x.y, 0) for g = dL/dC
+    (the layout of c) through drot_sqeuclidean_cost_grad."""
+    n = len(descs)
+    arr = (DrotCostInstance * n)()
+    for k, (m, nn, ld, xo, yo, co) in enumerate(descs):
+        a = arr[k]
+        a.m, a.n, a.ld, a.x_offset, a.y_offset, a.c_offset = m, nn, ld, xo, yo, co
+    gx = torch.empty_like(x)
+    gy = torch.empty_like(y)
+    with torch.cuda.device(x.device):
+        nbytes = int(lib().drot_sqeuclidean_cost_grad_workspace_bytes(n, arr, x.size(1)))
+        if nbytes == 0:
+            raise RuntimeError("drot_sqeuclidean_cost_grad_workspace_bytes: invalid instances")
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=x.device)
+        rc = lib().drot_sqeuclidean_cost_grad(n, arr, x.data_ptr(), y.data_ptr(), x.size(1),
+                                              float(scale), c.data_ptr() if clamp else None,
+                                              g.data_ptr(), gx.data_ptr(), gy.data_ptr(),
+                                              ws.data_ptr(), nbytes,
+                                              torch.cuda.current_stream(x.device).cuda_stream)
+    check(rc, "sqeuclidean_cost_grad")
     return gx, gy
 
 
@@ -75,10 +93,9 @@ class SqEuclideanCostFn(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gc):
         x, y, c = ctx.saved_tensors
-        G = gc.float()
-        if ctx.clamp:
-            G = G * (c > 0)
-        gx, gy = _point_grads(G, x, y, ctx.scale)
+        m, n = x.size(0), y.size(0)
+        G = gc.float().contiguous()
+        gx, gy = _chain_rule([(m, n, m, 0, 0, 0)], x, y, ctx.scale, c, G, ctx.clamp)
         return gx, gy, None, None
 
 
@@ -111,17 +128,17 @@ class PackedSqEuclideanCostFn(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gc):
         x, y, c = ctx.saved_tensors
-        B = ctx.batch
-        G = gc.float()
+        G = gc.float().contiguous()
         gx = torch.empty_like(x)
         gy = torch.empty_like(y)
-        for k, (m, n, ld, xo, yo, co) in enumerate(ctx.descs):
-            Gk = B.view(G, k)
-            if ctx.clamp:
-                Gk = Gk * (B.view(c, k) > 0)
-            gxk, gyk = _point_grads(Gk, x[xo:xo + m], y[yo:yo + n], ctx.scale)
-            gx[xo:xo + m] = gxk
-            gy[yo:yo + n] = gyk
+        for s in range(0, len(ctx.descs), 256):
+            part = ctx.descs[s:s + 256]
+            gxs, gys = _chain_rule(part, x, y, ctx.scale, c, G, ctx.clamp)
+            # each call writes the rows of its own instances only
+            x0, x1 = part[0][3], part[-1][3] + part[-1][0]
+            y0, y1 = part[0][4], part[-1][4] + part[-1][1]
+            gx[x0:x1] = gxs[x0:x1]
+            gy[y0:y1] = gys[y0:y1]
         return gx, gy, None, None, None, None
 
 

@@ -24,7 +24,7 @@ output after ``max_iters = T - 1`` is the CUDA iterate after T iterations,
 and its primal residual log entry k is the CUDA residual of iteration k.
 
 Usage (in a container that has the reference checkout):
-    python tests/golden/gen_golden.py [/path/to/Regularized-DROT]
+    python tests/golden/gen_golden.py /path/to/Regularized-DROT
 writes tests/golden/npdrot_golden.npz.
 """
 import json
@@ -136,4 +136,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: gen_golden.py /path/to/Regularized-DROT (the reference checkout)")
+    main(sys.argv[1])

@@ -85,3 +85,19 @@ def test_support_from_duals_not_from_positive_entries():
     X = o["x"]
     assert (X[S] > 1e-9).all()
     assert (X[~S] < 1e-12).all()
+
+
+def test_sparse_adjoint_matches_dense_least_squares():
+    """The sparse FP64 CG form of the adjoint (used at sizes where the dense
+    least-squares system does not fit) gives the dense solution."""
+    rng = np.random.default_rng(12)
+    xs, yt = rng.normal(size=(90, 4)), rng.normal(size=(70, 4))
+    c = A.sqeuclidean(xs, yt)
+    c /= c.max()
+    p, q = rng.dirichlet(np.ones(90)), rng.dirichlet(np.ones(70))
+    o = A.solve64(c, p, q, 2.0, 1e-2)
+    _, gd, ad, bd = A.grads_at_state(o, c, 2.0, 1e-2, 0.3, sparse=False)
+    _, gs, as_, bs = A.grads_at_state(o, c, 2.0, 1e-2, 0.3, sparse=True)
+    assert np.abs(gs - gd).max() <= 1e-10 * np.abs(gd).max()
+    assert np.abs(as_ - ad).max() <= 1e-10 * np.abs(ad).max()
+    assert np.abs(bs - bd).max() <= 1e-10 * np.abs(bd).max()

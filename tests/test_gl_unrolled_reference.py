@@ -49,3 +49,31 @@ def test_unrolled_gradient_matches_finite_differences():
     fd = (L(c + h * E) - L(c - h * E)) / (2 * h)
     an = float((ct.grad.numpy() * E).sum())
     assert abs(fd - an) <= 1e-5 * max(1.0, abs(fd)), (fd, an)
+
+
+def test_truncated_unrolled_gradient_is_the_last_steps_gradient():
+    """gl_unrolled(last_k=K): the gradient of the last K steps from the state
+    they start at -- equal to differentiating a K-step run started at that
+    (detached) state; the forward value does not change."""
+    nr, nc, G, rw, T, K = 40, 30, 2, 1e-3, 25, 9
+    c, p, q = _problem(nr, nc, 6)
+    rng = np.random.default_rng(2)
+    W = torch.tensor(rng.normal(size=(nc, nr)))
+    ct = torch.tensor(c, requires_grad=True)
+    X = A.gl_unrolled(ct, torch.tensor(p), torch.tensor(q), G, 2.0, rw, T, last_k=K)
+    Xf = A.gl_unrolled(torch.tensor(c), torch.tensor(p), torch.tensor(q), G, 2.0, rw, T)
+    assert torch.equal(X.detach(), Xf)
+    (X * W).sum().backward()
+    # finite difference in C of the last K steps only: perturb C in those
+    # steps, keep the state at T - K from the unperturbed run
+    E = rng.normal(size=c.shape)
+    h = 1e-7
+
+    def L(eps_):
+        with torch.no_grad():
+            out = A.gl_unrolled(torch.tensor(c), torch.tensor(p), torch.tensor(q), G, 2.0, rw, T,
+                                last_k=K, c_last=torch.tensor(c + eps_ * E))
+        return float((out * W).sum())
+    fd = (L(h) - L(-h)) / (2 * h)
+    an = float((ct.grad.numpy() * E).sum())
+    assert abs(fd - an) <= 1e-5 * max(1.0, abs(fd)), (fd, an)

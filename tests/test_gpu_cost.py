@@ -6,7 +6,8 @@ Bound: the Gram term is split TF32 (hi.hi + hi.lo + lo.hi, FP32 accumulate),
 whose error is about 2^-22 |x_i||y_j| per product term; with FP32 norms the
 error of an entry stays below 4e-6 (|x_i|^2 + |y_j|^2) * scale -- a plain
 single-pass TF32 product would miss this bound by about three orders of
-magnitude.  Gradients (two FP32 GEMMs) against FP64 autograd: 1e-5 relative.
+magnitude.  Gradients (drot_sqeuclidean_cost_grad: FP32 sums in a fixed
+order) against FP64 autograd: 1e-5 relative.
 """
 import pytest
 
@@ -54,12 +55,15 @@ def test_cost_identical_points_and_no_clamp(cuda, solver_lib):
     assert bool((err <= _bound(x, x, 1.0)).all())
 
 
-def test_cost_backward_matches_fp64_autograd(cuda, solver_lib):
+@pytest.mark.parametrize("m,n,d", [(300, 257, 16), (301, 257, 8), (517, 64, 24), (129, 700, 32)])
+def test_cost_backward_matches_fp64_autograd(cuda, solver_lib, m, n, d):
+    """drot_sqeuclidean_cost_grad (hand-written chain rule) against FP64
+    autograd of the same formula; n_rows % 4 != 0 takes the scalar loads."""
     from reg_drot.cost import sqeuclidean_cost
-    g = torch.Generator(device=cuda).manual_seed(3)
-    x = torch.randn(300, 16, generator=g, device=cuda, requires_grad=True)
-    y = torch.randn(257, 16, generator=g, device=cuda, requires_grad=True)
-    G = torch.randn(257, 300, generator=g, device=cuda)
+    g = torch.Generator(device=cuda).manual_seed(3 + m)
+    x = torch.randn(m, d, generator=g, device=cuda, requires_grad=True)
+    y = torch.randn(n, d, generator=g, device=cuda, requires_grad=True)
+    G = torch.randn(n, m, generator=g, device=cuda)
     (sqeuclidean_cost(x, y, 0.25) * G).sum().backward()
     xd = x.detach().double().requires_grad_(True)
     yd = y.detach().double().requires_grad_(True)
@@ -86,6 +90,29 @@ def test_packed_cost_for_a_batch(cuda, solver_lib):
     for k in range(len(shapes)):
         B.view(mask, k).fill_(False)
     assert float(c[mask].abs().max()) == 0.0 and float(ref[mask].abs().max()) == 0.0
+
+
+def test_packed_cost_backward_for_a_batch(cuda, solver_lib):
+    from reg_drot.batch import QRBatch
+    from reg_drot.cost import packed_sqeuclidean_cost
+    shapes = [(64, 96), (300, 257), (513, 200), (7, 1100), (1030, 333)]
+    g = torch.Generator(device=cuda).manual_seed(19)
+    xc = torch.randn(sum(m for m, _ in shapes), 16, generator=g, device=cuda, requires_grad=True)
+    yc = torch.randn(sum(n for _, n in shapes), 16, generator=g, device=cuda, requires_grad=True)
+    B = QRBatch(shapes, 2.0, 1e-3, 1e-4, device=cuda, cols_per_tile=64)
+    c = packed_sqeuclidean_cost(B, xc, yc, 1.0 / 64)
+    G = torch.randn(c.shape, generator=g, device=cuda)
+    (c * G).sum().backward()
+    xo = yo = 0
+    for k, (m, n) in enumerate(shapes):
+        xd = xc[xo:xo + m].detach().double().requires_grad_(True)
+        yd = yc[yo:yo + n].detach().double().requires_grad_(True)
+        (_ref(xd, yd, 1.0 / 64) * B.view(G, k).double()).sum().backward()
+        for a, b in ((xc.grad[xo:xo + m], xd.grad), (yc.grad[yo:yo + n], yd.grad)):
+            rel = float((a.double() - b).norm() / b.norm())
+            assert rel <= 1e-5, (k, rel)
+        xo += m
+        yo += n
 
 
 def test_cost_rejects_bad_inputs(cuda, solver_lib):

@@ -39,11 +39,11 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
-def _reference(c, p, q, W, G, rw, T):
+def _reference(c, p, q, W, G, rw, T, convention="torch", last_k=None):
     ct = torch.tensor(c, dtype=torch.float64, requires_grad=True)
     pt = torch.tensor(p, dtype=torch.float64, requires_grad=True)
     qt = torch.tensor(q, dtype=torch.float64, requires_grad=True)
-    X = A.gl_unrolled(ct, pt, qt, G, 2.0, rw, T)
+    X = A.gl_unrolled(ct, pt, qt, G, 2.0, rw, T, convention=convention, last_k=last_k)
     (X * torch.tensor(W, dtype=torch.float64)).sum().backward()
     return X.detach().numpy(), ct.grad.numpy(), pt.grad.numpy(), qt.grad.numpy()
 
@@ -87,3 +87,26 @@ def test_gl_forward_equals_operator(cuda, solver_lib):
     x1 = reg_drot.group_lasso_drot(*args, 2, 2.0, 1e-3, 20000, 1e-4)
     x2 = group_lasso_drot_fn(*args, 2, 2.0, 1e-3, 20000, 1e-4, segment=7)
     assert torch.equal(x1, x2)
+
+
+@pytest.mark.parametrize("last_k,seg,conv", [(20, 8, "operator"), (33, 16, "wrapper"),
+                                             (64, 32, "wrapper")])
+def test_gl_truncated_adjoint_matches_fp64(cuda, solver_lib, last_k, seg, conv):
+    """The truncated adjoint (last_k iterations unrolled, the state before
+    them held fixed) against the FP64 unrolled map truncated the same way;
+    both lambda conventions (operator r * sqrt(n/G), C++ wrapper r / sqrt(n/G))."""
+    from reg_drot.autograd import group_lasso_drot_fn
+    nr, nc, G, rw, T = 300, 200, 2, 1e-3, 90
+    c, p, q, W = _problem(nr, nc, 17)
+    ct = torch.tensor(c, device=cuda, requires_grad=True)
+    pt = torch.tensor(p, device=cuda, requires_grad=True)
+    qt = torch.tensor(q, device=cuda, requires_grad=True)
+    x = group_lasso_drot_fn(ct, pt, qt, G, 2.0, rw, T, 0.0, segment=seg, convention=conv,
+                            last_k=last_k)
+    (x * torch.tensor(W, device=cuda)).sum().backward()
+    X64, gc, gp, gq = _reference(c, p, q, W, G, rw, T, "torch" if conv == "operator" else conv,
+                                 last_k)
+    assert _rel(x.detach().cpu().numpy(), X64) <= 1e-4
+    assert _rel(ct.grad.cpu().numpy(), gc) <= TOL, _rel(ct.grad.cpu().numpy(), gc)
+    assert _rel(pt.grad.cpu().numpy(), gp) <= TOL, _rel(pt.grad.cpu().numpy(), gp)
+    assert _rel(qt.grad.cpu().numpy(), gq) <= TOL, _rel(qt.grad.cpu().numpy(), gq)

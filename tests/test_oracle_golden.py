@@ -123,3 +123,28 @@ def test_oracle_thread_count_does_not_change_fp32_iterates_beyond_rounding():
     b = O.group_lasso_drot(C, p, q, 2, 2.0, 1e-2, 5000, 1e-4, threads=4)
     assert a["n_iter"] == b["n_iter"]
     assert np.abs(a["x"] - b["x"]).max() <= 1e-6 * np.abs(a["x"]).max()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_oracle_stopped_at_its_own_stop_is_the_converged_solve(dtype):
+    """quadratic_drot_at (the QR loop stopped as though the test passed at a
+    given even iteration) reproduces the loop's own converged result when
+    given the iteration the loop stopped at, bit for bit, and otherwise the
+    state a later stop would return."""
+    rng = np.random.default_rng(8)
+    nr, nc = 120, 70
+    C = (rng.random((nc, nr)) + 1e-3).astype(np.float32)
+    C /= C.max()
+    p = rng.dirichlet(np.ones(nr)).astype(np.float32)
+    q = rng.dirichlet(np.ones(nc)).astype(np.float32)
+    o = O.quadratic_drot(C, p, q, 2.0, 1e-2, 20000, 1e-4, dtype=dtype)
+    assert (o["n_iter"] - 1) % 2 == 0 and o["residual"] < 1e-4
+    a = O.quadratic_drot_at(C, p, q, 2.0, 1e-2, o["n_iter"], dtype=dtype)
+    assert np.array_equal(a["x"], o["x"])
+    assert a["objective"] == o["objective"] and a["residual"] == o["residual"]
+    assert a["n_iter"] == o["n_iter"]
+    assert O.quadratic_drot_matching(o["n_iter"], o, C, p, q, 2.0, 1e-2, dtype=dtype) is o
+    later = O.quadratic_drot_at(C, p, q, 2.0, 1e-2, o["n_iter"] + 2, dtype=dtype)
+    assert later["n_iter"] == o["n_iter"] + 2 and later["residual"] < o["residual"]
+    with pytest.raises(ValueError):
+        O.quadratic_drot_at(C, p, q, 2.0, 1e-2, o["n_iter"] + 1, dtype=dtype)

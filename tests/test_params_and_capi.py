@@ -190,5 +190,10 @@ def test_cost_and_adjoint_reject_bad_arguments_on_the_host(solver_lib):
     assert solver_lib.drot_sqeuclidean_cost(1, arr, 16, 16, 12, 1.0, 1, 16, None) == 4  # dim 12
     adj = (DrotAdjointInstance * 1)()
     adj[0].n_rows, adj[0].n_cols, adj[0].ld, adj[0].step_size = 10, 10, 9, 0.1
+    adj[0].lambda_ = 2.0
     assert solver_lib.drot_qr_adjoint_workspace_bytes(1, adj) == 0  # ld < n_rows
     assert solver_lib.drot_qr_adjoint_solve(1, adj, None, None, 1e-6, 10, None, 0, None, None) == 1
+    assert solver_lib.drot_qr_adjoint_grad(1, adj, None, None, None, None, None, None, 0,
+                                           None) == 1
+    adj[0].ld, adj[0].lambda_ = 10, 0.0
+    assert solver_lib.drot_qr_adjoint_workspace_bytes(1, adj) == 0  # lambda must be > 0

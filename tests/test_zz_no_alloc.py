@@ -12,7 +12,9 @@ The check: through the C ABI, two calls in a row on the same inputs give the
 result of drot_quadratic_drot (the reg_drot.quadratic_drot entry point) with
 its own workspace -- the same iteration count, and X and the objective within
 the parity tolerance used for the solver (1e-5 relative); the second call
-also shows that what the first left in the shared array does not leak in.
+also shows that what the first left in the shared array does not leak in,
+and that it changes neither torch's reserved pool nor the driver's free
+device memory (it allocates nothing).
 """
 import ctypes
 
@@ -44,12 +46,18 @@ def test_noalloc_matches_regular_entry_point_twice(cuda, solver_lib):
         x_ref, info_ref, _ = reg_drot.solve_qr(c, p, q, 2.0, 1e-3, 20000, eps)
         assert info_ref["converged"] == 1
         stream = torch.cuda.current_stream().cuda_stream
-        for call in range(2):
-            x = torch.full_like(c, float("nan"))
+        outs = [torch.full_like(c, float("nan")) for _ in range(2)]
+        mem = []
+        for call, x in enumerate(outs):
             res = DrotResult()
             rc = L.drot_quadratic_drot_noalloc(c.data_ptr(), p.data_ptr(), q.data_ptr(), nr, nc,
                                                2.0, 1e-3, 20000, eps, x.data_ptr(),
                                                ctypes.byref(res), stream)
+            torch.cuda.synchronize()
+            # Device memory after the call: torch's pool and the driver's free
+            # bytes.  The first call may load the library's device code; from
+            # then on a call must not change either.
+            mem.append((torch.cuda.memory_reserved(cuda), torch.cuda.mem_get_info(cuda)[0]))
             assert rc == 0, (call, rc)
             assert res.status == 0 and res.converged == 1
             assert res.n_iter == info_ref["n_iter"], (call, res.n_iter, info_ref["n_iter"])
@@ -57,6 +65,7 @@ def test_noalloc_matches_regular_entry_point_twice(cuda, solver_lib):
                         torch.linalg.norm(x_ref.double()))
             assert err <= 1e-5, (call, err)
             assert abs(res.objective - info_ref["objective"]) <= 1e-5 * abs(info_ref["objective"])
+        assert mem[1] == mem[0], mem
 
 
 def test_noalloc_rejects_problems_beyond_its_array(cuda, solver_lib):
