@@ -753,7 +753,7 @@ def run_gpu(args):
                 "x_update_10000": {"achieved": hbm["achieved_GBps"],
                                    "frac": hbm["achieved_GBps"] / peak,
                                    "us_per_iteration": hbm["us_per_iteration"]}}
-    e2e = e2e_point(step, xs, ys, min(args.steps, 5))
+    e2e = e2e_point(step, xs, ys, min(args.steps, 3))
     plain = plain_point(dev, shapes, xs, ys, eps, flush)
     extra = {"qr_3000": qr_3000_point(dev, flush), "hbm_point": hbm,
              "gl_da": gl_da_point(dev), "gl_da_weight_5e-3": gl_da_point(dev, 5e-3),
@@ -824,11 +824,25 @@ def run_diff_case(n_inst, iters):
     info = B.results()
     nbytes = solve_bytes(shapes, info)
     peak, _ = measured_peak()
+    # the cost kernel alone: C bytes written (4 per stored element) per call;
+    # each call also reads back its 4-byte status, inside the events
+    with torch.no_grad():
+        xd, yd = x.detach(), y.detach()
+        for _ in range(2):
+            packed_sqeuclidean_cost(B, xd, yd, DIFF_SCALE)
+        a.record()
+        for _ in range(5):
+            packed_sqeuclidean_cost(B, xd, yd, DIFF_SCALE)
+        b.record()
+        b.synchronize()
+    t_cost = a.elapsed_time(b) / 1e3 / 5
+    cost_bytes = 4 * sum(m * n for m, n in shapes)
     print(json.dumps({"case": f"diff:{n_inst}:{iters}", "elements": sum(m * n for m, n in shapes),
                       "cg_iters": X.grad_fn.cg_iters[:4], "solve_s": t,
                       "us_per_iteration": 1e6 * t / max(1, iters),
                       "achieved_GBps": nbytes / t / 1e9, "frac": nbytes / t / 1e9 / peak,
-                      "pf": os.environ.get("DROT_BATCH_PF", "0")}), flush=True)
+                      "cost_us": 1e6 * t_cost, "cost_GBps": cost_bytes / t_cost / 1e9,
+                      "cost_frac": cost_bytes / t_cost / 1e9 / peak}), flush=True)
     return 0
 
 
@@ -882,6 +896,9 @@ def run_batch_timeline(workload="config4"):
                      "active_elements_M": float(elems[it > lo].sum() / 1e6),
                      "us_per_iteration": float(np.nanmean(total[sl])),
                      "fused_update_us": float(np.mean(t[sl, 1] - t[sl, 0])),
+                     # even iterations read C (12 B / element), odd ones do not (8 B)
+                     "fused_update_even_us": float(np.mean((t[sl, 1] - t[sl, 0])[ev])),
+                     "fused_update_odd_us": float(np.mean((t[sl, 1] - t[sl, 0])[~ev])),
                      "barrier1_wait_us": float(np.mean(t[sl, 2] - t[sl, 1])),
                      "dual_update_us": float(np.mean(t[sl, 3] - t[sl, 2])),
                      "rest_even_us": float(np.nanmean(rest[sl][ev])),

@@ -82,6 +82,32 @@ int drot_gl_get_work_size_update_x(int n_rows, int n_cols);
  * the kernel choice of core/drot_glr.hpp:280). */
 int drot_gl_group_bounds(int n_rows, int n_groups, int *bounds);
 
+/* Launch shape of the single-instance solver (drot_*_solve and the entry
+ * points built on them).  Replaces the reference's columns-per-block
+ * heuristic (core/drot_qr.hpp:236-239) where a caller -- normally the
+ * autotuner reg_drot.tune, which times the candidates on the caller's data
+ * -- pins one; zero fields keep the planner's choice.
+ *   vectors_per_lane  QR: cap 1, 2 or 4 (128-bit vectors per lane: 128-,
+ *                     256- or 512-row bands); GL: 1, 2, 4 or 8
+ *   warps_per_cta     4..16 (default 8 on the register path, 16 on the ring)
+ *   data_path         0 register loads, 1 TMA bulk-copy ring (FP32 C with
+ *                     16-byte aligned columns; otherwise the register path
+ *                     runs with the other fields)
+ *   ctas_per_sm       ring only: 1 or 2 CTAs share an SM's shared memory */
+typedef struct {
+  int vectors_per_lane, warps_per_cta, data_path, ctas_per_sm;
+} drot_launch_choice;
+
+/* Pins `choice` for problems of mode (0 QR, 1 GL), shape n_rows x n_cols
+ * (n_groups for GL) and cost type c_dtype on the current device; n_rows =
+ * n_cols = 0 pins it for every shape of that mode and cost type without an
+ * exact entry.  choice == NULL removes the entry.  DROT_ERR_UNSUPPORTED
+ * when the shape cannot be planned with it.  Workspace sizes queried after
+ * the call include the pinned plan. */
+int drot_set_launch_choice(int mode, int n_rows, int n_cols, int n_groups, int c_dtype,
+                           const drot_launch_choice *choice);
+int drot_clear_launch_choices(void);
+
 /* Initial state.  warm != 0: the reference warm start (X = 0 and constant
  * phi1, phi2, a, b, alpha from step_size; core/drot_qr.hpp:321-346,
  * pytorch/src/qr_drot_cuda_kernel.cu:107-133).  warm == 0: the cold start
@@ -312,6 +338,42 @@ int drot_batch_plan_create(int n_inst, const drot_batch_instance *inst,
 int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance *inst,
                               int cols_per_tile, int band_rows,
                               drot_batch_plan *plan);
+/* Batched group-lasso solves (no counterpart in the reference, whose GL
+ * callers loop: core/multiexp_glr.cu).  Per instance: n_groups contiguous
+ * row classes with the reference's boundaries (drot_gl_group_bounds),
+ * lambda the shrink threshold (the lambda of drot_gl_solve: r_weight *
+ * sqrt(n_rows / n_groups) for the PyTorch operator, r_weight /
+ * sqrt(n_rows / n_groups) for the C++ wrapper), and the GL loop of
+ * drot_gl_solve per instance (core/drot_glr.hpp:242-355: stop on residual
+ * <= eps tested every iteration, n_iter = iterations run, X never folded).
+ * Groups of at most 4096 rows.  Launched with drot_qr_batch_launch like a
+ * QR plan (cost-matrix launches only). */
+typedef struct {
+  int n_rows, n_cols, ld, n_groups;
+  long long c_offset, x_offset, p_offset, q_offset;
+  float rho, lambda, eps, pad;
+} drot_gl_batch_instance;
+int drot_gl_batch_plan_create(int n_inst, const drot_gl_batch_instance *inst,
+                              int cols_per_tile, drot_batch_plan *plan);
+/* Tile-level shape of the batch plans created after the call (process-wide,
+ * no counterpart in the reference; NULL restores the defaults).  A field
+ * below 0 keeps its default:
+ *   fine_cols          128   columns of the second tile level's tiles
+ *   finest_cols         32   columns of the third level's tiles (0: no third level)
+ *   item_lines        1024   rows + columns per dual-update item
+ *   finest_item_lines   64   the same on the third level
+ *   level_quarters       8   fewer active tiles than level_quarters / 4 x the
+ *                            grid move the solve to the next finer level
+ *                            (0: stay on the coarse tiles)
+ *   prefetch_distance    1   L2 prefetch of the fused update, warp steps
+ *                            ahead (0..8; 0: off)
+ * Tuning changes the schedule, not the arithmetic of an instance: every
+ * setting gives the same iterates up to summation order. */
+typedef struct {
+  int fine_cols, finest_cols, item_lines, finest_item_lines, level_quarters,
+      prefetch_distance;
+} drot_batch_tuning;
+int drot_batch_set_tuning(const drot_batch_tuning *tuning);
 void drot_batch_plan_destroy(drot_batch_plan plan);
 /* Workspace bytes of a plan (device memory, 256-byte aligned). */
 size_t drot_batch_plan_workspace_bytes(drot_batch_plan plan);
@@ -358,6 +420,13 @@ int drot_batch_results(drot_batch_plan plan, const void *workspace,
  * entries start at the sum of the earlier instances' n_rows / n_cols. */
 int drot_batch_state(drot_batch_plan plan, void *workspace, float **phi1,
                      float **phi2);
+/* The whole final state inside a launched workspace (device pointers): a,
+ * phi1 (rows), b, phi2 (columns), packed as in drot_batch_state, and alpha
+ * [2][n_inst] by iteration parity -- instance k's final alpha is
+ * alpha[(iters_run & 1) * n_inst + k].  With the plans X this is the state a
+ * single-instance solve (drot_qr_solve / drot_gl_solve) continues from. */
+int drot_batch_state_ex(drot_batch_plan plan, void *workspace, float **a, float **b,
+                        float **phi1, float **phi2, float **alpha);
 
 /* ---------------------------------------------------------------------------
  * Implicit adjoint of the quadratic-regularised plan (autograd backward)

@@ -139,7 +139,7 @@ def point_grads(xs, yt, gc):
 
 
 def gl_unrolled(c, p, q, n_class, rho, r_weight, iters, norm_eps=1e-9, convention="torch",
-                last_k=None, c_last=None):
+                last_k=None, c_last=None, state=None, lam=None):
     """X after `iters` GL iterations from the warm start, in FP64 torch (CPU)
     so that autograd gives the exact gradient of the unrolled map.  Restates
     the oracle's GL loop (oracle_gl_solve: core/drot_glr.hpp:242-355,
@@ -149,21 +149,29 @@ def gl_unrolled(c, p, q, n_class, rho, r_weight, iters, norm_eps=1e-9, conventio
     iters - last_k iterations run without autograd, so the gradient is that
     of the last last_k steps with the state before them held fixed (the
     truncated unrolled adjoint); c_last, if given, is the cost those last
-    steps use (c the earlier ones).  c, p, q: torch float64 tensors
-    ([n_cols, n_rows], [n_rows], [n_cols])."""
+    steps use (c the earlier ones).  state: start there (a dict of x, a, b,
+    phi1, phi2, alpha tensors, held fixed) instead of the warm start; lam:
+    the threshold itself instead of the convention's.  c, p, q: torch
+    float64 tensors ([n_cols, n_rows], [n_rows], [n_cols])."""
     import torch
     nc, nr = c.shape
     s = O.step_size(rho, nr, nc)
-    lam = O.gl_lambda(r_weight, nr, n_class, convention)
+    if lam is None:
+        lam = O.gl_lambda(r_weight, nr, n_class, convention)
     w = O.warm_start(s, nr, nc)
     bounds = [int(v) for v in O.group_bounds(nr, n_class)]
     f64 = dict(dtype=torch.float64)
-    X = torch.zeros(nc, nr, **f64)
-    phi1 = torch.full((nr,), float(w["phi1"]), **f64)
-    phi2 = torch.full((nc,), float(w["phi2"]), **f64)
-    a = torch.full((nr,), float(w["a"]), **f64)
-    b = torch.full((nc,), float(w["b"]), **f64)
-    alpha = torch.tensor(float(w["alpha"]), **f64)
+    if state is None:
+        X = torch.zeros(nc, nr, **f64)
+        phi1 = torch.full((nr,), float(w["phi1"]), **f64)
+        phi2 = torch.full((nc,), float(w["phi2"]), **f64)
+        a = torch.full((nr,), float(w["a"]), **f64)
+        b = torch.full((nc,), float(w["b"]), **f64)
+        alpha = torch.tensor(float(w["alpha"]), **f64)
+    else:
+        X, phi1, phi2, a, b = (torch.as_tensor(state[k], **f64).detach().clone()
+                               for k in ("x", "phi1", "phi2", "a", "b"))
+        alpha = torch.as_tensor(state["alpha"], **f64).detach().reshape(())
     t_free = iters - last_k if last_k is not None else 0
     for it in range(iters):
         if it == t_free and last_k is not None:

@@ -154,24 +154,22 @@ static int occupancy(SolveFn fn, int threads, size_t smem) {
   return nb;
 }
 
-// Warps per CTA on the TMA path (DROT_TMA_WARPS, 4..16, default 16).
-static int tma_warps() {
-  const char* e = getenv("DROT_TMA_WARPS");
-  const int w = e ? atoi(e) : 0;
-  return (w >= 4 && w <= 16) ? w : 16;
-}
-
-// Warps per CTA on the register path (DROT_REG_WARPS, 4..16, default 8).
-static int reg_warps() {
-  const char* e = getenv("DROT_REG_WARPS");
-  const int w = e ? atoi(e) : 0;
-  return (w >= 4 && w <= 16) ? w : 8;
-}
+// Launch shape pinned for a problem shape (drot_set_launch_choice, set by
+// the autotuner); zero fields leave the planner's own choice.
+struct LaunchChoice {
+  int kv = 0;     // vectors per lane (QR: cap 1, 2, 4; GL: 1, 2, 4, 8)
+  int warps = 0;  // warps per CTA, 4..16
+  int tma = 0;    // 1: TMA bulk-copy ring (FP32 C, 16-byte aligned columns)
+  int ctas = 0;   // TMA ring: CTAs per SM sharing its shared memory (1 or 2)
+  bool operator==(const LaunchChoice& o) const {
+    return kv == o.kv && warps == o.warps && tma == o.tma && ctas == o.ctas;
+  }
+};
 
 // Build the launch plan for one data path (tma: shared-memory TMA ring, else
 // register loads).  Returns a drot_status.
 static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma, int ctype,
-                              Plan& pl, const int* ubounds) {
+                              Plan& pl, const int* ubounds, const LaunchChoice& ch) {
   if (nr <= 0 || nc <= 0) return DROT_ERR_INVALID_ARG;
   if (tma && vec != 4) return DROT_ERR_UNSUPPORTED;
   const DeviceInfo dev = device_info();
@@ -185,12 +183,9 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
     // Four 128-bit vectors per lane (512-row sub-bands); short panels use
     // fewer so lanes are not left idle.
     pl.kv = nr <= SV ? 1 : (nr <= 2 * SV ? 2 : 4);
-    // DROT_QR_KV (1, 2 or 4) caps the vectors per lane: shorter bands, fewer
-    // registers per thread, more CTAs per SM (tuning knob).
-    if (const char* e = getenv("DROT_QR_KV")) {
-      const int k = atoi(e);
-      if (k == 1 || k == 2 || k == 4) pl.kv = std::min(pl.kv, k);
-    }
+    // A pinned choice caps the vectors per lane: shorter bands, fewer
+    // registers per thread, more CTAs per SM.
+    if (ch.kv == 1 || ch.kv == 2 || ch.kv == 4) pl.kv = std::min(pl.kv, ch.kv);
     pl.wt = 1;
   } else {
     if (G <= 0) return DROT_ERR_INVALID_ARG;
@@ -206,13 +201,9 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
     }
     hmax = std::max(hmax, 1);
     // Vectors per lane: the smallest that covers a group in one warp, up to
-    // a cap (DROT_GL_KV, 1/2/4/8, default 8); taller groups use teams of
-    // warps.
-    int kvcap = 8;
-    if (const char* e = getenv("DROT_GL_KV")) {
-      const int k = atoi(e);
-      if (k == 1 || k == 2 || k == 4 || k == 8) kvcap = k;
-    }
+    // a cap (a pinned choice, else 8); taller groups use teams of warps.
+    const bool kv_pinned = ch.kv == 1 || ch.kv == 2 || ch.kv == 4 || ch.kv == 8;
+    int kvcap = kv_pinned ? ch.kv : 8;
     pl.kv = 0;
     for (int kv : {1, 2, 4, 8})
       if (kv <= kvcap && SV * kv >= hmax) { pl.kv = kv; break; }
@@ -220,7 +211,7 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
       // Groups taller than one warp covers: teams of 4-vector warps (the
       // 8-vector kernel spills at the register cap; measured at 3000^2 with
       // two 1500-row groups: 26.7 us per iteration against 31.8).
-      if (!getenv("DROT_GL_KV")) kvcap = std::min(kvcap, 4);
+      if (!kv_pinned) kvcap = std::min(kvcap, 4);
       pl.kv = kvcap;
       pl.wt = (hmax + kvcap * SV - 1) / (kvcap * SV);
       if (pl.wt > 16) return DROT_ERR_UNSUPPORTED;
@@ -232,14 +223,14 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
   SolveFn fn = kernel_for(mode, vec, pl.kv, tma, ctype);
   if (!fn) return DROT_ERR_UNSUPPORTED;
   pl.ctype = ctype;
-  // TMA ring: DROT_TMA_CTAS (1 or 2) CTAs per SM share the shared memory.
-  const int tma_ctas = tma ? std::max(1, std::min(2, getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1)) : 1;
+  // TMA ring: 1 (default) or 2 CTAs per SM share the shared memory.
+  const int tma_ctas = tma ? std::max(1, std::min(2, ch.ctas > 0 ? ch.ctas : 1)) : 1;
   const size_t budget = (size_t)std::max(dev.smem_optin, 48 * 1024) / tma_ctas - 1024;
 
   // Warps per CTA: 8 on the register path (two CTAs per SM), up to 16 when
   // a band needs teams of 3 or more warps (fewer CTAs per band keeps the
   // phase-2 partial count down).
-  const int wtarget = tma ? tma_warps() : reg_warps();
+  const int wtarget = (ch.warps >= 4 && ch.warps <= 16) ? ch.warps : (tma ? 16 : 8);
   for (int attempt = 0; attempt < 8; ++attempt) {
     const int wcap = (!tma && pl.wt >= 3) ? 16 : wtarget;
     int teams = pl.wt >= wcap ? 1 : std::max(1, wcap / pl.wt);
@@ -338,13 +329,12 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
 // Plans are cached per (device, mode, shape, path): planning queries the
 // occupancy calculator, which costs microseconds per call.
 struct PlanKey {
-  int dev, mode, nr, nc, G, vec, tma, warps, ctas, ctype;
+  int dev, mode, nr, nc, G, vec, tma, ctype;
   std::vector<int> ubounds;  // caller's GL group boundaries (empty: the reference's)
-  int qr_kv;                 // DROT_QR_KV and DROT_GL_KV knobs
+  LaunchChoice ch;
   bool operator==(const PlanKey& o) const {
     return dev == o.dev && mode == o.mode && nr == o.nr && nc == o.nc && G == o.G &&
-           vec == o.vec && tma == o.tma && warps == o.warps && ctas == o.ctas &&
-           ctype == o.ctype && ubounds == o.ubounds && qr_kv == o.qr_kv;
+           vec == o.vec && tma == o.tma && ctype == o.ctype && ubounds == o.ubounds && ch == o.ch;
   }
 };
 
@@ -352,14 +342,11 @@ static std::mutex g_plan_mu;
 static std::vector<std::pair<PlanKey, Plan>> g_plans;
 
 static int make_plan(int mode, int nr, int nc, int G, int vec, bool tma, Plan& pl,
-                     int ctype = DROT_C_F32, const int* ubounds = nullptr) {
+                     int ctype = DROT_C_F32, const int* ubounds = nullptr,
+                     const LaunchChoice& ch = LaunchChoice()) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return DROT_ERR_CUDA;
-  PlanKey key = {dev, mode, nr, nc, mode == MODE_GL ? G : 0, vec, tma ? 1 : 0,
-                 tma ? tma_warps() : reg_warps(),
-                 tma && getenv("DROT_TMA_CTAS") ? atoi(getenv("DROT_TMA_CTAS")) : 1, ctype, {},
-                 (getenv("DROT_QR_KV") ? atoi(getenv("DROT_QR_KV")) : 0) +
-                     16 * (getenv("DROT_GL_KV") ? atoi(getenv("DROT_GL_KV")) : 0)};
+  PlanKey key = {dev, mode, nr, nc, mode == MODE_GL ? G : 0, vec, tma ? 1 : 0, ctype, {}, ch};
   if (mode == MODE_GL && ubounds) key.ubounds.assign(ubounds, ubounds + G + 1);
   {
     std::lock_guard<std::mutex> lk(g_plan_mu);
@@ -367,7 +354,7 @@ static int make_plan(int mode, int nr, int nc, int G, int vec, bool tma, Plan& p
       if (e.first == key) { pl = e.second; return DROT_OK; }
   }
   const int rc = make_plan_uncached(mode, nr, nc, G, vec, tma, ctype, pl,
-                                    mode == MODE_GL ? ubounds : nullptr);
+                                    mode == MODE_GL ? ubounds : nullptr, ch);
   if (rc == DROT_OK) {
     std::lock_guard<std::mutex> lk(g_plan_mu);
     if (g_plans.size() >= 64) g_plans.erase(g_plans.begin());
@@ -376,29 +363,51 @@ static int make_plan(int mode, int nr, int nc, int G, int vec, bool tma, Plan& p
   return rc;
 }
 
-// Data path override for tests and measurements: DROT_PATH=reg forces the
-// register path, DROT_PATH=tma requires the TMA ring.
-static int path_override() {
-  const char* e = getenv("DROT_PATH");
-  if (!e) return 0;
-  if (!strcmp(e, "reg")) return 1;
-  if (!strcmp(e, "tma")) return 2;
-  return 0;
+// Pinned launch choices per (device, mode, shape, cost type); a key with
+// n_rows = n_cols = 0 applies to every shape of its mode and cost type that
+// has no exact entry.
+struct ChoiceKey {
+  int dev, mode, nr, nc, G, ctype;
+  bool operator==(const ChoiceKey& o) const {
+    return dev == o.dev && mode == o.mode && nr == o.nr && nc == o.nc && G == o.G &&
+           ctype == o.ctype;
+  }
+};
+
+static std::mutex g_choice_mu;
+static std::vector<std::pair<ChoiceKey, LaunchChoice>> g_choices;
+
+static LaunchChoice find_choice(int mode, int nr, int nc, int G, int ctype) {
+  int dev = 0;
+  LaunchChoice ch;
+  if (cudaGetDevice(&dev) != cudaSuccess) return ch;
+  const ChoiceKey exact = {dev, mode, nr, nc, mode == MODE_GL ? G : 0, ctype};
+  const ChoiceKey any = {dev, mode, 0, 0, 0, ctype};
+  std::lock_guard<std::mutex> lk(g_choice_mu);
+  bool found = false;
+  for (auto& e : g_choices) {
+    if (e.first == exact) return e.second;
+    if (!found && e.first == any) {
+      ch = e.second;
+      found = true;
+    }
+  }
+  return ch;
 }
 
 // Plan for the given alignment.  The register path is the default: on this
 // part the fused update is bound by per-warp instruction latency, and two
 // 8-warp CTAs per SM with register-resident segments beat one 16-warp CTA
-// fed by the shared-memory TMA ring.  DROT_PATH=tma selects the ring.
-
+// fed by the shared-memory TMA ring.  A pinned choice can select the ring
+// (used when C is FP32 and the columns are 16-byte aligned, else the
+// register path runs with the choice's other fields).
 static int choose_plan(int mode, int nr, int nc, int G, bool aligned4, Plan& pl,
                        int ctype = DROT_C_F32, const int* ubounds = nullptr) {
-  const int ov = path_override();
-  if (ov == 2 && ctype == DROT_C_F32) {
-    if (!aligned4) return DROT_ERR_UNSUPPORTED;
-    return make_plan(mode, nr, nc, G, 4, true, pl, DROT_C_F32, ubounds);
-  }
-  return make_plan(mode, nr, nc, G, aligned4 ? 4 : 1, false, pl, ctype, ubounds);
+  const LaunchChoice ch = find_choice(mode, nr, nc, G, ctype);
+  if (ch.tma && aligned4 && ctype == DROT_C_F32 &&
+      make_plan(mode, nr, nc, G, 4, true, pl, DROT_C_F32, ubounds, ch) == DROT_OK)
+    return DROT_OK;
+  return make_plan(mode, nr, nc, G, aligned4 ? 4 : 1, false, pl, ctype, ubounds, ch);
 }
 
 static size_t scratch_bytes(int mode, int nr, int nc, int G, const int* ubounds = nullptr) {
@@ -410,6 +419,17 @@ static size_t scratch_bytes(int mode, int nr, int nc, int G, const int* ubounds 
     best = std::max(best, pl.total);
   if (make_plan(mode, nr, nc, G, 1, false, pl, DROT_C_F32, ubounds) == DROT_OK)
     best = std::max(best, pl.total);
+  // pinned choices (either cost type) may plan more partials
+  for (int ctype : {DROT_C_F32, DROT_C_BF16}) {
+    const LaunchChoice ch = find_choice(mode, nr, nc, G, ctype);
+    if (ch == LaunchChoice()) continue;
+    for (int v : {4, 1})
+      if (make_plan(mode, nr, nc, G, v, false, pl, ctype, ubounds, ch) == DROT_OK)
+        best = std::max(best, pl.total);
+    if (ch.tma && ctype == DROT_C_F32 &&
+        make_plan(mode, nr, nc, G, 4, true, pl, ctype, ubounds, ch) == DROT_OK)
+      best = std::max(best, pl.total);
+  }
   return best;
 }
 
@@ -632,6 +652,55 @@ int drot_gl_get_work_size_update_x(int n_rows, int n_cols) {
 int drot_gl_group_bounds(int n_rows, int n_groups, int* bounds) {
   if (n_rows <= 0 || n_groups <= 0 || !bounds) return DROT_ERR_INVALID_ARG;
   group_bounds(n_rows, n_groups, bounds);
+  return DROT_OK;
+}
+
+int drot_set_launch_choice(int mode, int n_rows, int n_cols, int n_groups, int c_dtype,
+                           const drot_launch_choice* choice) {
+  if ((mode != MODE_QR && mode != MODE_GL) || n_rows < 0 || n_cols < 0 ||
+      (n_rows == 0) != (n_cols == 0) || (mode == MODE_GL && n_rows > 0 && n_groups <= 0) ||
+      (c_dtype != DROT_C_F32 && c_dtype != DROT_C_BF16))
+    return DROT_ERR_INVALID_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return DROT_ERR_CUDA;
+  const ChoiceKey key = {dev, mode, n_rows, n_cols, (mode == MODE_GL && n_rows > 0) ? n_groups : 0,
+                         c_dtype};
+  LaunchChoice ch;
+  if (choice) {
+    const drot_launch_choice& c = *choice;
+    const bool kv_ok = c.vectors_per_lane == 0 || c.vectors_per_lane == 1 ||
+                       c.vectors_per_lane == 2 || c.vectors_per_lane == 4 ||
+                       (mode == MODE_GL && c.vectors_per_lane == 8);
+    if (!kv_ok || (c.warps_per_cta != 0 && (c.warps_per_cta < 4 || c.warps_per_cta > 16)) ||
+        (c.data_path != 0 && c.data_path != 1) || c.ctas_per_sm < 0 || c.ctas_per_sm > 2)
+      return DROT_ERR_INVALID_ARG;
+    ch.kv = c.vectors_per_lane;
+    ch.warps = c.warps_per_cta;
+    ch.tma = c.data_path;
+    ch.ctas = c.ctas_per_sm;
+    if (n_rows > 0) {
+      // the pinned shape must plan (on the path it names, when it can run there)
+      Plan pl;
+      int rc = make_plan(mode, n_rows, n_cols, n_groups, 4, ch.tma != 0, pl, c_dtype, nullptr,
+                         ch);
+      if (rc != DROT_OK && ch.tma) rc = make_plan(mode, n_rows, n_cols, n_groups, 4, false, pl,
+                                                  c_dtype, nullptr, ch);
+      if (rc != DROT_OK) return rc;
+    }
+  }
+  std::lock_guard<std::mutex> lk(g_choice_mu);
+  for (size_t k = 0; k < g_choices.size(); ++k)
+    if (g_choices[k].first == key) {
+      g_choices.erase(g_choices.begin() + k);
+      break;
+    }
+  if (choice) g_choices.emplace_back(key, ch);
+  return DROT_OK;
+}
+
+int drot_clear_launch_choices(void) {
+  std::lock_guard<std::mutex> lk(g_choice_mu);
+  g_choices.clear();
   return DROT_OK;
 }
 

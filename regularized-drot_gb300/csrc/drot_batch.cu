@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <new>
 #include <type_traits>
 #include <vector>
@@ -47,7 +48,7 @@ struct BatchInst {
   int row_off, col_off;                  // its rows / columns in the packed state arrays
   float s, kappa, kappa_rcp, eps, nc_rcp, nr_rcp;
   float w_phi1, w_phi2, w_a, w_b, w_alpha;  // warm-start constants
-  int pad;
+  float lambda;      // GL plans: the group threshold of the shrink
   double res2_stop;  // converged when the squared residual is below this (res2_threshold)
 };
 
@@ -103,6 +104,7 @@ struct BatchParams {
   int* abort_flag;
   long long timeout_ns;
   int stall_cta;       // test hook of the bounded waits (grid_barrier); -1 off
+  int band_cover;      // GL plans: rows of shared staging per band (>= every group's cover)
   int pf_dist;         // L2 prefetch distance of the fused update, in warp steps (0 off)
   // Optional profile of CTA 0 for iterations it < iter_log_cap: globaltimer
   // at the start of the iteration, after its fused-update tiles, after the
@@ -384,6 +386,120 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
   }
 }
 
+// GL tile: the band is one group [lo, hi) of the instance (the rows of one
+// class, any height up to the plan's band cover), columns [c0, c1).  A warp
+// takes one column at a time.  Pass A walks the group in 512-row steps (four
+// 128-bit vectors per lane, all loads issued first): y = max((X + phi1) +
+// phi2 - sC, 0) (kernel_glr.hpp:163-305), stored back, and the float sum of
+// y^2 -- the group norm, a float sum as the reference's atomics make it.
+// The shrink factor max(1 - lambda / (||y|| + 1e-9), 0) follows
+// (kernel_glr.hpp:307-326).  Pass B re-reads the column's y and C -- just
+// touched, so from L2 -- stores X = y * scale and adds the column, row
+// (per-warp shared row partials wred[row - base]), mass and objective sums.
+// DRAM traffic stays 12 bytes per element, as in the single-pass update.
+// Stores the vector of rows r..r+3 that lie inside [lo, hi); a vector that
+// straddles a group boundary is stored element by element (the rows of the
+// neighbouring group belong to another tile, possibly in flight).
+__device__ __forceinline__ void gl_store(float* xcol, int r, int lo, int hi, const float (&v)[4]) {
+  if (r >= lo && r + 4 <= hi) {
+    store_vec<4>(xcol + r, v);
+  } else {
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (r + e >= lo && r + e < hi) xcol[r + e] = v[e];
+  }
+}
+
+template <typename CT>
+__device__ __forceinline__ void batch_gl_tile_columns(const BatchParams& P, const BatchInst& I,
+                                                      const BatchTile& T, const float* f1s,
+                                                      float* wred, float& ms_hi, float& ms_lo,
+                                                      float& ob_hi, float& ob_lo, int lane,
+                                                      int warp, int W) {
+  constexpr int VEC = 4;
+  const CT* const cbase = reinterpret_cast<const CT*>(P.c);
+  const int lo = T.lo, hi = T.hi, base = lo & ~3;
+  const int nsub = (hi - base + 511) / 512;
+  const float s = I.s;
+  for (int j = T.c0 + warp; j < T.c1; j += W) {
+    const float f2 = __ldcg(P.phi2 + I.col_off + j);
+    float* xcol = P.x + I.x_off + (long long)j * I.ld;
+    const CT* ccol = cbase + I.c_off + (long long)j * I.ld;
+    float nsl = 0.0f;
+    for (int sb = 0; sb < nsub; ++sb) {
+      float xv[4][VEC], cv[4][VEC];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int r = base + sb * 512 + v * 128 + lane * VEC;
+        if (r < hi) {
+          load_vec<VEC>(xcol + r, xv[v]);
+          load_c<VEC, CT>(ccol + r, cv[v]);
+        } else {
+#pragma unroll
+          for (int e = 0; e < VEC; ++e) { xv[v][e] = 0.0f; cv[v][e] = 0.0f; }
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int r = base + sb * 512 + v * 128 + lane * VEC;
+        if (r >= hi) continue;
+        const int li = r - base;
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+          const bool ok = r + e >= lo && r + e < hi;
+          const float t = fmaf(-s, cv[v][e], (xv[v][e] + f1s[li + e]) + f2);
+          const float y = ok ? fmaxf(t, 0.0f) : 0.0f;
+          xv[v][e] = y;
+          nsl = fmaf(y, y, nsl);
+        }
+        gl_store(xcol, r, lo, hi, xv[v]);
+      }
+    }
+    nsl = warp_sum(nsl);
+    const float scale = gl_shrink(nsl, I.lambda);
+    float colp = 0.0f, objp = 0.0f;
+    for (int sb = 0; sb < nsub; ++sb) {
+      float xv[4][VEC], cv[4][VEC];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int r = base + sb * 512 + v * 128 + lane * VEC;
+        if (r < hi) {
+          load_vec<VEC>(xcol + r, xv[v]);
+          load_c<VEC, CT>(ccol + r, cv[v]);
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int r = base + sb * 512 + v * 128 + lane * VEC;
+        if (r >= hi) continue;
+        const int li = r - base;
+        float4 acc = *reinterpret_cast<float4*>(wred + li);
+        float* ap = reinterpret_cast<float*>(&acc);
+#pragma unroll
+        for (int e = 0; e < VEC; ++e) {
+          const bool ok = r + e >= lo && r + e < hi;
+          const float xn = xv[v][e] * scale;
+          if (ok) {
+            xv[v][e] = xn;
+            ap[e] += xn;
+            colp += xn;
+            objp = fmaf(xn, cv[v][e], objp);
+          }
+        }
+        *reinterpret_cast<float4*>(wred + li) = acc;
+        gl_store(xcol, r, lo, hi, xv[v]);
+      }
+    }
+    float e1;
+    two_sum(ms_hi, colp, ms_hi, e1);
+    ms_lo += e1;
+    two_sum(ob_hi, objp, ob_hi, e1);
+    ob_lo += e1;
+    colp = warp_sum(colp);
+    if (lane == 0) P.colpart[I.cp_off + (long long)T.band * I.nc + j] = colp;
+  }
+}
+
 // Line sums of `n` partial vectors (partial c of line l at base[c * stride
 // + l]) for lines lo + threadIdx.x + k * blockDim.x below hi.  A thread takes
 // 4 lines and issues the loads of 8 partials of each before adding any (one
@@ -521,9 +637,14 @@ __device__ void build_active_lists(const BatchParams& P, int* scan) {
   if (tid < 5) P.counters[8 + tid] = (unsigned)s_carry[tid];
 }
 
-template <typename CT, int DIM>
+// GL = true: the group-lasso iteration (core/drot_glr.hpp:242-355) on plans
+// made by drot_gl_batch_plan_create -- bands are the instances' groups, the
+// stop test runs on every iteration with "<=", no fold, and n_iter counts
+// the iterations run.
+template <typename CT, int DIM, bool GL = false>
 __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P) {
-  constexpr int VEC = 4, KV = kBatchKV, S = kBatchS;
+  constexpr int VEC = 4, KV = kBatchKV;
+  const int S = GL ? P.band_cover : kBatchS;  // rows of the band staging
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int W = blockDim.x >> 5;
   float* red = reinterpret_cast<float*>(smem_raw);  // [W][S]
@@ -592,6 +713,46 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       if (__ldcg(P.conv + T.inst)) continue;
       const BatchInst I = P.inst[T.inst];
       const int lo = T.lo, hi = T.hi;
+      if constexpr (GL) {
+        // phi1 of the group's rows (from the 16-byte boundary below lo) and
+        // zeroed per-warp row partials, then the two-pass column walk.
+        const int base = lo & ~3, cover = hi - base;
+        for (int idx = threadIdx.x; idx < cover; idx += blockDim.x) {
+          const int r = base + idx;
+          f1s[idx] = r >= lo ? __ldcg(P.phi1 + I.row_off + r) : 0.0f;
+        }
+        for (int idx = threadIdx.x; idx < W * S; idx += blockDim.x) red[idx] = 0.0f;
+        __syncthreads();
+        float ms_hi = 0.0f, ms_lo = 0.0f, ob_hi = 0.0f, ob_lo = 0.0f;
+        batch_gl_tile_columns<CT>(P, I, T, f1s, red + (size_t)warp * S, ms_hi, ms_lo, ob_hi,
+                                  ob_lo, lane, warp, W);
+        const fpair wsum = warp_sum_fp(fpair{ms_hi, ms_lo});
+        const fpair wobj = warp_sum_fp(fpair{ob_hi, ob_lo});
+        if (lane == 0) {
+          dscr[warp] = wsum;
+          oscr[warp] = wobj;
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < cover; idx += blockDim.x) {
+          const int r = base + idx;
+          if (r >= lo) {
+            float tsum = 0.0f;
+            for (int w = 0; w < W; ++w) tsum += red[(size_t)w * S + idx];
+            P.rowpart[I.rp_off + (long long)T.chunk * I.nr + r] = tsum;
+          }
+        }
+        if (warp == 0) {
+          fpair a1 = lane < W ? dscr[lane] : fp_make(0.0f);
+          fpair a2 = lane < W ? oscr[lane] : fp_make(0.0f);
+          a1 = warp_sum_fp(a1);
+          a2 = warp_sum_fp(a2);
+          if (lane == 0) {
+            P.tile_sum[t] = make_float2(a1.hi, a1.lo);
+            P.tile_obj[t] = make_float2(a2.hi, a2.lo);
+          }
+        }
+        continue;
+      }
       for (int idx = threadIdx.x; idx < S; idx += blockDim.x) {
         const int r = lo + idx;
         f1s[idx] = r < hi ? __ldcg(P.phi1 + I.row_off + r) : 0.0f;
@@ -699,13 +860,13 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       for (int i = threadIdx.x; i < ntl; i += blockDim.x) {
         const float2 u = __ldcg(P.tile_sum + t0 + i);
         sg = fp_add(sg, fpair{u.x, u.y});
-        if (even && first) {
+        if ((even || GL) && first) {
           const float2 o = __ldcg(P.tile_obj + t0 + i);
           og = fp_add(og, fpair{o.x, o.y});
         }
       }
       sg = block_sum_fp(sg, dscr);
-      if (even && first) og = block_sum_fp(og, dscr);
+      if ((even || GL) && first) og = block_sum_fp(og, dscr);
       const float sigma = sg.hi + sg.lo;  // the float total mass
       const float alpha = __ldcg(P.alpha + (size_t)(it & 1) * P.n_inst + k);
       const float gamma =
@@ -733,7 +894,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       res = block_sum_fp(res, dscr);
       if (threadIdx.x == 0) {
         P.res_slot[qi] = make_float2(res.hi, res.lo);
-        if (even && first) P.obj_slot[k] = fp_value(og);
+        if ((even || GL) && first) P.obj_slot[k] = fp_value(og);
       }
       __syncthreads();
     }
@@ -744,7 +905,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       break;
     }
 
-    if (even) {
+    if (even || GL) {
       // Stop test (drot_qr.hpp:219-229: even iterations, residual < eps), by
       // the CTA of each instance's first item, then one more barrier so the
       // next fused update sees every decision.
@@ -800,7 +961,8 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
   // ------------------------------------------------------------ epilogue
   // Unfold the X of converged instances (fix_x, kernel_qr.hpp:469-482);
   // static tile assignment (the last barrier ordered every earlier write).
-  if (!aborted) {
+  // GL stores X unfolded on every iteration.
+  if (!GL && !aborted) {
     for (int t = blockIdx.x; t < P.n_tiles; t += G) {
       const BatchTile T = P.tiles[t];
       if (!__ldcg(P.conv + T.inst)) continue;
@@ -836,7 +998,9 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
     if (threadIdx.x == 0) {
       BatchStat st = P.stats[k];
       if (!st.converged) {
-        st.n_iter = P.max_iters + 1;  // drot_qr.hpp:233 without convergence
+        // drot_qr.hpp:233 without convergence (QR); GL counts the
+        // iterations run (drot_glr.hpp:354)
+        st.n_iter = GL ? P.max_iters : P.max_iters + 1;
         st.iters_run = aborted ? it : P.max_iters;
       }
       P.stats[k] = st;
@@ -852,10 +1016,41 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
 static const size_t kAl = 256;
 static inline size_t al(size_t v) { return (v + kAl - 1) / kAl * kAl; }
 
+// Tile-level shape of the plans created after drot_batch_set_tuning (one
+// process-wide setting, read once per plan).  Defaults, measured:
+//  * fine_cols 128, level_quarters 8: on 256 instances of U{64..2048}^2 with
+//    256-column coarse tiles, 128-column fine tiles and the switch at grid / 2
+//    gave 3.20 s against 3.45 s without the fine list (32-column fine tiles:
+//    3.45-3.85 s).  On the 64-instance differentiable workload the switch at
+//    2 / 8 / 16 / 32 quarters of the grid gave 5.70 / 5.66 / 5.72 / 5.76 s per
+//    solve (finer tiles balance the tail's CTAs -- barrier wait 14 -> 6 us --
+//    until their per-tile cost wins).
+//  * finest_cols 32, finest_item_lines 64: the level used once the fine list
+//    too leaves CTAs idle (in the 256-instance workload the last few
+//    instances, mostly the largest, for the last two thirds of the
+//    iterations); a lone 2048-column instance still spreads over ~250 CTAs.
+//  * item_lines 1024: rows + columns per dual-update item.
+//  * prefetch_distance 1: on the 64-instance workload (377 M elements, all
+//    active) one warp step ahead took an iteration from 663 to 601 us (0.85
+//    -> 0.94 of the measured HBM copy bandwidth); 2 steps 606 us, 4 steps 647.
+struct BatchTuning {
+  int fine_cols = 128, finest_cols = 32, item_lines = 1024, finest_item_lines = 64,
+      level_quarters = 8, prefetch_distance = 1;
+};
+static std::mutex g_tuning_mu;
+static BatchTuning g_tuning;
+static BatchTuning current_tuning() {
+  std::lock_guard<std::mutex> lk(g_tuning_mu);
+  return g_tuning;
+}
+
 struct BatchPlanImpl {
   int n_inst = 0, n_tiles = 0, n_tiles_f = 0, n_tiles_x = 0, n_items = 0, n_items_x = 0;
   int grid = 0, threads = 256, cols_per_tile = 0;
   int band_rows = 512;
+  int gl = 0;                 // group-lasso plan
+  int band_cover = kBatchS;   // GL: rows of the band staging (>= every group's cover)
+  BatchTuning tune;           // tile-level shape and prefetch (drot_batch_set_tuning)
   size_t smem = 0;
   long long rows = 0, cols = 0, rowpart = 0, colpart = 0;
   std::vector<BatchInst> inst;
@@ -870,64 +1065,6 @@ struct BatchPlanImpl {
          off_yn = 0, total = 0;
   bool uploaded_any = false;
 };
-
-// Fine-list shape: columns per fine tile and the switch point (fewer active
-// coarse tiles than grid / divisor).  Measured on 256 instances of
-// U{64..2048}^2 with 256-column coarse tiles: 128 columns, grid / 2 and
-// 1024-line dual-update items gave 3.20 s against 3.45 s without the fine
-// list (32-column fine tiles: 3.45-3.85 s; their per-tile overhead and the
-// longer row-partial sums cost more than the parallelism gains).
-// DROT_BATCH_FINE_COLS and DROT_BATCH_FINE_DIV override them (0 as divisor
-// disables the fine list).
-static int fine_cols() {
-  const char* e = getenv("DROT_BATCH_FINE_COLS");
-  const int v = e ? atoi(e) : 0;
-  return v > 0 ? v : 128;
-}
-// L2 prefetch distance of the fused update in warp steps (DROT_BATCH_PF,
-// 0..8; 0 switches the prefetch off).
-static int prefetch_distance() {
-  const char* e = getenv("DROT_BATCH_PF");
-  const int d = (e && *e) ? atoi(e) : 0;
-  return d < 0 ? 0 : (d > 8 ? 8 : d);
-}
-
-// Active tiles of a level below which the solve moves to the next finer
-// level, in quarters of the grid: DROT_BATCH_FINE_QUARTERS (default 2, i.e.
-// half the CTAs; 0 never moves).  DROT_BATCH_FINE_DIV=d, the older knob,
-// sets the threshold to grid / d.
-static long long fine_threshold(int grid) {
-  if (const char* e = getenv("DROT_BATCH_FINE_QUARTERS")) {
-    const int v = atoi(e);
-    return v <= 0 ? 0 : (long long)grid * v / 4;
-  }
-  const char* e = getenv("DROT_BATCH_FINE_DIV");
-  const int v = e ? atoi(e) : -1;
-  if (v == 0) return 0;
-  return grid / (v > 0 ? v : 2);
-}
-static int item_lines() {  // lines per dual-update item (DROT_BATCH_ITEM_LINES overrides)
-  const char* e = getenv("DROT_BATCH_ITEM_LINES");
-  const int v = e ? atoi(e) : 0;
-  return v > 0 ? v : 1024;
-}
-// The finest level, used once the fine list too leaves CTAs idle (in the
-// 256-instance workload: the last few instances, mostly the single largest,
-// for the last two thirds of the iterations): 32-column tiles, so a lone
-// 2048-column instance still spreads over ~250 CTAs, and 64-line dual-update
-// items, so the row sums over its ~60 column chunks are spread as widely.
-// DROT_BATCH_FINEST_COLS (0 disables the level) and
-// DROT_BATCH_FINEST_ITEM_LINES override them.
-static int finest_cols() {
-  const char* e = getenv("DROT_BATCH_FINEST_COLS");
-  const int v = e ? atoi(e) : -1;
-  return v >= 0 ? v : 32;
-}
-static int finest_item_lines() {
-  const char* e = getenv("DROT_BATCH_FINEST_ITEM_LINES");
-  const int v = e ? atoi(e) : 0;
-  return v > 0 ? v : 64;
-}
 
 // Tiles of one instance: every 512-row band x `chunks` column chunks.
 static void add_tiles(std::vector<BatchTile>& tiles, int k, const BatchInst& I, int chunks) {
@@ -947,11 +1084,46 @@ static void add_tiles(std::vector<BatchTile>& tiles, int k, const BatchInst& I, 
     }
 }
 
-// Dynamic shared memory: row reduction [warps][512], phi1 stage [512], FP64
-// scratch, and for point launches the band's x (k-major) and norms.
-static size_t batch_smem(int warps, int dim) {
-  return sizeof(float) * ((size_t)warps * kBatchS + kBatchS) + sizeof(fpair) * (2 * warps + 1) +
-         16 /* alignment of the point stage */ + sizeof(float) * ((size_t)dim * 128 + 128);
+// GL tiles of one instance: every group (the reference's contiguous class
+// row ranges, bounds[0..G]) x `chunks` column chunks.
+static void add_gl_tiles(std::vector<BatchTile>& tiles, int k, const BatchInst& I, int chunks,
+                         const std::vector<int>& bounds) {
+  for (int g = 0; g + 1 < (int)bounds.size(); ++g)
+    for (int c = 0; c < chunks; ++c) {
+      BatchTile T;
+      T.inst = k;
+      T.band = g;
+      T.chunk = c;
+      T.lo = bounds[g];
+      T.hi = bounds[g + 1];
+      T.c0 = (int)(((long long)I.nc * c) / chunks);
+      T.c1 = (int)(((long long)I.nc * (c + 1)) / chunks);
+      T.kvr = 4;
+      tiles.push_back(T);
+    }
+}
+
+// Group row boundaries of the reference GL kernels (core/kernel_glr.hpp:79-80
+// with +0.49 when ceil(n_rows/G) <= 256, drot_glr.hpp:280; +0.49999
+// otherwise, kernel_glr.hpp:185-186), FP32 products as the reference.
+static std::vector<int> gl_bounds(int nr, int G) {
+  std::vector<int> b(G + 1);
+  const double off = ((nr + G - 1) / G) <= 256 ? 0.49 : 0.49999;
+  const float per = (float)nr / (float)G;
+  for (int k = 0; k <= G; ++k) b[k] = (int)((double)(per * (float)k) + off);
+  return b;
+}
+
+// Largest group height a GL plan stages (rows of shared memory per warp).
+constexpr int kBatchGlMaxCover = 4096;
+
+// Dynamic shared memory: row reduction [warps][S], phi1 stage [S] (S = 512
+// rows, or a GL plan's band cover), FP64 scratch, and for point launches the
+// band's x (k-major) and norms.
+static size_t batch_smem(int warps, int dim, int band_cover = kBatchS) {
+  return sizeof(float) * ((size_t)warps * band_cover + band_cover) +
+         sizeof(fpair) * (2 * warps + 1) + 16 /* alignment of the point stage */ +
+         sizeof(float) * ((size_t)dim * 128 + 128);
 }
 
 }  // namespace drot
@@ -967,21 +1139,68 @@ struct drot_batch_plan_s {
 
 extern "C" {
 
+int drot_batch_set_tuning(const drot_batch_tuning* t) {
+  BatchTuning v;
+  if (t) {
+    const BatchTuning d;
+    if (t->fine_cols > 4096 || t->finest_cols > 4096 || t->item_lines > (1 << 24) ||
+        t->finest_item_lines > (1 << 24) || t->level_quarters > 4096 ||
+        t->prefetch_distance > 8 || t->fine_cols == 0 || t->item_lines == 0 ||
+        t->finest_item_lines == 0)
+      return DROT_ERR_INVALID_ARG;
+    v.fine_cols = t->fine_cols > 0 ? t->fine_cols : d.fine_cols;
+    v.finest_cols = t->finest_cols >= 0 ? t->finest_cols : d.finest_cols;
+    v.item_lines = t->item_lines > 0 ? t->item_lines : d.item_lines;
+    v.finest_item_lines = t->finest_item_lines > 0 ? t->finest_item_lines : d.finest_item_lines;
+    v.level_quarters = t->level_quarters >= 0 ? t->level_quarters : d.level_quarters;
+    v.prefetch_distance = t->prefetch_distance >= 0 ? t->prefetch_distance : d.prefetch_distance;
+  }
+  std::lock_guard<std::mutex> lk(g_tuning_mu);
+  g_tuning = v;
+  return DROT_OK;
+}
+
 int drot_batch_plan_create(int n_inst, const drot_batch_instance* desc, int cols_per_tile,
                            drot_batch_plan* out) {
   return drot_batch_plan_create_ex(n_inst, desc, cols_per_tile, 512, out);
 }
 
-int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int cols_per_tile,
-                              int band_rows, drot_batch_plan* out) {
+}  // extern "C"
+
+// Plan of a QR batch, or of a GL batch when groups != nullptr (groups[k] the
+// class count and lambdas[k] the shrink threshold of instance k; the
+// descriptors' r_weight is then unused).
+static int batch_plan_create_impl(int n_inst, const drot_batch_instance* desc, int cols_per_tile,
+                                  int band_rows, const int* groups, const float* lambdas,
+                                  drot_batch_plan* out) {
   if (!out || n_inst <= 0 || n_inst > 65535 || !desc) return DROT_ERR_INVALID_ARG;
   if (band_rows != 128 && band_rows != 512) return DROT_ERR_INVALID_ARG;
+  const bool gl = groups != nullptr;
+  if (gl && band_rows != 512) return DROT_ERR_INVALID_ARG;
   *out = nullptr;
   if (cols_per_tile <= 0) cols_per_tile = 128;
   BatchPlanImpl P;
+  P.tune = current_tuning();
+  const int fine_cols = P.tune.fine_cols, finest_cols = P.tune.finest_cols;
   P.n_inst = n_inst;
   P.cols_per_tile = cols_per_tile;
+  P.gl = gl ? 1 : 0;
   P.inst.resize(n_inst);
+  std::vector<std::vector<int>> bounds(gl ? n_inst : 0);
+  if (gl) {
+    int cover = 0;
+    for (int k = 0; k < n_inst; ++k) {
+      if (groups[k] <= 0 || groups[k] > desc[k].n_rows || !(lambdas[k] >= 0.0f))
+        return DROT_ERR_INVALID_ARG;
+      bounds[k] = gl_bounds(desc[k].n_rows, groups[k]);
+      for (int g = 0; g < groups[k]; ++g) {
+        if (bounds[k][g + 1] <= bounds[k][g]) return DROT_ERR_INVALID_ARG;
+        cover = std::max(cover, bounds[k][g + 1] - (bounds[k][g] & ~3));
+      }
+    }
+    P.band_cover = (cover + kBatchS - 1) / kBatchS * kBatchS;
+    if (P.band_cover > kBatchGlMaxCover) return DROT_ERR_UNSUPPORTED;
+  }
   long long rows = 0, cols = 0, rp = 0, cpp = 0;
   for (int k = 0; k < n_inst; ++k) {
     const drot_batch_instance& d = desc[k];
@@ -1002,12 +1221,13 @@ int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int c
     // Bands of 512 rows; the last one takes the remainder and the narrowest
     // warp step (128, 256 or 512 rows x 4, 2 or 1 columns) that covers it.
     I.band_h = band_rows;
-    I.nbands = (d.n_rows + band_rows - 1) / band_rows;
+    I.nbands = gl ? groups[k] : (d.n_rows + band_rows - 1) / band_rows;
     I.P = (d.n_cols + cols_per_tile - 1) / cols_per_tile;
-    I.Pf = (d.n_cols + fine_cols() - 1) / fine_cols();
-    I.Px = finest_cols() > 0 ? (d.n_cols + finest_cols() - 1) / finest_cols() : 0;
+    I.Pf = (d.n_cols + fine_cols - 1) / fine_cols;
+    I.Px = finest_cols > 0 ? (d.n_cols + finest_cols - 1) / finest_cols : 0;
     I.tile0 = (int)P.tiles.size();
-    add_tiles(P.tiles, k, I, I.P);
+    if (gl) add_gl_tiles(P.tiles, k, I, I.P, bounds[k]);
+    else add_tiles(P.tiles, k, I, I.P);
     I.ntiles = (int)P.tiles.size() - I.tile0;
     I.row_off = (int)rows;
     I.col_off = (int)cols;
@@ -1017,7 +1237,7 @@ int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int c
     cols += d.n_cols;
     rp += (long long)std::max(std::max(I.P, I.Pf), I.Px) * d.n_rows;
     I.item0 = (int)P.items.size();
-    const int ilines = item_lines();
+    const int ilines = P.tune.item_lines;
     for (int l = 0; l < d.n_rows + d.n_cols; l += ilines) {
       BatchItem Q;
       Q.inst = k;
@@ -1037,7 +1257,9 @@ int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int c
     I.kappa = 1.0f + t;
     I.kappa_rcp = (float)(1.0 / (double)I.kappa);
     I.eps = d.eps;
-    I.res2_stop = res2_threshold(d.eps, true);
+    // QR stops on residual < eps, GL on residual <= eps (drot_glr.hpp:348)
+    I.res2_stop = res2_threshold(d.eps, !gl);
+    I.lambda = gl ? lambdas[k] : 0.0f;
     I.nc_rcp = (float)(1.0 / (double)(float)d.n_cols);
     I.nr_rcp = (float)(1.0 / (double)(float)d.n_rows);
     const float n = (float)d.n_rows, m = (float)d.n_cols;
@@ -1055,27 +1277,31 @@ int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int c
     P.inst[k] = I;
   }
   P.n_tiles = (int)P.tiles.size();
-  // The fine list (fine_cols()-column chunks) after the coarse one; unused when the
+  // The fine list (fine_cols-column chunks) after the coarse one; unused when the
   // coarse tiles are no wider.
   for (int k = 0; k < n_inst; ++k) {
     BatchInst& I = P.inst[k];
     I.tile0f = (int)P.tiles.size();
-    add_tiles(P.tiles, k, I, I.Pf);
+    if (gl) add_gl_tiles(P.tiles, k, I, I.Pf, bounds[k]);
+    else add_tiles(P.tiles, k, I, I.Pf);
     I.ntilesf = (int)P.tiles.size() - I.tile0f;
   }
-  P.n_tiles_f = fine_cols() < cols_per_tile ? (int)P.tiles.size() - P.n_tiles : 0;
+  P.n_tiles_f = fine_cols < cols_per_tile ? (int)P.tiles.size() - P.n_tiles : 0;
   // The finest list after the fine one (only when the fine list is used).
-  const bool use_x = P.n_tiles_f > 0 && finest_cols() > 0 && finest_cols() < fine_cols();
+  const bool use_x = P.n_tiles_f > 0 && finest_cols > 0 && finest_cols < fine_cols;
   const int x0 = (int)P.tiles.size();
   P.n_items = (int)P.items.size();
   for (int k = 0; k < n_inst; ++k) {
     BatchInst& I = P.inst[k];
     I.tile0x = (int)P.tiles.size();
-    if (use_x) add_tiles(P.tiles, k, I, I.Px);
+    if (use_x) {
+      if (gl) add_gl_tiles(P.tiles, k, I, I.Px, bounds[k]);
+      else add_tiles(P.tiles, k, I, I.Px);
+    }
     I.ntilesx = (int)P.tiles.size() - I.tile0x;
     I.item0x = (int)P.items.size();
     if (use_x) {
-      const int xl = finest_item_lines();
+      const int xl = P.tune.finest_item_lines;
       for (int l = 0; l < I.nr + I.nc; l += xl) {
         BatchItem Q;
         Q.inst = k;
@@ -1107,13 +1333,23 @@ int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int c
     return DROT_ERR_CUDA;
   P.threads = 256;
   P.band_rows = band_rows;
-  P.smem = batch_smem(P.threads / 32, 16);  // sized for every kernel variant
-  const void* kernels[] = {(const void*)batch_solve_kernel<float, 0>,
-                           (const void*)batch_solve_kernel<__nv_bfloat16, 0>,
-                           (const void*)batch_solve_kernel<float, 8>,
-                           (const void*)batch_solve_kernel<float, 16>};
+  P.smem = gl ? batch_smem(P.threads / 32, 0, P.band_cover)
+              : batch_smem(P.threads / 32, 16);  // sized for every kernel variant
+  const void* qr_kernels[] = {(const void*)batch_solve_kernel<float, 0>,
+                              (const void*)batch_solve_kernel<__nv_bfloat16, 0>,
+                              (const void*)batch_solve_kernel<float, 8>,
+                              (const void*)batch_solve_kernel<float, 16>};
+  const void* gl_kernels[] = {(const void*)batch_solve_kernel<float, 0, true>,
+                              (const void*)batch_solve_kernel<__nv_bfloat16, 0, true>};
+  std::vector<const void*> kernels;
+  if (gl) kernels.assign(gl_kernels, gl_kernels + 2);
+  else kernels.assign(qr_kernels, qr_kernels + 4);
   int occ = 1 << 30;
   for (const void* fn : kernels) {
+    if (P.smem > 48 * 1024 &&
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem) !=
+            cudaSuccess)
+      return DROT_ERR_CUDA;
     int o = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, P.threads, P.smem) != cudaSuccess)
       return DROT_ERR_CUDA;
@@ -1151,6 +1387,39 @@ int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int c
   h->p = std::move(P);
   *out = h;
   return DROT_OK;
+}
+
+extern "C" {
+
+int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance* desc, int cols_per_tile,
+                              int band_rows, drot_batch_plan* out) {
+  return batch_plan_create_impl(n_inst, desc, cols_per_tile, band_rows, nullptr, nullptr, out);
+}
+
+int drot_gl_batch_plan_create(int n_inst, const drot_gl_batch_instance* desc, int cols_per_tile,
+                              drot_batch_plan* out) {
+  if (!desc || n_inst <= 0 || n_inst > 65535) return DROT_ERR_INVALID_ARG;
+  std::vector<drot_batch_instance> d(n_inst);
+  std::vector<int> groups(n_inst);
+  std::vector<float> lambdas(n_inst);
+  for (int k = 0; k < n_inst; ++k) {
+    const drot_gl_batch_instance& g = desc[k];
+    memset(&d[k], 0, sizeof(d[k]));
+    d[k].n_rows = g.n_rows;
+    d[k].n_cols = g.n_cols;
+    d[k].ld = g.ld;
+    d[k].c_offset = g.c_offset;
+    d[k].x_offset = g.x_offset;
+    d[k].p_offset = g.p_offset;
+    d[k].q_offset = g.q_offset;
+    d[k].rho = g.rho;
+    d[k].r_weight = 0.0f;
+    d[k].eps = g.eps;
+    groups[k] = g.n_groups;
+    lambdas[k] = g.lambda;
+  }
+  return batch_plan_create_impl(n_inst, d.data(), cols_per_tile, 512, groups.data(),
+                                lambdas.data(), out);
 }
 
 void drot_batch_plan_destroy(drot_batch_plan plan) { delete plan; }
@@ -1194,7 +1463,8 @@ static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, 
   B.n_tiles_f = P.n_tiles_f;
   B.n_tiles_x = P.n_tiles_x;
   B.n_items_x = P.n_items_x;
-  B.fine_threshold = (int)fine_threshold(P.grid);
+  // active tiles of a level below which the solve moves to the next finer one
+  B.fine_threshold = (int)((long long)P.grid * P.tune.level_quarters / 4);
   B.items = (const BatchItem*)(ws + P.off_items);
   B.n_items = P.n_items;
   B.res_slot = (float2*)(ws + P.off_res);
@@ -1223,7 +1493,8 @@ static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, 
   // failure-detection test hook of the bounded waits; off by default).
   const char* sc = getenv("DROT_TEST_STALL_CTA");
   B.stall_cta = (sc && *sc) ? atoi(sc) : -1;
-  B.pf_dist = prefetch_distance();
+  B.pf_dist = P.tune.prefetch_distance;
+  B.band_cover = P.band_cover;
   if (cudaMemsetAsync(ws + P.off_ctrl, 0, 512, st) != cudaSuccess) return DROT_ERR_CUDA;
   batch_init_kernel<<<dim3(64, P.n_inst), 256, 0, st>>>(B);
   if (cudaGetLastError() != cudaSuccess) return DROT_ERR_CUDA;
@@ -1256,8 +1527,12 @@ int drot_qr_batch_launch(drot_batch_plan plan, const void* c, int c_dtype, const
   B.iter_log = plan->iter_log;
   B.iter_tiles = plan->iter_tiles;
   B.iter_log_cap = plan->iter_log_cap;
-  const void* fn = c_dtype == DROT_C_F32 ? (const void*)batch_solve_kernel<float, 0>
-                                         : (const void*)batch_solve_kernel<__nv_bfloat16, 0>;
+  const bool gl = plan->p.gl != 0;
+  const void* fn = c_dtype == DROT_C_F32
+                       ? (gl ? (const void*)batch_solve_kernel<float, 0, true>
+                             : (const void*)batch_solve_kernel<float, 0>)
+                       : (gl ? (const void*)batch_solve_kernel<__nv_bfloat16, 0, true>
+                             : (const void*)batch_solve_kernel<__nv_bfloat16, 0>);
   return batch_launch(plan->p, fn, B, workspace, workspace_bytes, max_iters,
                       (cudaStream_t)stream);
 }
@@ -1269,7 +1544,7 @@ int drot_qr_batch_launch_points(drot_batch_plan plan, const float* xpts, const f
   if (!plan || !xpts || !ypts || !p || !q || !x || !workspace || max_iters < 0)
     return DROT_ERR_INVALID_ARG;
   if (dim != 8 && dim != 16) return DROT_ERR_UNSUPPORTED;
-  if (plan->p.band_rows != 128) return DROT_ERR_INVALID_ARG;  // point tiles are 128-row bands
+  if (plan->p.band_rows != 128 || plan->p.gl) return DROT_ERR_INVALID_ARG;  // point tiles: 128-row QR bands
   if (((uintptr_t)x & 15u) || ((uintptr_t)xpts & 15u) || ((uintptr_t)ypts & 15u))
     return DROT_ERR_INVALID_ARG;
   const BatchPlanImpl& P = plan->p;
@@ -1314,6 +1589,18 @@ int drot_batch_state(drot_batch_plan plan, void* workspace, float** phi1, float*
   char* ws = (char*)workspace;
   *phi1 = (float*)(ws + plan->p.off_phi1);
   *phi2 = (float*)(ws + plan->p.off_phi2);
+  return DROT_OK;
+}
+
+int drot_batch_state_ex(drot_batch_plan plan, void* workspace, float** a, float** b,
+                        float** phi1, float** phi2, float** alpha) {
+  if (!plan || !workspace || !a || !b || !phi1 || !phi2 || !alpha) return DROT_ERR_INVALID_ARG;
+  char* ws = (char*)workspace;
+  *a = (float*)(ws + plan->p.off_a);
+  *b = (float*)(ws + plan->p.off_b);
+  *phi1 = (float*)(ws + plan->p.off_phi1);
+  *phi2 = (float*)(ws + plan->p.off_phi2);
+  *alpha = (float*)(ws + plan->p.off_alpha);
   return DROT_OK;
 }
 

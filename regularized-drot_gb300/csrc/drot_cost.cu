@@ -13,12 +13,16 @@
 // cores (the dropped x_lo.y_lo term is below 2^-22 relative).  Norms are
 // FP32 FMA sums in k order.
 //
-// One CTA per 128 x 256 tile: 4 warps stage the hi / lo operand tiles in
-// shared memory (K-major, no swizzle: 8-row x 16-byte core matrices), one
-// thread issues 3 * d/8 MMAs into a 128-lane x 256-column TMEM accumulator,
-// a tcgen05.commit arrives on an mbarrier, then each warp reads its 32 TMEM
-// lanes (tcgen05.ld 32x32b) and writes its rows of every column (128 bytes
-// per warp store).  The kernel is bound by the C stores (4 bytes per element).
+// Persistent kernel (at most two CTAs per SM, each walking the tiles of all
+// instances with stride grid): per 128 x 128 tile, 256 threads stage the
+// hi / lo operand tiles in shared memory (K-major, no swizzle: 8-row x
+// 16-byte core matrices), one thread issues 3 * d/8 MMAs into a 128-lane x
+// 128-column TMEM accumulator and a tcgen05.commit arrives on an mbarrier;
+// then each warp reads its TMEM lane quadrant for half of the columns
+// (tcgen05.ld 32x32b) and writes those rows of each column (128 bytes per
+// warp store).  Operands and accumulators are double-buffered, so tile n+1's
+// loads and MMAs run while tile n's C is stored.  The kernel is bound by the
+// C stores (4 bytes per element).
 #include <cuda_runtime.h>
 
 #include <stdint.h>
@@ -36,12 +40,12 @@ namespace drot {
 constexpr int kCostM = 128;        // tile rows (x points) = TMEM lanes
 constexpr int kCostN = 128;        // tile columns (y points) = TMEM columns
 constexpr int kCostMaxInst = 256;  // instances per launch (descriptors travel in the parameters)
-constexpr int kCostThreads = 128;
+constexpr int kCostThreads = 256;  // 8 warps: x / y rows staged one per thread
 
 struct CostInst {
   long long x_off, y_off, c_off;  // element offsets: x (m x d), y (n x d), C (ld x n)
   int m, n, ld, tiles_m, tiles;
-  int pad;
+  int tile0;  // tiles of the earlier instances
 };
 
 struct CostParams {
@@ -50,7 +54,7 @@ struct CostParams {
   float* c;
   int* err;
   long long timeout_ns;
-  int dim, n_inst, clamp, pad;
+  int dim, n_inst, clamp, total_tiles;
   float scale, pad2;
   CostInst inst[kCostMaxInst];
 };
@@ -92,150 +96,195 @@ __device__ __forceinline__ uint32_t kmaj_off(int r, int k, int kc) {
   return (uint32_t)((((r >> 3) * kc + (k >> 2)) << 7) + ((r & 7) << 4) + ((k & 3) << 2));
 }
 
-__global__ void __launch_bounds__(kCostThreads) cost_sqeuclid_kernel(const __grid_constant__ CostParams P) {
-  const int k = blockIdx.y;
-  if (k >= P.n_inst) return;
-  const CostInst& I = P.inst[k];
-  const int t = blockIdx.x;
-  if (t >= I.tiles) return;
-  const int i0 = (t % I.tiles_m) * kCostM;
-  const int j0 = (t / I.tiles_m) * kCostN;
-  const int d = P.dim, kc = d >> 2;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+// Stage tile (i0, j0) of instance I into one operand buffer: x rows by
+// threads 0..127, y rows by threads 128..255 (one row each): hi / lo TF32
+// parts in the K-major layout, FP32 norms in k order.
+__device__ __forceinline__ void cost_stage(const CostParams& P, const CostInst& I, int i0, int j0,
+                                           unsigned char* buf, uint32_t op_bytes, float* norms) {
+  const int d = P.dim, kc = d >> 2, tid = threadIdx.x;
+  const bool is_y = tid >= kCostM;
+  const int r = is_y ? tid - kCostM : tid;
+  const int row = (is_y ? j0 : i0) + r;
+  const bool in = row < (is_y ? I.n : I.m);
+  const float4* src = reinterpret_cast<const float4*>(
+      (is_y ? P.y + I.y_off : P.x + I.x_off) + (long long)(in ? row : 0) * d);
+  unsigned char* hi_t = buf + (is_y ? 2 * op_bytes : 0);
+  unsigned char* lo_t = hi_t + op_bytes;
+  float nrm = 0.0f;
+  for (int c4 = 0; c4 < kc; ++c4) {
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (in) v = __ldg(src + c4);
+    const float e[4] = {v.x, v.y, v.z, v.w};
+    uint32_t hi[4], lo[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      hi[q] = to_tf32(e[q]);
+      lo[q] = to_tf32(e[q] - __uint_as_float(hi[q]));
+      nrm = fmaf(e[q], e[q], nrm);
+    }
+    const uint32_t off = kmaj_off(r, c4 * 4, kc);
+    *reinterpret_cast<uint4*>(hi_t + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+    *reinterpret_cast<uint4*>(lo_t + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+  }
+  norms[tid] = nrm;  // x norms [0, 128), y norms [128, 256)
+}
 
+// The 3 x d/8 MMAs of one tile into a 128-column TMEM accumulator, then a
+// commit arriving on `bar` (one thread).
+__device__ __forceinline__ void cost_issue(unsigned char* buf, uint32_t op_bytes, int d,
+                                           uint32_t tmem, uint64_t* bar) {
+  const uint32_t sbo = (uint32_t)(d >> 2) * 128u;
+  const uint32_t ah = smem_u32(buf), al = ah + op_bytes;
+  const uint32_t bh = al + op_bytes, bl = bh + op_bytes;
+  const int ks_n = d >> 3;  // K = 8 per kind::tf32 MMA = 2 core matrices
+  for (int ks = 0; ks < ks_n; ++ks)
+    mma_tf32(tmem, smem_desc(ah + ks * 256, 128, sbo), smem_desc(bh + ks * 256, 128, sbo),
+             ks > 0 ? 1u : 0u);
+  for (int ks = 0; ks < ks_n; ++ks)
+    mma_tf32(tmem, smem_desc(ah + ks * 256, 128, sbo), smem_desc(bl + ks * 256, 128, sbo), 1u);
+  for (int ks = 0; ks < ks_n; ++ks)
+    mma_tf32(tmem, smem_desc(al + ks * 256, 128, sbo), smem_desc(bh + ks * 256, 128, sbo), 1u);
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+               :: "r"(smem_u32(bar)) : "memory");
+}
+
+// Instance and tile coordinates of global tile g (k advances monotonically).
+__device__ __forceinline__ void cost_locate(const CostParams& P, int g, int& k, int& i0, int& j0) {
+  while (g >= P.inst[k].tile0 + P.inst[k].tiles) ++k;
+  const int t = g - P.inst[k].tile0;
+  i0 = (t % P.inst[k].tiles_m) * kCostM;
+  j0 = (t / P.inst[k].tiles_m) * kCostN;
+}
+
+// Persistent: CTA b takes tiles b, b + grid, ... of all instances in order.
+// Operand buffers and TMEM accumulators are double-buffered, so while the
+// eight warps stage tile n+1 and then store tile n's C, the tensor core
+// computes tile n+1: the MMA and the operand loads hide behind the stores.
+__global__ void __launch_bounds__(kCostThreads, 1) cost_sqeuclid_kernel(const __grid_constant__ CostParams P) {
+  const int d = P.dim;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   extern __shared__ __align__(1024) unsigned char smem[];
-  const uint32_t a_bytes = (uint32_t)kCostM * d * 4, b_bytes = (uint32_t)kCostN * d * 4;
-  unsigned char* a_hi = smem;
-  unsigned char* a_lo = a_hi + a_bytes;
-  unsigned char* b_hi = a_lo + a_bytes;
-  unsigned char* b_lo = b_hi + b_bytes;
-  float* xn = reinterpret_cast<float*>(b_lo + b_bytes);
-  float* yn = xn + kCostM;
-  __shared__ __align__(8) uint64_t mbar;
+  const uint32_t op_bytes = (uint32_t)kCostM * d * 4;  // one hi or lo tile (x or y: 128 rows)
+  const uint32_t buf_bytes = 4 * op_bytes;
+  // norms of tile n in slot n % 3: staging writes tile n+1's while slower
+  // warps may still read tile n-1's
+  float* norms = reinterpret_cast<float*>(smem + 2 * buf_bytes);  // [3][256]
+  __shared__ __align__(8) uint64_t mbar[2];
   __shared__ uint32_t s_tmem;
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                 :: "r"(smem_u32(&s_tmem)), "r"((uint32_t)kCostN) : "memory");
+                 :: "r"(smem_u32(&s_tmem)), "r"((uint32_t)(2 * kCostN)) : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    mbar_init(&mbar, 1);
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
     fence_mbar_init();
   }
-
-  // Stage x rows (one per thread) and y rows (two per thread): hi / lo TF32
-  // parts in the K-major layout, FP32 norms.
-  {
-    const int r = tid;
-    const int i = i0 + r;
-    float nrm = 0.0f;
-    for (int c4 = 0; c4 < kc; ++c4) {
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (i < I.m) v = __ldg(reinterpret_cast<const float4*>(P.x + I.x_off + (long long)i * d) + c4);
-      const float e[4] = {v.x, v.y, v.z, v.w};
-      uint32_t hi[4], lo[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        hi[q] = to_tf32(e[q]);
-        lo[q] = to_tf32(e[q] - __uint_as_float(hi[q]));
-        nrm = fmaf(e[q], e[q], nrm);
-      }
-      const uint32_t off = kmaj_off(r, c4 * 4, kc);
-      *reinterpret_cast<uint4*>(a_hi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-      *reinterpret_cast<uint4*>(a_lo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
-    }
-    xn[r] = nrm;
-  }
-  for (int r = tid; r < kCostN; r += kCostThreads) {
-    const int j = j0 + r;
-    float nrm = 0.0f;
-    for (int c4 = 0; c4 < kc; ++c4) {
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (j < I.n) v = __ldg(reinterpret_cast<const float4*>(P.y + I.y_off + (long long)j * d) + c4);
-      const float e[4] = {v.x, v.y, v.z, v.w};
-      uint32_t hi[4], lo[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        hi[q] = to_tf32(e[q]);
-        lo[q] = to_tf32(e[q] - __uint_as_float(hi[q]));
-        nrm = fmaf(e[q], e[q], nrm);
-      }
-      const uint32_t off = kmaj_off(r, c4 * 4, kc);
-      *reinterpret_cast<uint4*>(b_hi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-      *reinterpret_cast<uint4*>(b_lo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
-    }
-    yn[r] = nrm;
+  int g = blockIdx.x, kk = 0, i0 = 0, j0 = 0;
+  if (g < P.total_tiles) {
+    cost_locate(P, g, kk, i0, j0);
+    cost_stage(P, P.inst[kk], i0, j0, smem, op_bytes, norms);
   }
   fence_proxy_async_shared();  // generic-proxy smem writes -> visible to the tensor core
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = s_tmem;
+  if (tid == 0 && g < P.total_tiles) cost_issue(smem, op_bytes, d, tmem, &mbar[0]);
 
-  if (tid == 0) {
-    const uint32_t sbo = (uint32_t)kc * 128u;
-    const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
-    const uint32_t bh = smem_u32(b_hi), bl = smem_u32(b_lo);
-    const int ks_n = d >> 3;  // K = 8 per kind::tf32 MMA = 2 core matrices
-    for (int ks = 0; ks < ks_n; ++ks)
-      mma_tf32(tmem, smem_desc(ah + ks * 256, 128, sbo), smem_desc(bh + ks * 256, 128, sbo),
-               ks > 0 ? 1u : 0u);
-    for (int ks = 0; ks < ks_n; ++ks)
-      mma_tf32(tmem, smem_desc(ah + ks * 256, 128, sbo), smem_desc(bl + ks * 256, 128, sbo), 1u);
-    for (int ks = 0; ks < ks_n; ++ks)
-      mma_tf32(tmem, smem_desc(al + ks * 256, 128, sbo), smem_desc(bh + ks * 256, 128, sbo), 1u);
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                 :: "r"(smem_u32(&mbar)) : "memory");
-  }
-  bool ok = mbar_wait(&mbar, 0, P.timeout_ns);
-  if (!ok) {
-    atomicExch(P.err, 1);
-    ok = false;
-    mbar_wait(&mbar, 0, P.timeout_ns);  // give the MMAs a second bounded chance to land
-  }
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // Epilogue split: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its lane
+  // quadrant) and columns 64 (w / 4) .. + 63 of the accumulator.
+  const int quad = warp & 3, half = warp >> 2;
+  for (int n = 0; g < P.total_tiles; ++n, g += gridDim.x) {
+    const int b = n & 1;
+    const int g_next = g + (int)gridDim.x;
+    int kn = kk, in0 = 0, jn0 = 0;
+    if (g_next < P.total_tiles) {
+      cost_locate(P, g_next, kn, in0, jn0);
+      cost_stage(P, P.inst[kn], in0, jn0, smem + (b ^ 1) * buf_bytes, op_bytes,
+                 norms + ((n + 1) % 3) * 256);
+    }
+    fence_proxy_async_shared();
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (tid == 0 && g_next < P.total_tiles)
+      cost_issue(smem + (b ^ 1) * buf_bytes, op_bytes, d, tmem + (uint32_t)((b ^ 1) * kCostN),
+                 &mbar[b ^ 1]);
+    // tile n's accumulator: use n >> 1 of buffer b
+    bool got = mbar_wait(&mbar[b], (uint32_t)((n >> 1) & 1), P.timeout_ns);
+    if (!__syncthreads_and(got ? 1 : 0)) {
+      // An MMA that never completed: report it, give the MMAs in flight a
+      // second bounded chance to land, and stop without storing.
+      if (tid == 0) atomicExch(P.err, 1);
+      mbar_wait(&mbar[b], (uint32_t)((n >> 1) & 1), P.timeout_ns);
+      if (g_next < P.total_tiles) mbar_wait(&mbar[b ^ 1], (uint32_t)(((n + 1) >> 1) & 1), P.timeout_ns);
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
-  // Epilogue: warp w owns TMEM lanes 32w..32w+31 = rows i0 + 32w + lane.
-  const int i = i0 + warp * 32 + lane;
-  const float xi = xn[warp * 32 + lane];
-  float* crow = P.c + I.c_off + i;
-  for (int cb = 0; cb < kCostN; cb += 32) {
-    uint32_t r[32];
-    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cb;
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-          "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
-          "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
-          "=r"(r[31])
-        : "r"(taddr) : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    if (ok && i < I.m) {
+    const CostInst& I = P.inst[kk];
+    const int i = i0 + quad * 32 + lane;
+    const float* nb = norms + (n % 3) * 256;
+    const float xi = nb[quad * 32 + lane];
+    float* crow = P.c + I.c_off + (long long)(j0 + half * 64) * I.ld + i;
+    const bool full = i0 + kCostM <= I.m && j0 + kCostN <= I.n;
+    const bool row_in = i < I.m;
 #pragma unroll
-      for (int e = 0; e < 32; ++e) {
-        const int j = j0 + cb + e;
-        if (j < I.n) {
-          float v = fmaf(-2.0f, __uint_as_float(r[e]), xi + yn[cb + e]);
+    for (int cb = 0; cb < 64; cb += 32) {
+      uint32_t r[32];
+      const uint32_t taddr = tmem + (uint32_t)(b * kCostN) + ((uint32_t)(quad * 32) << 16) +
+                             (uint32_t)(half * 64 + cb);
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+          "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+            "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+            "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+            "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+            "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+            "=r"(r[31])
+          : "r"(taddr) : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      const float* yn = nb + kCostM + half * 64 + cb;
+      float* cp = crow + (long long)cb * I.ld;
+      if (full) {
+#pragma unroll
+        for (int e = 0; e < 32; ++e) {
+          float v = fmaf(-2.0f, __uint_as_float(r[e]), xi + yn[e]);
           if (P.clamp) v = fmaxf(v, 0.0f);
-          crow[(long long)j * I.ld] = v * P.scale;
+          cp[(long long)e * I.ld] = v * P.scale;
+        }
+      } else if (row_in) {
+        const int jb = j0 + half * 64 + cb;
+#pragma unroll
+        for (int e = 0; e < 32; ++e) {
+          if (jb + e < I.n) {
+            float v = fmaf(-2.0f, __uint_as_float(r[e]), xi + yn[e]);
+            if (P.clamp) v = fmaxf(v, 0.0f);
+            cp[(long long)e * I.ld] = v * P.scale;
+          }
         }
       }
     }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    kk = kn;
+    i0 = in0;
+    j0 = jn0;
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
-                 :: "r"(tmem), "r"((uint32_t)kCostN) : "memory");
+                 :: "r"(tmem), "r"((uint32_t)(2 * kCostN)) : "memory");
 }
 
 static size_t cost_smem_bytes(int dim) {
-  return (size_t)(kCostM + kCostN) * dim * 4 * 2 + sizeof(float) * (kCostM + kCostN);
+  // two operand buffers (x hi / lo, y hi / lo: 4 x 128 rows x dim floats) + [3][256] norms
+  return (size_t)2 * 4 * kCostM * dim * 4 + sizeof(float) * 3 * 256;
 }
 
 // ---------------------------------------------------------------------------
@@ -511,7 +560,7 @@ int drot_sqeuclidean_cost(int n_inst, const drot_cost_instance* inst, const floa
   if (!err_flag[dev] && cudaMalloc(&err_flag[dev], sizeof(int)) != cudaSuccess) return DROT_ERR_CUDA;
   int* err = err_flag[dev];
   memset(&P, 0, sizeof(P));
-  int max_tiles = 0;
+  long long total_tiles = 0;
   for (int k = 0; k < n_inst; ++k) {
     const drot_cost_instance& a = inst[k];
     if (a.m <= 0 || a.n <= 0 || a.ld < a.m || a.x_offset < 0 || a.y_offset < 0 ||
@@ -528,7 +577,9 @@ int drot_sqeuclidean_cost(int n_inst, const drot_cost_instance* inst, const floa
     const long long tiles = (long long)I.tiles_m * ((a.n + kCostN - 1) / kCostN);
     if (tiles > 65535LL * 1024) return DROT_ERR_UNSUPPORTED;
     I.tiles = (int)tiles;
-    max_tiles = std::max(max_tiles, I.tiles);
+    I.tile0 = (int)total_tiles;
+    total_tiles += tiles;
+    if (total_tiles > (1LL << 30)) return DROT_ERR_UNSUPPORTED;
   }
   cudaStream_t st = (cudaStream_t)stream;
   P.x = x;
@@ -540,12 +591,22 @@ int drot_sqeuclidean_cost(int n_inst, const drot_cost_instance* inst, const floa
   P.n_inst = n_inst;
   P.clamp = clamp ? 1 : 0;
   P.scale = scale;
+  P.total_tiles = (int)total_tiles;
   const size_t smem = cost_smem_bytes(dim);
   if (cudaFuncSetAttribute((const void*)cost_sqeuclid_kernel,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return DROT_ERR_CUDA;
+  // Persistent grid: the resident CTAs, at most two per SM (each holds 256
+  // of the SM's 512 TMEM columns, so a third would wait on its allocation).
+  int sms = 0, per_sm = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cost_sqeuclid_kernel, kCostThreads,
+                                                    smem) != cudaSuccess)
+    return DROT_ERR_CUDA;
+  per_sm = std::max(1, std::min(per_sm, 2));
+  const int grid = (int)std::min<long long>(total_tiles, (long long)sms * per_sm);
   if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) return DROT_ERR_CUDA;
-  cost_sqeuclid_kernel<<<dim3(max_tiles, n_inst), kCostThreads, smem, st>>>(P);
+  cost_sqeuclid_kernel<<<grid, kCostThreads, smem, st>>>(P);
   if (cudaGetLastError() != cudaSuccess) return DROT_ERR_CUDA;
   int h_err = 0;
   if (cudaMemcpyAsync(&h_err, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||

@@ -24,7 +24,7 @@ import torch
 from ._lib import DrotError, DrotResult, check, lib, status_string  # noqa: F401
 
 __all__ = ["quadratic_drot", "group_lasso_drot", "solve_qr", "solve_gl", "DrotError",
-           "group_bounds", "workspace_bytes"]
+           "group_bounds", "workspace_bytes", "tune"]
 
 
 C_F32, C_BF16 = 0, 1  # DROT_C_F32 / DROT_C_BF16 of drot_gb300.h
@@ -166,3 +166,9 @@ def group_bounds(n_rows, n_class):
 
 
 ctypes_byref = ctypes.byref
+
+
+def tune(kind, c, p, q, rho, r_weight, n_class=1, iters=200, repeats=2, stream=None):
+    """Autotune the launch shape of this problem shape (reg_drot.autotune.tune)."""
+    from .autotune import tune as _tune
+    return _tune(kind, c, p, q, rho, r_weight, n_class, iters, repeats, stream)

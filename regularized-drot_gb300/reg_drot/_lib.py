@@ -70,6 +70,11 @@ class DrotAdjointInstance(ctypes.Structure):
 _AIP = ctypes.POINTER(DrotAdjointInstance)
 
 
+class DrotLaunchChoice(ctypes.Structure):
+    _fields_ = [("vectors_per_lane", ctypes.c_int), ("warps_per_cta", ctypes.c_int),
+                ("data_path", ctypes.c_int), ("ctas_per_sm", ctypes.c_int)]
+
+
 class DrotCostInstance(ctypes.Structure):
     _fields_ = [
         ("m", ctypes.c_int), ("n", ctypes.c_int), ("ld", ctypes.c_int), ("pad", ctypes.c_int),
@@ -80,9 +85,31 @@ class DrotCostInstance(ctypes.Structure):
 
 _CIP = ctypes.POINTER(DrotCostInstance)
 _BIP = ctypes.POINTER(DrotBatchInstance)
+
+
+class DrotGlBatchInstance(ctypes.Structure):
+    _fields_ = [
+        ("n_rows", ctypes.c_int), ("n_cols", ctypes.c_int), ("ld", ctypes.c_int),
+        ("n_groups", ctypes.c_int),
+        ("c_offset", ctypes.c_longlong), ("x_offset", ctypes.c_longlong),
+        ("p_offset", ctypes.c_longlong), ("q_offset", ctypes.c_longlong),
+        ("rho", ctypes.c_float), ("lambda_", ctypes.c_float), ("eps", ctypes.c_float),
+        ("pad", ctypes.c_float),
+    ]
+
+
+class DrotBatchTuning(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("fine_cols", "finest_cols", "item_lines",
+                                           "finest_item_lines", "level_quarters",
+                                           "prefetch_distance")]
+
+
 _BRP = ctypes.POINTER(DrotBatchResult)
 
 SIGNATURES = {
+    "drot_set_launch_choice": (_c_int, [_c_int, _c_int, _c_int, _c_int, _c_int,
+                                        ctypes.POINTER(DrotLaunchChoice)]),
+    "drot_clear_launch_choices": (_c_int, []),
     "drot_status_string": (ctypes.c_char_p, [_c_int]),
     "drot_last_status": (_c_int, []),
     "drot_q_get_work_size_update_x": (_c_int, [_c_int, _c_int]),
@@ -130,8 +157,12 @@ SIGNATURES = {
                                              _c_int, _c_float, _vp, _RP, _vp]),
     "drot_batch_plan_create": (_c_int, [_c_int, _BIP, _c_int, ctypes.POINTER(_vp)]),
     "drot_batch_plan_create_ex": (_c_int, [_c_int, _BIP, _c_int, _c_int, ctypes.POINTER(_vp)]),
+    "drot_batch_state_ex": (_c_int, [_vp, _vp] + [ctypes.POINTER(_vp)] * 5),
+    "drot_gl_batch_plan_create": (_c_int, [_c_int, ctypes.POINTER(DrotGlBatchInstance), _c_int,
+                                           ctypes.POINTER(_vp)]),
     "drot_qr_batch_launch_points": (_c_int, [_vp, _vp, _vp, _c_int, _c_float, _vp, _vp, _vp, _c_int,
                                              _vp, _c_size, _vp]),
+    "drot_batch_set_tuning": (_c_int, [ctypes.POINTER(DrotBatchTuning)]),
     "drot_batch_plan_destroy": (None, [_vp]),
     "drot_batch_plan_workspace_bytes": (_c_size, [_vp]),
     "drot_batch_plan_tiles": (_c_int, [_vp]),

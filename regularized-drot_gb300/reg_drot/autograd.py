@@ -352,41 +352,111 @@ class GroupLassoDROTFn(torch.autograd.Function):
     def backward(ctx, gx):
         c, p, q = ctx.saved_tensors
         nr, nc, G, s, lam, seg, T, t_lo = ctx.meta
-        dev = c.device
-        st = _GLState(c.detach(), p.detach(), q.detach(), G, s, lam)
-        xbar = gx.detach().float().contiguous().clone()
-        vbar = torch.zeros(2 * (nr + nc) + 1, device=dev)
-        cbar = torch.zeros(c.shape, dtype=torch.float32, device=dev)
-        pbar = torch.zeros(nr, device=dev)
-        qbar = torch.zeros(nc, device=dev)
-        with torch.cuda.device(dev):
-            abytes = int(lib().drot_gl_adjoint_workspace_bytes(nr, nc, G))
-        if abytes == 0:
-            raise RuntimeError("group_lasso_drot_fn: shape unsupported by the adjoint")
-        aws = torch.empty(abytes + 256, dtype=torch.uint8, device=dev)
-        aptr = aws.data_ptr() + (-aws.data_ptr()) % 256
-        cdt = C_BF16 if c.dtype == torch.bfloat16 else C_F32
-        states = torch.empty(seg * (nr * nc + nr + nc), device=dev)
-        t = st.t
-        for si, snap in reversed(ctx.checkpoints):
-            k0 = si * seg
-            k1 = min(k0 + seg, T)
-            if k1 <= t_lo:
-                break
-            st.restore(snap)
-            if k0 < t_lo:
-                # truncated adjoint: advance to its first iteration without it
-                st.run(t_lo - k0, -1.0)
-                k0 = t_lo
-            with torch.cuda.device(dev):
-                rc = lib().drot_gl_adjoint_segment(
-                    c.data_ptr(), cdt, p.data_ptr(), q.data_ptr(), nr, nc, G, s, lam,
-                    t["x"].data_ptr(), t["a"].data_ptr(), t["b"].data_ptr(), t["phi1"].data_ptr(),
-                    t["phi2"].data_ptr(), t["alpha"].data_ptr(), k1 - k0, states.data_ptr(),
-                    st.wptr, st.nbytes, xbar.data_ptr(), vbar.data_ptr(), cbar.data_ptr(),
-                    pbar.data_ptr(), qbar.data_ptr(), aptr, abytes, st.stream())
-            check(rc, "gl_adjoint_segment")
+        cbar, pbar, qbar = _gl_unrolled_backward(c, p, q, G, s, lam, seg, ctx.checkpoints, T,
+                                                 t_lo, gx.detach().float().contiguous())
         return cbar.to(c.dtype), pbar, qbar, None, None, None, None, None, None, None, None
+
+
+def _gl_unrolled_backward(c, p, q, G, s, lam, seg, checkpoints, T, t_lo, xbar):
+    """Adjoint of GL iterations [t_lo, T) (checkpoints: (segment index,
+    state) of the segments covering them, every `seg` iterations from 0)
+    applied to xbar = dL/dX at T; returns (dL/dC, dL/dp, dL/dq)."""
+    nc, nr = c.shape
+    dev = c.device
+    st = _GLState(c.detach(), p.detach(), q.detach(), G, s, lam)
+    xbar = xbar.clone()
+    vbar = torch.zeros(2 * (nr + nc) + 1, device=dev)
+    cbar = torch.zeros(c.shape, dtype=torch.float32, device=dev)
+    pbar = torch.zeros(nr, device=dev)
+    qbar = torch.zeros(nc, device=dev)
+    with torch.cuda.device(dev):
+        abytes = int(lib().drot_gl_adjoint_workspace_bytes(nr, nc, G))
+    if abytes == 0:
+        raise RuntimeError("group_lasso_drot_fn: shape unsupported by the adjoint")
+    aws = torch.empty(abytes + 256, dtype=torch.uint8, device=dev)
+    aptr = aws.data_ptr() + (-aws.data_ptr()) % 256
+    cdt = C_BF16 if c.dtype == torch.bfloat16 else C_F32
+    states = torch.empty(seg * (nr * nc + nr + nc), device=dev)
+    t = st.t
+    for si, snap in reversed(checkpoints):
+        k0 = si * seg
+        k1 = min(k0 + seg, T)
+        if k1 <= t_lo:
+            break
+        st.restore(snap)
+        if k0 < t_lo:
+            # truncated adjoint: advance to its first iteration without it
+            st.run(t_lo - k0, -1.0)
+            k0 = t_lo
+        with torch.cuda.device(dev):
+            rc = lib().drot_gl_adjoint_segment(
+                c.data_ptr(), cdt, p.data_ptr(), q.data_ptr(), nr, nc, G, s, lam,
+                t["x"].data_ptr(), t["a"].data_ptr(), t["b"].data_ptr(), t["phi1"].data_ptr(),
+                t["phi2"].data_ptr(), t["alpha"].data_ptr(), k1 - k0, states.data_ptr(),
+                st.wptr, st.nbytes, xbar.data_ptr(), vbar.data_ptr(), cbar.data_ptr(),
+                pbar.data_ptr(), qbar.data_ptr(), aptr, abytes, st.stream())
+        check(rc, "gl_adjoint_segment")
+    return cbar, pbar, qbar
+
+
+class BatchGroupLassoDROTFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, c, p, q, batch, max_iters, last_k, segment):
+        x, info = batch.solve(c.detach(), p.detach(), q.detach(), max_iters)
+        if not all(r["converged"] for r in info):
+            warnings.warn("batch_group_lasso_drot_fn: some instances did not converge; the "
+                          "adjoint is taken at the last iterate")
+        ctx.save_for_backward(c, p, q)
+        ctx.batch, ctx.last_k, ctx.seg = batch, int(last_k), int(segment)
+        ctx.state = batch.state(info)
+        ctx.x = x.detach().clone()
+        ctx.info = info
+        return x
+
+    @staticmethod
+    def backward(ctx, gx):
+        c, p, q = ctx.saved_tensors
+        B = ctx.batch
+        G = gx.detach().float()
+        cbar = torch.zeros(c.shape, dtype=torch.float32, device=c.device)
+        pbars, qbars = [], []
+        prow = pcol = 0
+        for k, (nr, nc) in enumerate(B.shapes):
+            s, lam = B.step_sizes()[k], B.lambdas[k]
+            ck = B.view(c.detach(), k).contiguous()
+            pk, qk = p.detach()[prow:prow + nr], q.detach()[pcol:pcol + nc]
+            # the K steps taken from the solution: checkpoints every `seg`
+            # iterations of a run that starts at the final state
+            st = _GLState(ck, pk, qk, B.n_class[k], s, lam)
+            init = dict(ctx.state[k], x=B.view(ctx.x, k).contiguous())
+            st.restore(init)
+            checkpoints, T = [], 0
+            while T < ctx.last_k:
+                checkpoints.append((T // ctx.seg, st.snapshot()))
+                n = min(ctx.seg, ctx.last_k - T)
+                st.run(n, -1.0)
+                T += n
+            cb, pb, qb = _gl_unrolled_backward(ck, pk, qk, B.n_class[k], s, lam, ctx.seg,
+                                               checkpoints, T, 0,
+                                               B.view(G, k).contiguous())
+            B.view(cbar, k).copy_(cb)
+            pbars.append(pb)
+            qbars.append(qb)
+            prow += nr
+            pcol += nc
+        return cbar.to(c.dtype), torch.cat(pbars), torch.cat(qbars), None, None, None, None
+
+
+def batch_group_lasso_drot_fn(batch, c, p, q, max_iters, *, last_k=64, segment=32):
+    """GLBatch.solve with a backward: for every instance, the unrolled
+    adjoint of last_k GL iterations taken from its solution (the state the
+    batched solve stopped at, held fixed) -- the truncated adjoint at the
+    fixed point, where last_k more iterations leave the plan within the stop
+    tolerance.  c, p, q packed (GLBatch.pack_c / pack_marginals)."""
+    if int(last_k) <= 0:
+        raise RuntimeError("last_k must be positive")
+    return BatchGroupLassoDROTFn.apply(c, p, q, batch, int(max_iters), int(last_k),
+                                       int(segment))
 
 
 def group_lasso_drot_fn(c, p, q, n_class, rho, r_weight, max_iters, eps, *, segment=32,
@@ -407,5 +477,6 @@ def group_lasso_drot_fn(c, p, q, n_class, rho, r_weight, max_iters, eps, *, segm
                                   None if last_k is None else int(last_k))
 
 
-__all__ = ["quadratic_drot_fn", "batch_quadratic_drot_fn", "group_lasso_drot_fn", "qr_lambda",
+__all__ = ["quadratic_drot_fn", "batch_quadratic_drot_fn", "group_lasso_drot_fn",
+           "batch_group_lasso_drot_fn", "qr_lambda",
            "step_and_kappa", "gl_step_and_lambda"]

@@ -24,14 +24,57 @@ cooperative launch), so it can be captured in a CUDA graph
 width by timing short runs of each candidate on the caller's data.
 """
 import ctypes
+import threading
 
 import torch
 
-from ._lib import DrotBatchInstance, DrotBatchResult, DrotError, check, lib
+from ._lib import (DrotBatchInstance, DrotBatchResult, DrotBatchTuning, DrotError,
+                   DrotGlBatchInstance, check, lib)
 
 C_F32, C_BF16 = 0, 1
 TILE_CANDIDATES = (32, 64, 128, 256)
 _ALIGN = 32  # elements between instance blocks (128 bytes of FP32)
+
+
+_TUNING_FIELDS = ("fine_cols", "finest_cols", "item_lines", "finest_item_lines",
+                  "level_quarters", "prefetch_distance")
+_tuning_lock = threading.Lock()
+_tuning = {}
+
+
+def _apply_tuning(t):
+    v = DrotBatchTuning(*(int(t.get(f, -1)) for f in _TUNING_FIELDS))
+    check(lib().drot_batch_set_tuning(ctypes.byref(v)), "drot_batch_set_tuning")
+
+
+def set_tuning(**fields):
+    """Tile-level shape of the batch plans created afterwards (process-wide;
+    drot_batch_set_tuning).  Fields left out or below 0 keep the default:
+    fine_cols 128, finest_cols 32 (0: no third level), item_lines 1024,
+    finest_item_lines 64, level_quarters 8 (0: keep the coarse tiles),
+    prefetch_distance 1 (0: off).  ``set_tuning()`` restores the defaults.
+    Plans already built keep theirs; a batch built with ``tuning=`` uses its
+    own."""
+    bad = set(fields) - set(_TUNING_FIELDS)
+    if bad:
+        raise RuntimeError(f"unknown tuning fields {sorted(bad)}")
+    global _tuning
+    with _tuning_lock:
+        _apply_tuning(fields)
+        _tuning = dict(fields)
+
+
+def _create_plan(fn, tuning, *args):
+    """fn(*args) with the batch's own tuning in force (the process-wide one
+    restored after)."""
+    with _tuning_lock:
+        if tuning is None:
+            return fn(*args)
+        _apply_tuning(tuning)
+        try:
+            return fn(*args)
+        finally:
+            _apply_tuning(_tuning)
 
 
 def _as_list(v, n, name):
@@ -46,7 +89,7 @@ class QRBatch:
     """A fixed set of instance shapes and parameters, planned once."""
 
     def __init__(self, shapes, rho, r_weight, eps, *, device=None, cols_per_tile=None,
-                 band_rows=512):
+                 band_rows=512, tuning=None):
         shapes = [(int(a), int(b)) for a, b in shapes]
         if not shapes:
             raise RuntimeError("QRBatch needs at least one instance")
@@ -89,6 +132,9 @@ class QRBatch:
         if band_rows not in (128, 512):
             raise RuntimeError("band_rows must be 128 or 512")
         self.band_rows = band_rows  # 128: plans for point-cloud launches (solve_points)
+        if tuning is not None and set(tuning) - set(_TUNING_FIELDS):
+            raise RuntimeError(f"unknown tuning fields {sorted(set(tuning) - set(_TUNING_FIELDS))}")
+        self.tuning = None if tuning is None else dict(tuning)  # tile levels (set_tuning)
 
     # ------------------------------------------------------------------ packing
     def pack_c(self, costs, dtype=torch.float32):
@@ -126,8 +172,9 @@ class QRBatch:
         if cpt not in self._plans:
             h = ctypes.c_void_p()
             with torch.cuda.device(self.device):
-                check(lib().drot_batch_plan_create_ex(self.n, self._desc, cpt, self.band_rows,
-                                                      ctypes.byref(h)), "batch_plan_create")
+                check(_create_plan(lib().drot_batch_plan_create_ex, self.tuning, self.n,
+                                   self._desc, cpt, self.band_rows, ctypes.byref(h)),
+                      "batch_plan_create")
             self._plans[cpt] = h
         return self._plans[cpt]
 
@@ -248,6 +295,30 @@ class QRBatch:
         phi2 = self._ws[o2:o2 + 4 * self.total_cols].view(torch.float32).clone()
         return phi1, phi2
 
+    def state(self, info=None):
+        """Per-instance copies of the final solver state after the last launch:
+        dicts (x, a, b, phi1, phi2, alpha) with x in the [n_cols, n_rows]
+        layout -- the state drot_gl_solve / drot_qr_solve continue from.
+        info: the launch's results (their iters_run give alpha's parity)."""
+        info = self.results() if info is None else info
+        h, ptr, _ = self.workspace_for(self._ws_plan or self.cols_per_tile or 128)
+        vp = [ctypes.c_void_p() for _ in range(5)]
+        check(lib().drot_batch_state_ex(h, ptr, *[ctypes.byref(v) for v in vp]), "batch_state_ex")
+        base = self._ws.data_ptr()
+
+        def vec(ptr_v, off, n):
+            o = ptr_v.value - base + 4 * off
+            return self._ws[o:o + 4 * n].view(torch.float32).clone()
+        out, prow, pcol = [], 0, 0
+        for k, (nr, nc) in enumerate(self.shapes):
+            par = int(info[k]["iters_run"]) & 1
+            out.append({"a": vec(vp[0], prow, nr), "b": vec(vp[1], pcol, nc),
+                        "phi1": vec(vp[2], prow, nr), "phi2": vec(vp[3], pcol, nc),
+                        "alpha": vec(vp[4], par * self.n + k, 1)})
+            prow += nr
+            pcol += nc
+        return out
+
     def step_sizes(self):
         """s = rho / (n_rows + n_cols) of every instance (FP32, as the solver)."""
         import numpy as np
@@ -310,4 +381,54 @@ class QRBatch:
         self._plans = {}
 
 
-__all__ = ["QRBatch", "DrotError", "TILE_CANDIDATES"]
+class GLBatch(QRBatch):
+    """Many group-lasso instances in one persistent launch
+    (drot_gl_batch_plan_create): per instance the loop of
+    reg_drot.group_lasso_drot -- n_class contiguous row classes with the
+    reference's boundaries, the stop test on every iteration (residual <=
+    eps), n_iter = iterations run, X never folded.  The threshold is
+    r_weight * sqrt(n_rows // n_class) (convention="operator", the PyTorch
+    operator) or r_weight / sqrt(n_rows // n_class) (convention="wrapper",
+    the C++ wrapper).  Packing, launch, capture and results as QRBatch;
+    classes of at most 4096 rows; cost matrices only (no point launches)."""
+
+    def __init__(self, shapes, n_class, rho, r_weight, eps, *, device=None, cols_per_tile=None,
+                 convention="operator", tuning=None):
+        super().__init__(shapes, rho, r_weight, eps, device=device, cols_per_tile=cols_per_tile,
+                         tuning=tuning)
+        from .autograd import gl_step_and_lambda
+        self.n_class = [int(v) for v in (n_class if isinstance(n_class, (list, tuple))
+                                         else [n_class] * self.n)]
+        if len(self.n_class) != self.n:
+            raise RuntimeError("n_class needs one value per instance")
+        self.convention = convention
+        self.lambdas = [gl_step_and_lambda(self.rho[k], self.r_weight[k], nr, nc,
+                                           self.n_class[k], convention)[1]
+                        for k, (nr, nc) in enumerate(self.shapes)]
+        desc = (DrotGlBatchInstance * self.n)()
+        for k, (nr, nc) in enumerate(self.shapes):
+            src, d = self._desc[k], desc[k]
+            d.n_rows, d.n_cols, d.ld, d.n_groups = nr, nc, src.ld, self.n_class[k]
+            d.c_offset, d.x_offset = src.c_offset, src.x_offset
+            d.p_offset, d.q_offset = src.p_offset, src.q_offset
+            d.rho, d.lambda_, d.eps = src.rho, self.lambdas[k], src.eps
+        self._gl_desc = desc
+
+    def _plan(self, cols_per_tile):
+        cpt = int(cols_per_tile)
+        if cpt not in self._plans:
+            h = ctypes.c_void_p()
+            with torch.cuda.device(self.device):
+                check(_create_plan(lib().drot_gl_batch_plan_create, self.tuning, self.n,
+                                   self._gl_desc, cpt, ctypes.byref(h)),
+                      "gl_batch_plan_create")
+            self._plans[cpt] = h
+        return self._plans[cpt]
+
+    def launch_points(self, *args, **kwargs):
+        raise RuntimeError("GLBatch solves cost matrices only")
+
+    solve_points = launch_points
+
+
+__all__ = ["QRBatch", "GLBatch", "DrotError", "TILE_CANDIDATES", "set_tuning"]

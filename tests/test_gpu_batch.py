@@ -46,10 +46,11 @@ def _instance(nr, nc, seed, marg="uniform"):
     return c, p, q
 
 
-def _batch(shapes, cuda, rho=2.0, rw=1e-3, eps=1e-4, marg="uniform", cpt=None, dtype=None):
+def _batch(shapes, cuda, rho=2.0, rw=1e-3, eps=1e-4, marg="uniform", cpt=None, dtype=None,
+           tuning=None):
     from reg_drot.batch import QRBatch
     insts = [_instance(nr, nc, 100 + k, marg) for k, (nr, nc) in enumerate(shapes)]
-    B = QRBatch(shapes, rho, rw, eps, device=cuda, cols_per_tile=cpt)
+    B = QRBatch(shapes, rho, rw, eps, device=cuda, cols_per_tile=cpt, tuning=tuning)
     c = B.pack_c([i[0].to(cuda) for i in insts], dtype=dtype or torch.float32)
     p, q = B.pack_marginals([i[1] for i in insts], [i[2] for i in insts])
     return B, insts, c, p, q
@@ -208,16 +209,17 @@ def test_batch_with_more_tiles_than_ctas(cuda, solver_lib):
     assert len({r["n_iter"] for r in info}) > 1
 
 
-@pytest.mark.parametrize("env", [{"DROT_BATCH_FINEST_COLS": "0"},
-                                 {"DROT_BATCH_FINEST_COLS": "0", "DROT_BATCH_FINE_DIV": "0"}])
-def test_batch_tile_levels_match_oracle(cuda, solver_lib, monkeypatch, env):
+@pytest.mark.parametrize("tuning", [{"finest_cols": 0},
+                                    {"finest_cols": 0, "level_quarters": 0},
+                                    {"prefetch_distance": 0, "item_lines": 256},
+                                    {"fine_cols": 64, "finest_cols": 16, "level_quarters": 64}])
+def test_batch_tile_levels_match_oracle(cuda, solver_lib, tuning):
     # The default plan moves to 128-column and then 32-column tiles (with
     # 64-line dual items) as instances converge; these plans stop at the
-    # fine level or keep the coarse tiles throughout.  Every level must give
-    # the oracle's solution.
-    for k, v in env.items():
-        monkeypatch.setenv(k, v)
-    B, insts, c, p, q = _batch(SHAPES, cuda, marg="dirichlet", cpt=256)
+    # fine level, keep the coarse tiles throughout, use short dual items
+    # without the prefetch, or move early to narrower levels.  Every
+    # schedule must give the oracle's solution.
+    B, insts, c, p, q = _batch(SHAPES, cuda, marg="dirichlet", cpt=256, tuning=tuning)
     x, info = B.solve(c, p, q, 20000)
     xs = B.unpack(x)
     for k, (ci, pi, qi) in enumerate(insts):

@@ -20,9 +20,9 @@ the iterates agree to FP32 rounding:
     X and the objective are compared on every run: when the QR stop moved,
     against the oracle stopped at the solver's iteration
     (oracle.quadratic_drot_at).
-Each parity case runs on both data paths: the register path (the default,
-DROT_PATH=reg) and the TMA shared-memory ring (DROT_PATH=tma, shapes with
-n_rows % 4 == 0).
+Each parity case runs on both data paths: the register path (the default)
+and the TMA shared-memory ring (pinned for every shape through
+drot_set_launch_choice, shapes with n_rows % 4 == 0).
 """
 import ctypes
 import json
@@ -43,9 +43,13 @@ RTOL_OBJ = 1e-5
 
 
 @pytest.fixture(params=["reg", "tma"])
-def path(request, monkeypatch):
-    monkeypatch.setenv("DROT_PATH", request.param)
-    return request.param
+def path(request, cuda):
+    from reg_drot import autotune
+    if request.param == "tma":
+        for kind in ("qr", "gl"):
+            autotune.pin(kind, 0, 0, data_path=1)
+    yield request.param
+    autotune.clear()
 
 
 def _tma_needs_aligned_rows(path, nr):
