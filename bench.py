@@ -904,9 +904,12 @@ def run_batch_timeline(workload="config4"):
                      "rest_even_us": float(np.nanmean(rest[sl][ev])),
                      "rest_odd_us": float(np.nanmean(rest[sl][~ev])),
                      "seconds": float(np.nansum(total[sl]) / 1e6)})
+    slowest = sorted(zip(it.tolist(), shapes), reverse=True)[:8]
     print(json.dumps({"case": f"batchlog:{workload}", "cols_per_tile": cpt, "tiles": B.tiles(cpt),
                       "s_per_batch": a.elapsed_time(b) / 1e3,
-                      "n_iter_max": int(it.max()), "ranges": rows}), flush=True)
+                      "n_iter_max": int(it.max()),
+                      "slowest": [[n, list(sh)] for n, sh in slowest],
+                      "ranges": rows}), flush=True)
     return 0
 
 

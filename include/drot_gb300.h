@@ -367,11 +367,16 @@ int drot_gl_batch_plan_create(int n_inst, const drot_gl_batch_instance *inst,
  *                            (0: stay on the coarse tiles)
  *   prefetch_distance    1   L2 prefetch of the fused update, warp steps
  *                            ahead (0..8; 0: off)
+ *   tail_quarters        4   the smallest unconverged instances, last in
+ *                            each iteration's tile order, take the finest
+ *                            tiles up to tail_quarters / 4 x the grid of
+ *                            them and the fine tiles up to twice that, so
+ *                            an iteration ends on short tiles (0: off)
  * Tuning changes the schedule, not the arithmetic of an instance: every
  * setting gives the same iterates up to summation order. */
 typedef struct {
   int fine_cols, finest_cols, item_lines, finest_item_lines, level_quarters,
-      prefetch_distance;
+      prefetch_distance, tail_quarters;
 } drot_batch_tuning;
 int drot_batch_set_tuning(const drot_batch_tuning *tuning);
 void drot_batch_plan_destroy(drot_batch_plan plan);

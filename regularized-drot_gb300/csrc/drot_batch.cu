@@ -79,9 +79,11 @@ struct BatchParams {
   int n_tiles_x;       // finest tiles, stored after the fine ones
   int n_items_x;       // short items of the finest level, stored after the n_items others
   const int* order;    // instances by decreasing size (the order of the active lists)
-  int* act;            // active lists: tile indices per level in the tiles' own index
-                       // ranges, then item indices (n_tiles + ... entries, then items)
-  int fine_threshold;  // next (finer) list once fewer active tiles of the current one remain
+  int* act;            // active lists: tile indices (at most n_tiles + n_tiles_f + n_tiles_x
+                       // entries), then dual-update item indices
+  int* ilvl;           // per instance: its tile level in the current lists
+  int fine_threshold;  // next (finer) base level once fewer active tiles of the current one remain
+  int tail_tiles;      // smallest instances at finer levels (build_active_lists); 0 off
   float *a, *b, *phi1, *phi2;  // packed state
   float* alpha;                // [2][n_inst], by iteration parity
   float2* res_slot;            // per item: squared residual (float pair)
@@ -98,8 +100,8 @@ struct BatchParams {
   int dim;
   unsigned* counters;  // [0], [1]: tile counters of even / odd iterations; [2]: converged
                        // instances; [3]: coarse tiles of unconverged instances;
-                       // [8..12]: lengths of the active lists (tiles of levels 0-2,
-                       // items, short items)
+                       // [8..10]: their tiles per level; [13]: base level;
+                       // [14], [15]: lengths of the tile and item lists
   unsigned* bar;
   int* abort_flag;
   long long timeout_ns;
@@ -583,58 +585,118 @@ __global__ void point_norms_kernel(const float* pts, int n, int dim, float* out)
   }
 }
 
-// Active lists (CTA 0, all threads): the tiles of every level and the
-// dual-update items of the unconverged instances, largest instances first
-// (P.order), so the fused update and the dual update never step over
-// converged instances and the last tiles taken in an iteration are small
-// ones (the wait at the following barrier is the length of the last tile).
-// Rebuilt at the start and whenever an instance converged (at most once per
-// instance); a grid barrier publishes them.  scan: 5 * blockDim ints.
-__device__ void build_active_lists(const BatchParams& P, int* scan) {
+// Inclusive block-wide scan of Q ints per thread over `scan` (Q * blockDim
+// ints of shared memory); every thread gets its inclusive prefix.
+template <int Q>
+__device__ __forceinline__ void block_scan_incl(int (&v)[Q], int* scan) {
   const int tid = threadIdx.x, nt = blockDim.x;
-  const int base[5] = {0, P.n_tiles, P.n_tiles + P.n_tiles_f, 0, P.n_items};
-  const int T = P.n_tiles + P.n_tiles_f + P.n_tiles_x;
-  __shared__ int s_carry[5];  // running totals of the lists
-  if (tid < 5) s_carry[tid] = 0;
+#pragma unroll
+  for (int l = 0; l < Q; ++l) scan[l * nt + tid] = v[l];
   __syncthreads();
-  for (int k0 = 0; k0 < P.n_inst; k0 += nt) {
-    const int k = k0 + tid < P.n_inst ? P.order[k0 + tid] : -1;
-    int cnt[5] = {0, 0, 0, 0, 0};
-    BatchInst I;
-    const bool live = k >= 0 && !__ldcg(P.conv + k);
-    if (live) {
-      I = P.inst[k];
-      cnt[0] = I.ntiles;
-      cnt[1] = P.n_tiles_f > 0 ? I.ntilesf : 0;
-      cnt[2] = P.n_tiles_x > 0 ? I.ntilesx : 0;
-      cnt[3] = I.nitems;
-      cnt[4] = P.n_items_x > 0 ? I.nitemsx : 0;
-    }
+  for (int o = 1; o < nt; o <<= 1) {  // Hillis-Steele
+    int u[Q];
 #pragma unroll
-    for (int l = 0; l < 5; ++l) scan[l * nt + tid] = cnt[l];
+    for (int l = 0; l < Q; ++l) u[l] = tid >= o ? scan[l * nt + tid - o] : 0;
     __syncthreads();
-    for (int o = 1; o < nt; o <<= 1) {  // inclusive Hillis-Steele scan
-      int v[5];
 #pragma unroll
-      for (int l = 0; l < 5; ++l) v[l] = tid >= o ? scan[l * nt + tid - o] : 0;
-      __syncthreads();
-#pragma unroll
-      for (int l = 0; l < 5; ++l) scan[l * nt + tid] += v[l];
-      __syncthreads();
-    }
-    if (live) {
-      const int src0[5] = {I.tile0, I.tile0f, I.tile0x, I.item0, I.item0x};
-#pragma unroll
-      for (int l = 0; l < 5; ++l) {
-        int* dst = P.act + (l < 3 ? 0 : T) + base[l] + s_carry[l] + scan[l * nt + tid] - cnt[l];
-        for (int u = 0; u < cnt[l]; ++u) dst[u] = src0[l] + u;
-      }
-    }
-    __syncthreads();
-    if (tid < 5) s_carry[tid] += scan[tid * nt + nt - 1];
+    for (int l = 0; l < Q; ++l) scan[l * nt + tid] += u[l];
     __syncthreads();
   }
-  if (tid < 5) P.counters[8 + tid] = (unsigned)s_carry[tid];
+#pragma unroll
+  for (int l = 0; l < Q; ++l) v[l] = scan[l * nt + tid];
+  __syncthreads();
+}
+
+// Active lists (CTA 0, all threads), rebuilt at the start and whenever an
+// instance converged (at most once per instance; a grid barrier publishes
+// them).  Every unconverged instance gets a tile level: the run's base level
+// -- coarse tiles, then the fine ones once fewer than fine_threshold coarse
+// tiles remain, then the finest ones likewise -- or a finer one for the
+// smallest instances, those at the end of the order: the instances whose
+// finest tiles, counted from the end, number at most tail_tiles take the
+// finest level, those whose fine tiles number at most 2 tail_tiles the fine
+// one.  The tile list holds each instance's tiles at its level, the item
+// list its dual-update items (the finest level's short ones at level 2),
+// largest instances first (P.order): the fused update and the dual update
+// never step over converged instances, and the last tiles taken in an
+// iteration are short ones (the wait at the following barrier is about the
+// length of the last tile).  Published: ilvl[k], counters[8..10] the tiles
+// of each level over unconverged instances, [13] the base level, [14] / [15]
+// the lengths of the tile / item lists.  scan: 2 * blockDim ints.
+__device__ void build_active_lists(const BatchParams& P, int* scan) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int T = P.n_tiles + P.n_tiles_f + P.n_tiles_x;  // item list offset in P.act
+  const bool has_f = P.n_tiles_f > 0, has_x = P.n_tiles_x > 0;
+  __shared__ int s_tot[3], s_carry[4];
+  if (tid < 3) s_tot[tid] = 0;
+  if (tid < 4) s_carry[tid] = 0;
+  __syncthreads();
+  // Tiles of every level over the unconverged instances.
+  {
+    int c[3] = {0, 0, 0};
+    for (int k = tid; k < P.n_inst; k += nt) {
+      if (__ldcg(P.conv + k)) continue;
+      c[0] += P.inst[k].ntiles;
+      c[1] += has_f ? P.inst[k].ntilesf : 0;
+      c[2] += has_x ? P.inst[k].ntilesx : 0;
+    }
+#pragma unroll
+    for (int l = 0; l < 3; ++l) {
+      for (int o = 16; o > 0; o >>= 1) c[l] += __shfl_xor_sync(0xffffffffu, c[l], o);
+      if ((tid & 31) == 0) atomicAdd(&s_tot[l], c[l]);
+    }
+  }
+  __syncthreads();
+  int L = (int)__ldcg(P.counters + 13);
+  if (L == 0 && has_f && s_tot[0] < P.fine_threshold) L = 1;
+  if (L == 1 && has_x && s_tot[1] < P.fine_threshold) L = 2;
+  for (int k0 = 0; k0 < P.n_inst; k0 += nt) {
+    const int k = k0 + tid < P.n_inst ? P.order[k0 + tid] : -1;
+    const bool live = k >= 0 && !__ldcg(P.conv + k);
+    BatchInst I;
+    if (live) I = P.inst[k];
+    // finest / fine tiles from the start of the order through this instance
+    int pre[2] = {live && has_x ? I.ntilesx : 0, live && has_f ? I.ntilesf : 0};
+    const int own[2] = {pre[0], pre[1]};
+    block_scan_incl<2>(pre, scan);
+    int lvl = L;
+    if (live) {
+      const int suf_x = s_tot[2] - (s_carry[0] + pre[0] - own[0]);  // this one and later ones
+      const int suf_f = s_tot[1] - (s_carry[1] + pre[1] - own[1]);
+      if (has_x && suf_x <= P.tail_tiles) lvl = 2;
+      else if (has_f && L < 1 && suf_f <= 2 * P.tail_tiles) lvl = 1;
+    }
+    int cnt[2] = {0, 0};
+    if (live) {
+      cnt[0] = lvl == 0 ? I.ntiles : (lvl == 1 ? I.ntilesf : I.ntilesx);
+      cnt[1] = lvl == 2 ? I.nitemsx : I.nitems;
+    }
+    int off[2] = {cnt[0], cnt[1]};
+    block_scan_incl<2>(off, scan);
+    if (live) {
+      P.ilvl[k] = lvl;
+      const int t0 = lvl == 0 ? I.tile0 : (lvl == 1 ? I.tile0f : I.tile0x);
+      const int q0 = lvl == 2 ? I.item0x : I.item0;
+      int* dt = P.act + s_carry[2] + off[0] - cnt[0];
+      int* dq = P.act + T + s_carry[3] + off[1] - cnt[1];
+      for (int u = 0; u < cnt[0]; ++u) dt[u] = t0 + u;
+      for (int u = 0; u < cnt[1]; ++u) dq[u] = q0 + u;
+    }
+    __syncthreads();
+    if (tid == nt - 1) {
+      s_carry[0] += pre[0];
+      s_carry[1] += pre[1];
+      s_carry[2] += off[0];
+      s_carry[3] += off[1];
+    }
+    __syncthreads();
+  }
+  if (tid < 3) P.counters[8 + tid] = (unsigned)s_tot[tid];
+  if (tid == 0) {
+    P.counters[13] = (unsigned)L;
+    P.counters[14] = (unsigned)s_carry[2];
+    P.counters[15] = (unsigned)s_carry[3];
+  }
 }
 
 // GL = true: the group-lasso iteration (core/drot_glr.hpp:242-355) on plans
@@ -664,26 +726,20 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
   unsigned epoch = 0;
   bool aborted = false;
   int it = 0;
-  // Tile list of the iteration (level 0: coarse, 1: fine, 2: finest, with
-  // its own short dual-update items): the coarse one while enough tiles
-  // remain to keep every CTA busy, then the next finer one.  The switch is
-  // read from the active-tile counts after the decision barrier, so every CTA
-  // switches at the same iteration.
-  const int list1 = P.n_tiles, list2 = P.n_tiles + P.n_tiles_f;
+  // Tile and item lists of the iteration (each unconverged instance at its
+  // own tile level, build_active_lists), read after the barrier that
+  // publishes them, so every CTA uses the same lists.
   const int items0 = P.n_tiles + P.n_tiles_f + P.n_tiles_x;  // item part of P.act
-  int n_act[5];        // active list lengths (tiles of levels 0-2, items, short items)
-  unsigned conv_seen;  // converged instances when the lists were last built
-  int level = 0;
-  // Builds the lists (CTA 0), publishes them and moves to a finer level once
-  // the current one leaves CTAs idle.  False when the run was aborted.
+  int n_list = 0, nq = 0;  // active tiles / dual-update items
+  unsigned conv_seen;      // converged instances when the lists were last built
+  // Builds the lists (CTA 0) and publishes them.  False when the run was
+  // aborted.
   auto rebuild = [&]() -> bool {
     if (blockIdx.x == 0) build_active_lists(P, reinterpret_cast<int*>(smem_raw));
     if (!grid_barrier(P.bar, P.abort_flag, P.timeout_ns, epoch, &s_flag, P.stall_cta)) return false;
-#pragma unroll
-    for (int l = 0; l < 5; ++l) n_act[l] = (int)__ldcg(P.counters + 8 + l);
+    n_list = (int)__ldcg(P.counters + 14);
+    nq = (int)__ldcg(P.counters + 15);
     conv_seen = __ldcg(P.counters + 2);
-    if (level == 0 && P.n_tiles_f > 0 && n_act[0] < P.fine_threshold) level = 1;
-    if (level == 1 && P.n_tiles_x > 0 && n_act[1] < P.fine_threshold) level = 2;
     return true;
   };
   if (!rebuild()) aborted = true;
@@ -696,11 +752,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       P.iter_log[4 * it] = globaltimer_ns();
       P.iter_tiles[it] = __ldcg(P.counters + 3);
     }
-    const int n_list = n_act[level];
-    const int list0 = level == 0 ? 0 : (level == 1 ? list1 : list2);
-    // Active dual-update items of the level: P.act[qa + 0 .. nq).
-    const int qa = items0 + (level == 2 ? P.n_items : 0);
-    const int nq = n_act[level == 2 ? 4 : 3];
+    const int qa = items0;  // active dual-update items: P.act[qa + 0 .. nq)
 
     // ---------------------------------------------------------- fused update
     for (;;) {
@@ -708,7 +760,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
       __syncthreads();
       if (s_tile >= n_list) break;
-      const int t = __ldcg(P.act + list0 + s_tile);
+      const int t = __ldcg(P.act + s_tile);
       const BatchTile T = P.tiles[t];
       if (__ldcg(P.conv + T.inst)) continue;
       const BatchInst I = P.inst[T.inst];
@@ -852,10 +904,11 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       const int k = Q.inst;
       if (__ldcg(P.conv + k)) continue;
       const BatchInst I = P.inst[k];
-      const bool first = qi == (level == 2 ? I.item0x : I.item0);
-      const int t0 = level == 0 ? I.tile0 : (level == 1 ? I.tile0f : I.tile0x);
-      const int ntl = level == 0 ? I.ntiles : (level == 1 ? I.ntilesf : I.ntilesx);
-      const int nchunks = level == 0 ? I.P : (level == 1 ? I.Pf : I.Px);
+      const int lvl = __ldcg(P.ilvl + k);
+      const bool first = qi == (lvl == 2 ? I.item0x : I.item0);
+      const int t0 = lvl == 0 ? I.tile0 : (lvl == 1 ? I.tile0f : I.tile0x);
+      const int ntl = lvl == 0 ? I.ntiles : (lvl == 1 ? I.ntilesf : I.ntilesx);
+      const int nchunks = lvl == 0 ? I.P : (lvl == 1 ? I.Pf : I.Px);
       fpair sg = fp_make(0.0f), og = fp_make(0.0f);
       for (int i = threadIdx.x; i < ntl; i += blockDim.x) {
         const float2 u = __ldcg(P.tile_sum + t0 + i);
@@ -916,8 +969,9 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
           const int qi = __ldcg(P.act + qa + qq);
           const int k = P.items[qi].inst;
           const BatchInst& I = P.inst[k];
-          const int i0 = level == 2 ? I.item0x : I.item0;
-          const int ni = level == 2 ? I.nitemsx : I.nitems;
+          const int lvl = __ldcg(P.ilvl + k);
+          const int i0 = lvl == 2 ? I.item0x : I.item0;
+          const int ni = lvl == 2 ? I.nitemsx : I.nitems;
           if (qi != i0 || __ldcg(P.conv + k)) continue;
           fpair r2 = fp_make(0.0f);
           for (int t = lane; t < ni; t += 32) {
@@ -1033,9 +1087,13 @@ static inline size_t al(size_t v) { return (v + kAl - 1) / kAl * kAl; }
 //  * prefetch_distance 1: on the 64-instance workload (377 M elements, all
 //    active) one warp step ahead took an iteration from 663 to 601 us (0.85
 //    -> 0.94 of the measured HBM copy bandwidth); 2 steps 606 us, 4 steps 647.
+//  * tail_quarters 4: the smallest instances (at the end of every
+//    iteration's tile order) take the finest tiles up to tail_quarters / 4 x
+//    the grid of them, and the fine tiles up to twice that, so the last
+//    tiles of an iteration are short (0: every instance at the base level).
 struct BatchTuning {
   int fine_cols = 128, finest_cols = 32, item_lines = 1024, finest_item_lines = 64,
-      level_quarters = 8, prefetch_distance = 1;
+      level_quarters = 8, prefetch_distance = 1, tail_quarters = 4;
 };
 static std::mutex g_tuning_mu;
 static BatchTuning g_tuning;
@@ -1061,7 +1119,8 @@ struct BatchPlanImpl {
   // workspace layout
   size_t off_ctrl = 0, off_inst = 0, off_tiles = 0, off_items = 0, off_a = 0, off_b = 0,
          off_phi1 = 0, off_phi2 = 0, off_alpha = 0, off_rp = 0, off_cp = 0, off_tsum = 0,
-         off_tobj = 0, off_res = 0, off_obj = 0, off_conv = 0, off_stats = 0, off_act = 0, off_order = 0, off_xn = 0,
+         off_tobj = 0, off_res = 0, off_obj = 0, off_conv = 0, off_stats = 0, off_act = 0, off_order = 0,
+         off_ilvl = 0, off_xn = 0,
          off_yn = 0, total = 0;
   bool uploaded_any = false;
 };
@@ -1145,7 +1204,8 @@ int drot_batch_set_tuning(const drot_batch_tuning* t) {
     const BatchTuning d;
     if (t->fine_cols > 4096 || t->finest_cols > 4096 || t->item_lines > (1 << 24) ||
         t->finest_item_lines > (1 << 24) || t->level_quarters > 4096 ||
-        t->prefetch_distance > 8 || t->fine_cols == 0 || t->item_lines == 0 ||
+        t->prefetch_distance > 8 || t->tail_quarters > 4096 || t->fine_cols == 0 ||
+        t->item_lines == 0 ||
         t->finest_item_lines == 0)
       return DROT_ERR_INVALID_ARG;
     v.fine_cols = t->fine_cols > 0 ? t->fine_cols : d.fine_cols;
@@ -1154,6 +1214,7 @@ int drot_batch_set_tuning(const drot_batch_tuning* t) {
     v.finest_item_lines = t->finest_item_lines > 0 ? t->finest_item_lines : d.finest_item_lines;
     v.level_quarters = t->level_quarters >= 0 ? t->level_quarters : d.level_quarters;
     v.prefetch_distance = t->prefetch_distance >= 0 ? t->prefetch_distance : d.prefetch_distance;
+    v.tail_quarters = t->tail_quarters >= 0 ? t->tail_quarters : d.tail_quarters;
   }
   std::lock_guard<std::mutex> lk(g_tuning_mu);
   g_tuning = v;
@@ -1378,6 +1439,7 @@ static int batch_plan_create_impl(int n_inst, const drot_batch_instance* desc, i
   P.off_stats = off; off = al(off + sizeof(BatchStat) * n_inst);
   P.off_act = off;   off = al(off + sizeof(int) * (P.tiles.size() + P.items.size()));
   P.off_order = off; off = al(off + sizeof(int) * n_inst);
+  P.off_ilvl = off;  off = al(off + sizeof(int) * n_inst);
   P.off_xn = off;    off = al(off + sizeof(float) * rows);
   P.off_yn = off;    off = al(off + sizeof(float) * cols);
   P.total = off;
@@ -1465,6 +1527,7 @@ static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, 
   B.n_items_x = P.n_items_x;
   // active tiles of a level below which the solve moves to the next finer one
   B.fine_threshold = (int)((long long)P.grid * P.tune.level_quarters / 4);
+  B.tail_tiles = (int)((long long)P.grid * P.tune.tail_quarters / 4);
   B.items = (const BatchItem*)(ws + P.off_items);
   B.n_items = P.n_items;
   B.res_slot = (float2*)(ws + P.off_res);
@@ -1483,6 +1546,7 @@ static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, 
   B.stats = (BatchStat*)(ws + P.off_stats);
   B.act = (int*)(ws + P.off_act);
   B.order = (const int*)(ws + P.off_order);
+  B.ilvl = (int*)(ws + P.off_ilvl);
   B.counters = (unsigned*)(ws + P.off_ctrl);
   B.bar = (unsigned*)(ws + P.off_ctrl + 64);
   B.abort_flag = (int*)(ws + P.off_ctrl + 128);

@@ -59,42 +59,8 @@ struct CostParams {
   CostInst inst[kCostMaxInst];
 };
 
-__device__ __forceinline__ uint32_t to_tf32(float v) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
-  return r;
-}
-
-// Shared-memory matrix descriptor (tcgen05): start address, leading byte
-// offset (between core matrices along K), stride byte offset (between 8-row
-// groups), descriptor version 1, no swizzle.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;
-  return d;
-}
-
-// Instruction descriptor of kind::tf32: D F32, A and B TF32, both K-major,
-// N >> 3 at bit 17, M >> 4 at bit 24.
-constexpr uint32_t kCostIdesc = (1u << 4) | (2u << 7) | (2u << 10) |
-                                ((uint32_t)(kCostN >> 3) << 17) | ((uint32_t)(kCostM >> 4) << 24);
-
-__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
-                                         uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
-      :: "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(kCostIdesc), "r"(accumulate) : "memory");
-}
-
-// Byte offset of element (r, k) of a K-major tile with kc = d / 4 core
-// matrices per 8-row group.
-__device__ __forceinline__ uint32_t kmaj_off(int r, int k, int kc) {
-  return (uint32_t)((((r >> 3) * kc + (k >> 2)) << 7) + ((r & 7) << 4) + ((k & 3) << 2));
-}
+// Instruction descriptor of the tile's MMAs (M = 128 x points, N = 128 y points).
+constexpr uint32_t kCostIdesc = tf32_idesc(kCostM, kCostN);
 
 // Stage tile (i0, j0) of instance I into one operand buffer: x rows by
 // threads 0..127, y rows by threads 128..255 (one row each): hi / lo TF32
@@ -133,19 +99,10 @@ __device__ __forceinline__ void cost_stage(const CostParams& P, const CostInst& 
 // commit arriving on `bar` (one thread).
 __device__ __forceinline__ void cost_issue(unsigned char* buf, uint32_t op_bytes, int d,
                                            uint32_t tmem, uint64_t* bar) {
-  const uint32_t sbo = (uint32_t)(d >> 2) * 128u;
   const uint32_t ah = smem_u32(buf), al = ah + op_bytes;
   const uint32_t bh = al + op_bytes, bl = bh + op_bytes;
-  const int ks_n = d >> 3;  // K = 8 per kind::tf32 MMA = 2 core matrices
-  for (int ks = 0; ks < ks_n; ++ks)
-    mma_tf32(tmem, smem_desc(ah + ks * 256, 128, sbo), smem_desc(bh + ks * 256, 128, sbo),
-             ks > 0 ? 1u : 0u);
-  for (int ks = 0; ks < ks_n; ++ks)
-    mma_tf32(tmem, smem_desc(ah + ks * 256, 128, sbo), smem_desc(bl + ks * 256, 128, sbo), 1u);
-  for (int ks = 0; ks < ks_n; ++ks)
-    mma_tf32(tmem, smem_desc(al + ks * 256, 128, sbo), smem_desc(bh + ks * 256, 128, sbo), 1u);
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-               :: "r"(smem_u32(bar)) : "memory");
+  gram_tf32x3(ah, al, bh, bl, d, tmem, kCostIdesc);
+  tc_commit(bar);
 }
 
 // Instance and tile coordinates of global tile g (k advances monotonically).
@@ -594,17 +551,20 @@ int drot_sqeuclidean_cost(int n_inst, const drot_cost_instance* inst, const floa
   P.total_tiles = (int)total_tiles;
   const size_t smem = cost_smem_bytes(dim);
   if (cudaFuncSetAttribute((const void*)cost_sqeuclid_kernel,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+      cudaFuncSetAttribute((const void*)cost_sqeuclid_kernel,
+                           cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess)
     return DROT_ERR_CUDA;
-  // Persistent grid: the resident CTAs, at most two per SM (each holds 256
-  // of the SM's 512 TMEM columns, so a third would wait on its allocation).
-  int sms = 0, per_sm = 0;
-  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cost_sqeuclid_kernel, kCostThreads,
-                                                    smem) != cudaSuccess)
+  // Persistent grid of two CTAs per SM: each holds 256 of the SM's 512 TMEM
+  // columns, and the registers (under 128 per thread, 256 threads) and
+  // shared memory (under 100 KB at d <= 24) of two fit an SM.  CTAs that do
+  // not fit (d = 32) start when one finishes; the tile stride keeps every
+  // tile covered either way.
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return DROT_ERR_CUDA;
-  per_sm = std::max(1, std::min(per_sm, 2));
-  const int grid = (int)std::min<long long>(total_tiles, (long long)sms * per_sm);
+  const int grid = (int)std::min<long long>(total_tiles, 2LL * sms);
   if (cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) return DROT_ERR_CUDA;
   cost_sqeuclid_kernel<<<grid, kCostThreads, smem, st>>>(P);
   if (cudaGetLastError() != cudaSuccess) return DROT_ERR_CUDA;

@@ -329,6 +329,106 @@ __device__ __forceinline__ void fence_mbar_init() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+// ---- tcgen05 split-TF32 Gram products (5th-generation tensor cores) ------
+//
+// <x_i, y_j> for 128 x points (MMA M) against N y points with K = d:
+// x = x_hi + x_lo, x_hi = RN_tf32(x), x_lo = RN_tf32(x - x_hi) (the same for
+// y), accumulated in FP32 as x_hi.y_hi, then x_hi.y_lo, then x_lo.y_hi
+// (the split-precision scheme that gives FP32-level products on TF32 tensor
+// cores; the dropped x_lo.y_lo term is below 2^-22 relative).  Operands are
+// K-major tiles in shared memory without swizzle: 8-row x 16-byte core
+// matrices, kc = d / 4 of them per 8-row group.
+
+__device__ __forceinline__ uint32_t to_tf32(float v) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(v));
+  return r;
+}
+
+// Shared-memory matrix descriptor: start address, leading byte offset
+// (between core matrices along K), stride byte offset (between 8-row
+// groups), descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// Instruction descriptor of kind::tf32: D F32, A and B TF32, both K-major,
+// N >> 3 at bit 17, M >> 4 at bit 24.
+constexpr uint32_t tf32_idesc(int m, int n) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+      :: "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
+}
+
+// Byte offset of element (r, k) of a K-major tile with kc = d / 4 core
+// matrices per 8-row group.
+__device__ __forceinline__ uint32_t kmaj_off(int r, int k, int kc) {
+  return (uint32_t)((((r >> 3) * kc + (k >> 2)) << 7) + ((r & 7) << 4) + ((k & 3) << 2));
+}
+
+// Splits 4 consecutive k of one row into its tf32 hi / lo parts in the
+// K-major tiles hi_t / lo_t.
+__device__ __forceinline__ void stage_split4(unsigned char* hi_t, unsigned char* lo_t, int r,
+                                             int k, int kc, float4 v) {
+  const float e[4] = {v.x, v.y, v.z, v.w};
+  uint32_t hi[4], lo[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    hi[q] = to_tf32(e[q]);
+    lo[q] = to_tf32(e[q] - __uint_as_float(hi[q]));
+  }
+  const uint32_t off = kmaj_off(r, k, kc);
+  *reinterpret_cast<uint4*>(hi_t + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+  *reinterpret_cast<uint4*>(lo_t + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+}
+
+// The 3 x d / 8 MMAs of one split-TF32 Gram tile into the accumulator at
+// tmem (shared-memory addresses of the four operand tiles; one thread).
+__device__ __forceinline__ void gram_tf32x3(uint32_t ah, uint32_t al, uint32_t bh, uint32_t bl,
+                                            int d, uint32_t tmem, uint32_t idesc) {
+  const uint32_t sbo = (uint32_t)(d >> 2) * 128u;
+  const int ks_n = d >> 3;  // K = 8 per kind::tf32 MMA = 2 core matrices
+  for (int ks = 0; ks < ks_n; ++ks)
+    mma_tf32(tmem, smem_desc(ah + ks * 256, 128, sbo), smem_desc(bh + ks * 256, 128, sbo), idesc,
+             ks > 0 ? 1u : 0u);
+  for (int ks = 0; ks < ks_n; ++ks)
+    mma_tf32(tmem, smem_desc(ah + ks * 256, 128, sbo), smem_desc(bl + ks * 256, 128, sbo), idesc,
+             1u);
+  for (int ks = 0; ks < ks_n; ++ks)
+    mma_tf32(tmem, smem_desc(al + ks * 256, 128, sbo), smem_desc(bh + ks * 256, 128, sbo), idesc,
+             1u);
+}
+
+// Arrive on `bar` once every MMA this thread issued has completed.
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+               :: "r"(smem_u32(bar)) : "memory");
+}
+
+// 16 consecutive TMEM columns of the warp's lane quadrant (thread = lane).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr) : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
 // Packed FP32 pairs: the sm_100-family add/mul/fma .f32x2 instructions work
 // on two floats in a 64-bit register pair, each lane rounded exactly as the
 // scalar instruction (round to nearest, no contraction), at half the issue

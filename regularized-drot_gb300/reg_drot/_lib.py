@@ -101,7 +101,7 @@ class DrotGlBatchInstance(ctypes.Structure):
 class DrotBatchTuning(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in ("fine_cols", "finest_cols", "item_lines",
                                            "finest_item_lines", "level_quarters",
-                                           "prefetch_distance")]
+                                           "prefetch_distance", "tail_quarters")]
 
 
 _BRP = ctypes.POINTER(DrotBatchResult)

@@ -37,7 +37,7 @@ _ALIGN = 32  # elements between instance blocks (128 bytes of FP32)
 
 
 _TUNING_FIELDS = ("fine_cols", "finest_cols", "item_lines", "finest_item_lines",
-                  "level_quarters", "prefetch_distance")
+                  "level_quarters", "prefetch_distance", "tail_quarters")
 _tuning_lock = threading.Lock()
 _tuning = {}
 
@@ -52,7 +52,9 @@ def set_tuning(**fields):
     drot_batch_set_tuning).  Fields left out or below 0 keep the default:
     fine_cols 128, finest_cols 32 (0: no third level), item_lines 1024,
     finest_item_lines 64, level_quarters 8 (0: keep the coarse tiles),
-    prefetch_distance 1 (0: off).  ``set_tuning()`` restores the defaults.
+    prefetch_distance 1 (0: off), tail_quarters 4 (the smallest instances on
+    finer tiles at the end of each iteration; 0: off).  ``set_tuning()``
+    restores the defaults.
     Plans already built keep theirs; a batch built with ``tuning=`` uses its
     own."""
     bad = set(fields) - set(_TUNING_FIELDS)

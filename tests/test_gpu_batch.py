@@ -210,15 +210,20 @@ def test_batch_with_more_tiles_than_ctas(cuda, solver_lib):
 
 
 @pytest.mark.parametrize("tuning", [{"finest_cols": 0},
-                                    {"finest_cols": 0, "level_quarters": 0},
+                                    {"finest_cols": 0, "level_quarters": 0, "tail_quarters": 0},
                                     {"prefetch_distance": 0, "item_lines": 256},
-                                    {"fine_cols": 64, "finest_cols": 16, "level_quarters": 64}])
+                                    {"fine_cols": 64, "finest_cols": 16, "level_quarters": 64},
+                                    {"tail_quarters": 0},
+                                    {"tail_quarters": 4096, "level_quarters": 0}])
 def test_batch_tile_levels_match_oracle(cuda, solver_lib, tuning):
     # The default plan moves to 128-column and then 32-column tiles (with
-    # 64-line dual items) as instances converge; these plans stop at the
+    # 64-line dual items) as instances converge, and puts the smallest
+    # instances on the finer levels from the start; these plans stop at the
     # fine level, keep the coarse tiles throughout, use short dual items
-    # without the prefetch, or move early to narrower levels.  Every
-    # schedule must give the oracle's solution.
+    # without the prefetch, move early to narrower levels, keep every
+    # instance on the base level, or put every instance on the finest level
+    # while the base level stays coarse.  Every schedule must give the
+    # oracle's solution.
     B, insts, c, p, q = _batch(SHAPES, cuda, marg="dirichlet", cpt=256, tuning=tuning)
     x, info = B.solve(c, p, q, 20000)
     xs = B.unpack(x)
