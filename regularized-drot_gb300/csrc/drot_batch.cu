@@ -755,6 +755,11 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
     const int qa = items0;  // active dual-update items: P.act[qa + 0 .. nq)
 
     // ---------------------------------------------------------- fused update
+    // A CTA takes its next list slot only when it is free: taking it earlier
+    // (as a tile starts, to hide the atomic) reserves tiles that idle CTAs
+    // could run at the end of the iteration (measured: barrier wait 8 -> 13
+    // us, solve +1.5 %).  The lists hold unconverged instances only (rebuilt
+    // after every stop test that converged one).
     for (;;) {
       __syncthreads();
       if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
@@ -762,7 +767,6 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       if (s_tile >= n_list) break;
       const int t = __ldcg(P.act + s_tile);
       const BatchTile T = P.tiles[t];
-      if (__ldcg(P.conv + T.inst)) continue;
       const BatchInst I = P.inst[T.inst];
       const int lo = T.lo, hi = T.hi;
       if constexpr (GL) {
