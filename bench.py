@@ -666,6 +666,52 @@ def diff_gl_point(dev, shapes, xs, ys, w, eps, gl_inst=8, gl_iters=20000):
             "lambda_convention": "wrapper"}
 
 
+def diff_gl_batched(dev, shapes, xs, ys, w, eps, gl_inst, gl_iters=20000, steps=1):
+    """The group-lasso half of the differentiable workload through the
+    batched solver: the first gl_inst instances in one GLBatch (2 classes,
+    the C++ wrapper's threshold), each stopped at its relative 1e-4, packed
+    tensor-core cost, backward = the truncated unrolled adjoint of the last
+    GL_LAST_K iterations per instance (batch_group_lasso_drot_fn).  Forward
+    and backward timed apart (CUDA events)."""
+    import torch
+    from reg_drot.autograd import batch_group_lasso_drot_fn
+    from reg_drot.batch import GLBatch
+    from reg_drot.cost import packed_sqeuclidean_cost
+    sh = shapes[:gl_inst]
+    sl = instance_slices(sh)
+    B = GLBatch(sh, 2, RHO, ALPHA, eps[:gl_inst], device=dev, cols_per_tile=256,
+                convention="wrapper")
+    p, q = B.pack_marginals([torch.full((m,), 1.0 / m) for m, _ in sh],
+                            [torch.full((n,), 1.0 / n) for _, n in sh])
+    x = torch.from_numpy(xs[:sl[-1][0].stop]).to(dev).requires_grad_(True)
+    y = torch.from_numpy(ys[:sl[-1][1].stop]).to(dev).requires_grad_(True)
+    fwd, bwd = [], []
+    for rep in range(steps + 1):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        c = packed_sqeuclidean_cost(B, x, y, DIFF_SCALE)
+        X = batch_group_lasso_drot_fn(B, c, p, q, gl_iters, last_k=GL_LAST_K)
+        e[1].record()
+        ((c * X).sum() + w * (X * X).sum()).backward()
+        e[2].record()
+        e[2].synchronize()
+        if rep > 0:
+            fwd.append(e[0].elapsed_time(e[1]) / 1e3)
+            bwd.append(e[1].elapsed_time(e[2]) / 1e3)
+    info = X.grad_fn.info
+    its = sorted(r["n_iter"] for r in info)
+    # GL reads X and C and writes X on every iteration: 12 B per element
+    nbytes = sum(12.0 * m * n * r["n_iter"] for (m, n), r in zip(sh, info))
+    peak, _ = measured_peak()
+    return {"instances": gl_inst, "solves_with_grad_per_s": gl_inst / (min(fwd) + min(bwd)),
+            "forward_s": min(fwd), "backward_s": min(bwd),
+            "forward_algorithmic_GBps": nbytes / min(fwd) / 1e9,
+            "forward_frac_of_measured_hbm": nbytes / min(fwd) / 1e9 / peak,
+            "n_iter_min_median_max": [its[0], its[len(its) // 2], its[-1]],
+            "converged": int(sum(r["converged"] for r in info)), "last_k": GL_LAST_K,
+            "lambda_convention": "wrapper"}
+
+
 def max_over_ranks(values, dist, device):
     """Element-wise maximum of per-rank timings (the slowest replica sets the
     job's time); identity without a process group."""
@@ -758,7 +804,9 @@ def run_gpu(args):
     extra = {"qr_3000": qr_3000_point(dev, flush), "hbm_point": hbm,
              "gl_da": gl_da_point(dev), "gl_da_weight_5e-3": gl_da_point(dev, 5e-3),
              "configs": config_points(dev, flush), "batched_config4": batched_point(dev, flush),
-             "diff_gl": diff_gl_point(dev, shapes, xs, ys, w, eps)}
+             "diff_gl": {"batched_64": diff_gl_batched(dev, shapes, xs, ys, w, eps, 64),
+                         "batched_8": diff_gl_batched(dev, shapes, xs, ys, w, eps, 8),
+                         "one_at_a_time_8": diff_gl_point(dev, shapes, xs, ys, w, eps)}}
     cpu = cpu_sample(budget_s=15.0) if world == 1 else None
     cg = fn.cg_iters
     line = {
@@ -848,16 +896,21 @@ def run_diff_case(n_inst, iters):
 
 def run_batch_timeline(workload="config4"):
     """Timeline of one solve of a batched workload (config4: the 256-instance
-    batch; diff: the headline's 64 instances): CTA 0's device clock at four
-    points of every iteration (QRBatch.iteration_log), summarised per
-    iteration range as mean stage times (--case batchlog[:diff])."""
+    batch; diff: the headline's 64 instances; gl: their group-lasso solve):
+    CTA 0's device clock at four points of every iteration
+    (QRBatch.iteration_log), summarised per iteration range as mean stage
+    times (--case batchlog[:diff|:gl])."""
     import torch
     from reg_drot.batch import QRBatch
     dev = torch.device("cuda", 0)
-    if workload == "diff":
+    if workload in ("diff", "gl"):
+        from reg_drot.batch import GLBatch
         from reg_drot.cost import packed_sqeuclidean_cost
         shapes, xs, ys, _, eps = diff_workload()
-        B = QRBatch(shapes, RHO, ALPHA, eps, device=dev)
+        if workload == "gl":  # the GL half: 2 classes, the C++ wrapper's threshold
+            B = GLBatch(shapes, 2, RHO, ALPHA, eps, device=dev, convention="wrapper")
+        else:
+            B = QRBatch(shapes, RHO, ALPHA, eps, device=dev)
         with torch.no_grad():
             c = packed_sqeuclidean_cost(B, torch.from_numpy(xs).to(dev),
                                         torch.from_numpy(ys).to(dev), DIFF_SCALE)
@@ -925,6 +978,18 @@ def run_case(spec):
         return run_batch_timeline(parts[1] if len(parts) > 1 else "config4")
     if parts[0] == "diff":
         return run_diff_case(int(parts[1]), int(parts[2]))
+    if parts[0] == "glbatch":
+        import warnings
+        import torch
+        warnings.simplefilter("ignore")
+        dev = torch.device("cuda", 0)
+        shapes, xs, ys, w, eps = diff_workload()
+        n = int(parts[1])
+        out = {"case": spec, "batched": diff_gl_batched(dev, shapes, xs, ys, w, eps, n)}
+        if n <= 8:
+            out["one_at_a_time"] = diff_gl_point(dev, shapes, xs, ys, w, eps, gl_inst=n)
+        print(json.dumps(out), flush=True)
+        return 0
     n, iters = int(parts[0]), int(parts[1])
     dev = torch.device("cuda", 0)
     c, p, q, _ = make_problem(n)

@@ -416,6 +416,15 @@ int drot_qr_batch_launch_points(drot_batch_plan plan, const float *xpts,
                                 const float *p, const float *q, float *x,
                                 int max_iters, void *workspace,
                                 size_t workspace_bytes, drot_stream_t stream);
+/* Group-lasso plans only: n_iters more iterations of every instance from
+ * the state left in the workspace by an earlier launch (a, b, phi1, phi2,
+ * alpha of parity slot 0 -- see drot_batch_state_ex) and the plans in x,
+ * with the stop test off; afterwards alpha is again in slot 0.  The
+ * recomputation step of the batched unrolled adjoint.  Asynchronous. */
+int drot_batch_resume(drot_batch_plan plan, const void *c, int c_dtype,
+                      const float *p, const float *q, float *x, int n_iters,
+                      void *workspace, size_t workspace_bytes,
+                      drot_stream_t stream);
 /* Copies the per-instance outcomes to out[n_inst]; synchronises `stream`.
  * Returns DROT_ERR_BARRIER_TIMEOUT when the launch gave up on a barrier. */
 int drot_batch_results(drot_batch_plan plan, const void *workspace,
@@ -549,6 +558,36 @@ int drot_gl_adjoint_segment(const void *c, int c_dtype, const float *p,
                             size_t solve_ws_bytes, float *xbar, float *vbar,
                             float *cbar, float *pbar, float *qbar, void *adj_ws,
                             size_t adj_ws_bytes, drot_stream_t stream);
+
+/* Batched GL adjoint steps (the reverse step of drot_gl_adjoint_step for
+ * many instances in one set of launches).  Instance k: X (and Xbar, Cbar)
+ * n_rows x n_cols column-major with leading dimension ld at element
+ * x_offset of the packed X buffers, C at c_offset of the packed C, its
+ * rows at row_offset of the packed row vectors (phi1, dL/dp) and columns
+ * at col_offset of the packed column vectors (phi2, dL/dq); its vector
+ * adjoint [phi1bar | phi2bar | abar | bbar | alphabar] (2 (n_rows + n_cols)
+ * + 1 floats) follows the earlier instances' in vbar.  The C++ ABI of a
+ * batch is: plan_create (host), setup (uploads the parameter blocks with
+ * the C / adjoint buffers; synchronises `stream`), then one step per
+ * reverse iteration with that iteration's packed state (X, phi1, phi2). */
+typedef struct {
+  int n_rows, n_cols, ld, n_groups;
+  long long x_offset, c_offset, row_offset, col_offset;
+  float step_size, lambda;
+} drot_gl_adjoint_batch_instance;
+typedef struct drot_gl_adjoint_batch_plan_s *drot_gl_adjoint_batch_plan;
+int drot_gl_adjoint_batch_plan_create(int n_inst, const drot_gl_adjoint_batch_instance *inst,
+                                      drot_gl_adjoint_batch_plan *plan);
+void drot_gl_adjoint_batch_plan_destroy(drot_gl_adjoint_batch_plan plan);
+size_t drot_gl_adjoint_batch_workspace_bytes(drot_gl_adjoint_batch_plan plan);
+int drot_gl_adjoint_batch_setup(drot_gl_adjoint_batch_plan plan,
+                                const drot_gl_adjoint_batch_instance *inst, const void *c,
+                                int c_dtype, float *xbar, float *vbar, float *cbar,
+                                float *pbar, float *qbar, void *workspace,
+                                size_t workspace_bytes, drot_stream_t stream);
+int drot_gl_adjoint_batch_step(drot_gl_adjoint_batch_plan plan, const float *x,
+                               const float *phi1, const float *phi2, void *workspace,
+                               size_t workspace_bytes, drot_stream_t stream);
 
 /* ---------------------------------------------------------------------------
  * Cost matrices of point clouds (tensor cores)

@@ -108,6 +108,8 @@ struct BatchParams {
   int stall_cta;       // test hook of the bounded waits (grid_barrier); -1 off
   int band_cover;      // GL plans: rows of shared staging per band (>= every group's cover)
   int pf_dist;         // L2 prefetch distance of the fused update, in warp steps (0 off)
+  int resume;          // start from the state in the workspace and X (no warm start)
+  int no_stop;         // run max_iters iterations on every instance (stop test off)
   // Optional profile of CTA 0 for iterations it < iter_log_cap: globaltimer
   // at the start of the iteration, after its fused-update tiles, after the
   // first barrier and after its dual-update items (iter_log[4 it + 0..3]),
@@ -127,10 +129,18 @@ __global__ void batch_init_kernel(const BatchParams P) {
   if (k >= P.n_inst) return;
   const BatchInst I = P.inst[k];
   const long long nx = I.ld * I.nc;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nx;
-       t += (long long)gridDim.x * blockDim.x)
-    P.x[I.x_off + t] = 0.0f;
-  if (blockIdx.x == 0) {
+  if (!P.resume)
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nx;
+         t += (long long)gridDim.x * blockDim.x)
+      P.x[I.x_off + t] = 0.0f;
+  if (blockIdx.x == 0 && P.resume) {
+    if (threadIdx.x == 0) {
+      if (k == 0) P.counters[3] = (unsigned)P.n_tiles;
+      P.conv[k] = 0;
+      BatchStat st = {0, 0, 0, 0, 0.0, -1.0};
+      P.stats[k] = st;
+    }
+  } else if (blockIdx.x == 0) {
     for (int i = threadIdx.x; i < I.nr; i += blockDim.x) {
       P.a[I.row_off + i] = I.w_a;
       P.phi1[I.row_off + i] = I.w_phi1;
@@ -395,9 +405,10 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
 // phi2 - sC, 0) (kernel_glr.hpp:163-305), stored back, and the float sum of
 // y^2 -- the group norm, a float sum as the reference's atomics make it.
 // The shrink factor max(1 - lambda / (||y|| + 1e-9), 0) follows
-// (kernel_glr.hpp:307-326).  Pass B re-reads the column's y and C -- just
+// (kernel_glr.hpp:307-326).  Pass B re-reads the column's y -- just
 // touched, so from L2 -- stores X = y * scale and adds the column, row
-// (per-warp shared row partials wred[row - base]), mass and objective sums.
+// (per-warp shared row partials wred[row - base]) and mass sums; the
+// column's objective term <C, X> = scale <C, y> comes from pass A.
 // DRAM traffic stays 12 bytes per element, as in the single-pass update.
 // Stores the vector of rows r..r+3 that lie inside [lo, hi); a vector that
 // straddles a group boundary is stored element by element (the rows of the
@@ -427,7 +438,7 @@ __device__ __forceinline__ void batch_gl_tile_columns(const BatchParams& P, cons
     const float f2 = __ldcg(P.phi2 + I.col_off + j);
     float* xcol = P.x + I.x_off + (long long)j * I.ld;
     const CT* ccol = cbase + I.c_off + (long long)j * I.ld;
-    float nsl = 0.0f;
+    float nsl = 0.0f, cy = 0.0f;  // the column's |y|^2 and <C, y> (lane parts)
     for (int sb = 0; sb < nsub; ++sb) {
       float xv[4][VEC], cv[4][VEC];
 #pragma unroll
@@ -453,22 +464,23 @@ __device__ __forceinline__ void batch_gl_tile_columns(const BatchParams& P, cons
           const float y = ok ? fmaxf(t, 0.0f) : 0.0f;
           xv[v][e] = y;
           nsl = fmaf(y, y, nsl);
+          cy = fmaf(y, ok ? cv[v][e] : 0.0f, cy);
         }
         gl_store(xcol, r, lo, hi, xv[v]);
       }
     }
     nsl = warp_sum(nsl);
     const float scale = gl_shrink(nsl, I.lambda);
-    float colp = 0.0f, objp = 0.0f;
+    // Pass B re-reads only y: the objective's <C, X> of the column is
+    // scale <C, y>, summed in pass A.
+    float colp = 0.0f;
+    const float objp = scale * cy;
     for (int sb = 0; sb < nsub; ++sb) {
-      float xv[4][VEC], cv[4][VEC];
+      float xv[4][VEC];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         const int r = base + sb * 512 + v * 128 + lane * VEC;
-        if (r < hi) {
-          load_vec<VEC>(xcol + r, xv[v]);
-          load_c<VEC, CT>(ccol + r, cv[v]);
-        }
+        if (r < hi) load_vec<VEC>(xcol + r, xv[v]);
       }
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
@@ -485,7 +497,6 @@ __device__ __forceinline__ void batch_gl_tile_columns(const BatchParams& P, cons
             xv[v][e] = xn;
             ap[e] += xn;
             colp += xn;
-            objp = fmaf(xn, cv[v][e], objp);
           }
         }
         *reinterpret_cast<float4*>(wred + li) = acc;
@@ -988,7 +999,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
           st.objective = __ldcg(P.obj_slot + k);
           st.objective_valid = 1;
           st.residual = fp_value(r2);
-          if (st.residual < I.res2_stop) {
+          if (!P.no_stop && st.residual < I.res2_stop) {
             // Converged at iteration it: the instance keeps its folded X
             // until the unfold pass at the end of the launch.
             st.converged = 1;
@@ -1603,6 +1614,40 @@ int drot_qr_batch_launch(drot_batch_plan plan, const void* c, int c_dtype, const
                              : (const void*)batch_solve_kernel<__nv_bfloat16, 0>);
   return batch_launch(plan->p, fn, B, workspace, workspace_bytes, max_iters,
                       (cudaStream_t)stream);
+}
+
+int drot_batch_resume(drot_batch_plan plan, const void* c, int c_dtype, const float* p,
+                      const float* q, float* x, int n_iters, void* workspace,
+                      size_t workspace_bytes, drot_stream_t stream) {
+  if (!plan || !c || !p || !q || !x || !workspace || n_iters < 0) return DROT_ERR_INVALID_ARG;
+  if (!plan->p.gl) return DROT_ERR_INVALID_ARG;  // QR keeps X folded between iterations
+  if (c_dtype != DROT_C_F32 && c_dtype != DROT_C_BF16) return DROT_ERR_INVALID_ARG;
+  if (((uintptr_t)x & 15u) || ((uintptr_t)c & (c_dtype == DROT_C_F32 ? 15u : 7u)))
+    return DROT_ERR_INVALID_ARG;
+  if (n_iters == 0) return DROT_OK;
+  const BatchPlanImpl& P = plan->p;
+  BatchParams B;
+  memset(&B, 0, sizeof(B));
+  B.c = c;
+  B.p = p;
+  B.q = q;
+  B.x = x;
+  B.resume = 1;
+  B.no_stop = 1;
+  const void* fn = c_dtype == DROT_C_F32 ? (const void*)batch_solve_kernel<float, 0, true>
+                                         : (const void*)batch_solve_kernel<__nv_bfloat16, 0, true>;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int rc = batch_launch(P, fn, B, workspace, workspace_bytes, n_iters, st);
+  if (rc != DROT_OK) return rc;
+  // alpha of the last iteration sits in parity slot n_iters & 1: bring it to
+  // slot 0, where the next launch reads it.
+  if (n_iters & 1) {
+    float* alpha = (float*)((char*)workspace + P.off_alpha);
+    if (cudaMemcpyAsync(alpha, alpha + P.n_inst, sizeof(float) * P.n_inst,
+                        cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+      return DROT_ERR_CUDA;
+  }
+  return DROT_OK;
 }
 
 int drot_qr_batch_launch_points(drot_batch_plan plan, const float* xpts, const float* ypts,

@@ -37,6 +37,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <new>
+#include <vector>
 
 #include "drot_gb300.h"
 #include "drot_kernels.cuh"
@@ -48,16 +50,29 @@ constexpr int kGlaRows = 1024;    // rows per CTA in gl_adj_elems
 constexpr int kGlaThreads = 256;
 constexpr double kGlaNormEps = 1e-9;
 
+// One instance's step.  X, Xbar, Cbar and C are column-major with leading
+// dimension ld (X at element e = j ld + i).  Single-instance steps pass it
+// in the kernel parameters with x / phi1 / phi2 pointing at the state;
+// batched steps read it from an array in device memory and add xo / ro /
+// co to the step's packed state buffers.
 struct GlaParams {
   const void* c;
   int c_bf16;
-  int nr, nc, G;
+  int nr, nc, G, ld;
+  int chunks, rblocks;  // gl_adj_elems grid of this instance
   float s, lambda;
   const float *x, *phi1, *phi2;
+  long long xo;   // batched: X's element offset in the packed state
+  int ro, co;     // batched: phi1 / phi2 offsets in the packed state
   float *xbar, *vbar, *cbar, *pbar, *qbar;
   // workspace
   float *rbar, *cbarv, *sbar, *sig, *coef, *rowpart, *colpart;
-  int bounds[kMaxGroups + 1];  // group row boundaries (travel in the parameters)
+  int bounds[kMaxGroups + 1];  // group row boundaries
+};
+
+// The state pointers of one step.
+struct GlaState {
+  const float *x, *phi1, *phi2;
 };
 
 __device__ __forceinline__ float load_cost(const GlaParams& A, long long e) {
@@ -69,9 +84,12 @@ __device__ __forceinline__ float load_cost(const GlaParams& A, long long e) {
 // Grid over the n_rows + n_cols lines; every CTA first forms gbar from all
 // of phi1bar', phi2bar' (8 loads in flight per thread, FP64 across the
 // block), then updates its own lines; CTA 0 writes sigbar and alphabar.
-__global__ void gl_adj_vec(const GlaParams A) {
+__device__ __forceinline__ void gl_adj_vec_body(const GlaParams& A) {
   __shared__ double red[kGlaThreads / 32 + 1];
   const int nr = A.nr, nc = A.nc;
+  // CTAs past this instance's lines (batched grids are sized for the
+  // largest instance) have nothing to do; CTA 0 always runs.
+  if (blockIdx.x > 0 && (long long)blockIdx.x * blockDim.x >= nr + nc) return;
   float* f1 = A.vbar;
   float* f2 = f1 + nr;
   float* ab = f2 + nc;
@@ -119,6 +137,11 @@ __global__ void gl_adj_vec(const GlaParams A) {
   }
 }
 
+__global__ void gl_adj_vec(const GlaParams A) { gl_adj_vec_body(A); }
+__global__ void gl_adj_vec_batch(const GlaParams* __restrict__ PA) {
+  gl_adj_vec_body(PA[blockIdx.y]);
+}
+
 // Group of row i: the last g with bounds[g] <= i (binary search; bounds
 // travel in the kernel parameters).
 __device__ __forceinline__ int group_of(const GlaParams& A, int i) {
@@ -132,7 +155,7 @@ __device__ __forceinline__ int group_of(const GlaParams& A, int i) {
 }
 
 // One warp per (group g, column j): n_gj, sig_gj and coef_gj.
-__global__ void gl_adj_groups(const GlaParams A) {
+__device__ __forceinline__ void gl_adj_groups_body(const GlaParams& A, const GlaState S) {
   const int lane = threadIdx.x & 31;
   const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
   const float sb = A.sbar[0];
@@ -140,7 +163,7 @@ __global__ void gl_adj_groups(const GlaParams A) {
        task < (long long)A.G * A.nc; task += warps) {
     const int g = (int)(task % A.G), j = (int)(task / A.G);
     const int i0 = A.bounds[g], i1 = A.bounds[g + 1];
-    const float f2 = A.phi2[j], cb = A.cbarv[j];
+    const float f2 = S.phi2[j], cb = A.cbarv[j];
     // Lane sums as float pairs (TwoSum), combined in FP64 across the warp
     // (FP64 arithmetic is slow on this part; a per-element FP64 FMA cost
     // more than the loads).
@@ -150,10 +173,10 @@ __global__ void gl_adj_groups(const GlaParams A) {
 #pragma unroll
       for (int u = 0; u < 4; ++u) {  // all loads of four rows first
         const int i = ib + 32 * u;
-        const long long e = (long long)j * A.nr + (i < i1 ? i : i0);
-        xv[u] = A.x[e];
+        const long long e = (long long)j * A.ld + (i < i1 ? i : i0);
+        xv[u] = S.x[e];
         cv[u] = load_cost(A, e);
-        f1[u] = A.phi1[i < i1 ? i : i0];
+        f1[u] = S.phi1[i < i1 ? i : i0];
         xb[u] = A.xbar[e];
         rb[u] = A.rbar[i < i1 ? i : i0];
       }
@@ -182,14 +205,23 @@ __global__ void gl_adj_groups(const GlaParams A) {
   }
 }
 
+__global__ void gl_adj_groups(const GlaParams A) {
+  gl_adj_groups_body(A, GlaState{A.x, A.phi1, A.phi2});
+}
+__global__ void gl_adj_groups_batch(const GlaParams* __restrict__ PA, const float* x,
+                                    const float* phi1, const float* phi2) {
+  const GlaParams& A = PA[blockIdx.y];
+  gl_adj_groups_body(A, GlaState{x + A.xo, phi1 + A.ro, phi2 + A.co});
+}
+
 // One CTA per (chunk of kGlaChunk columns, block of kGlaRows rows); thread
 // t owns rows r0 + t + 256 u (u < 4) of the CTA's row partial (registers)
 // and loads its four rows of a column before using any.  Column sums: one
 // FP32 partial per warp and column in shared memory, combined in warp order
 // at the end into the row block's column partial.
-__global__ void __launch_bounds__(kGlaThreads) gl_adj_elems(const GlaParams A) {
+__device__ __forceinline__ void gl_adj_elems_body(const GlaParams& A, const GlaState S,
+                                                  int chunk, int rb) {
   __shared__ float wcol[kGlaThreads / 32][kGlaChunk];
-  const int chunk = blockIdx.x, rb = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int j0 = chunk * kGlaChunk, j1 = min(j0 + kGlaChunk, A.nc);
   const int r0 = rb * kGlaRows, r1 = min(r0 + kGlaRows, A.nr);
@@ -202,19 +234,19 @@ __global__ void __launch_bounds__(kGlaThreads) gl_adj_elems(const GlaParams A) {
     const int i = r0 + threadIdx.x + u * kGlaThreads;
     const int ic = i < r1 ? i : r0;
     gi[u] = group_of(A, ic);
-    f1[u] = A.phi1[ic];
+    f1[u] = S.phi1[ic];
     rbv[u] = A.rbar[ic];
     racc[u] = 0.0f;
   }
   for (int j = j0; j < j1; ++j) {
-    const float f2 = A.phi2[j], cb = A.cbarv[j];
+    const float f2 = S.phi2[j], cb = A.cbarv[j];
     float xv[U], cv[U], xb[U], sg[U], cf[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int i = r0 + threadIdx.x + u * kGlaThreads;
-      const long long e = (long long)j * A.nr + (i < r1 ? i : r0);
+      const long long e = (long long)j * A.ld + (i < r1 ? i : r0);
       const long long gj = (long long)j * A.G + gi[u];
-      xv[u] = A.x[e];
+      xv[u] = S.x[e];
       cv[u] = load_cost(A, e);
       xb[u] = A.xbar[e];
       sg[u] = A.sig[gj];
@@ -225,7 +257,7 @@ __global__ void __launch_bounds__(kGlaThreads) gl_adj_elems(const GlaParams A) {
     for (int u = 0; u < U; ++u) {
       const int i = r0 + threadIdx.x + u * kGlaThreads;
       if (i >= r1) continue;
-      const long long e = (long long)j * A.nr + i;
+      const long long e = (long long)j * A.ld + i;
       const float t = fmaf(-A.s, cv[u], (xv[u] + f1[u]) + f2);
       const float xt = ((xb[u] + rbv[u]) + cb) + sb;
       const float ybar = fmaf(cf[u], fmaxf(t, 0.0f), sg[u] * xt);
@@ -251,11 +283,23 @@ __global__ void __launch_bounds__(kGlaThreads) gl_adj_elems(const GlaParams A) {
   }
 }
 
+__global__ void __launch_bounds__(kGlaThreads) gl_adj_elems(const GlaParams A) {
+  gl_adj_elems_body(A, GlaState{A.x, A.phi1, A.phi2}, blockIdx.x, blockIdx.y);
+}
+// Batched: blockIdx.z is the instance; CTAs past its chunks / row blocks
+// return at once (the grid is sized for the largest instance).
+__global__ void __launch_bounds__(kGlaThreads) gl_adj_elems_batch(
+    const GlaParams* __restrict__ PA, const float* x, const float* phi1, const float* phi2) {
+  const GlaParams& A = PA[blockIdx.z];
+  if ((int)blockIdx.x >= A.chunks || (int)blockIdx.y >= A.rblocks) return;
+  gl_adj_elems_body(A, GlaState{x + A.xo, phi1 + A.ro, phi2 + A.co}, blockIdx.x, blockIdx.y);
+}
+
 // phi1bar = sum over column chunks of the row partials, phi2bar = sum over
 // row blocks of the column partials (fixed order).
 // One warp per line: lanes take partials lane, lane + 32, ... (fixed order),
 // then a shuffle tree.
-__global__ void gl_adj_rows(const GlaParams A, int chunks, int rblocks) {
+__device__ __forceinline__ void gl_adj_rows_body(const GlaParams& A, int chunks, int rblocks) {
   const int n = A.nr + A.nc;
   const int lane = threadIdx.x & 31;
   const int warps = gridDim.x * (blockDim.x >> 5);
@@ -269,6 +313,14 @@ __global__ void gl_adj_rows(const GlaParams A, int chunks, int rblocks) {
     s = warp_sum_d(s);
     if (lane == 0) A.vbar[l] = (float)s;  // [phi1bar | phi2bar] of s_k
   }
+}
+
+__global__ void gl_adj_rows(const GlaParams A, int chunks, int rblocks) {
+  gl_adj_rows_body(A, chunks, rblocks);
+}
+__global__ void gl_adj_rows_batch(const GlaParams* __restrict__ PA) {
+  const GlaParams& A = PA[blockIdx.y];
+  gl_adj_rows_body(A, A.chunks, A.rblocks);
 }
 
 struct GlaLayout {
@@ -296,6 +348,18 @@ static GlaLayout gla_layout(int nr, int nc, int G) {
 }  // namespace drot
 
 using namespace drot;
+
+// Batched adjoint: the instances' parameter blocks live in the workspace
+// (uploaded once by drot_gl_adjoint_batch_setup), followed by every
+// instance's scratch (the single-instance layout, 256-byte aligned).
+struct drot_gl_adjoint_batch_plan_s {
+  int n_inst = 0;
+  std::vector<GlaParams> prm;  // host copies; pointers filled by setup
+  std::vector<size_t> ws_off;  // per instance: scratch offset in the workspace
+  size_t off_params = 0, total = 0;
+  int max_lines = 0, max_chunks = 0, max_rblocks = 0;
+  long long max_tasks = 0;
+};
 
 extern "C" {
 
@@ -326,6 +390,9 @@ int drot_gl_adjoint_step(const void* c, int c_dtype, int n_rows, int n_cols, int
   A.nr = n_rows;
   A.nc = n_cols;
   A.G = n_groups;
+  A.ld = n_rows;
+  A.chunks = L.chunks;
+  A.rblocks = L.rblocks;
   A.s = step_size;
   A.lambda = lambda;
   A.x = x;
@@ -349,6 +416,125 @@ int drot_gl_adjoint_step(const void* c, int c_dtype, int n_rows, int n_cols, int
   gl_adj_groups<<<gblocks, 256, 0, st>>>(A);
   gl_adj_elems<<<dim3(L.chunks, L.rblocks), kGlaThreads, 0, st>>>(A);
   gl_adj_rows<<<(n_rows + n_cols + 7) / 8, 256, 0, st>>>(A, L.chunks, L.rblocks);
+  return cudaGetLastError() == cudaSuccess ? DROT_OK : DROT_ERR_CUDA;
+}
+
+int drot_gl_adjoint_batch_plan_create(int n_inst, const drot_gl_adjoint_batch_instance* desc,
+                                      drot_gl_adjoint_batch_plan* out) {
+  if (!out || !desc || n_inst <= 0 || n_inst > 65535) return DROT_ERR_INVALID_ARG;
+  *out = nullptr;
+  auto al = [](size_t v) { return (v + 255) / 256 * 256; };
+  drot_gl_adjoint_batch_plan_s* P = new (std::nothrow) drot_gl_adjoint_batch_plan_s;
+  if (!P) return DROT_ERR_UNSUPPORTED;
+  P->n_inst = n_inst;
+  P->prm.resize(n_inst);
+  P->ws_off.resize(n_inst);
+  size_t off = al(sizeof(GlaParams) * (size_t)n_inst);
+  long long vo = 0;
+  for (int k = 0; k < n_inst; ++k) {
+    const drot_gl_adjoint_batch_instance& d = desc[k];
+    if (d.n_rows <= 0 || d.n_cols <= 0 || d.ld < d.n_rows || d.n_groups <= 0 ||
+        d.n_groups > kMaxGroups || d.n_groups > d.n_rows || d.x_offset < 0 || d.c_offset < 0 ||
+        d.row_offset < 0 || d.col_offset < 0 || !(d.step_size > 0.0f) || !(d.lambda >= 0.0f)) {
+      delete P;
+      return DROT_ERR_INVALID_ARG;
+    }
+    GlaParams& A = P->prm[k];
+    memset(&A, 0, sizeof(A));
+    if (drot_gl_group_bounds(d.n_rows, d.n_groups, A.bounds) != DROT_OK) {
+      delete P;
+      return DROT_ERR_INVALID_ARG;
+    }
+    const GlaLayout L = gla_layout(d.n_rows, d.n_cols, d.n_groups);
+    A.nr = d.n_rows;
+    A.nc = d.n_cols;
+    A.G = d.n_groups;
+    A.ld = d.ld;
+    A.chunks = L.chunks;
+    A.rblocks = L.rblocks;
+    A.s = d.step_size;
+    A.lambda = d.lambda;
+    A.xo = d.x_offset;
+    A.ro = (int)d.row_offset;
+    A.co = (int)d.col_offset;
+    // pointers are offsets until setup: C / Xbar / Cbar at c_offset / x_offset,
+    // p / q at the line offsets, vbar at the running offset vo
+    A.vbar = (float*)(uintptr_t)(vo * sizeof(float));
+    vo += 2LL * (d.n_rows + d.n_cols) + 1;
+    P->ws_off[k] = off;
+    off = al(off + L.total);
+    P->max_lines = std::max(P->max_lines, d.n_rows + d.n_cols);
+    P->max_chunks = std::max(P->max_chunks, L.chunks);
+    P->max_rblocks = std::max(P->max_rblocks, L.rblocks);
+    P->max_tasks = std::max(P->max_tasks, (long long)d.n_groups * d.n_cols);
+  }
+  P->off_params = 0;
+  P->total = off;
+  *out = P;
+  return DROT_OK;
+}
+
+void drot_gl_adjoint_batch_plan_destroy(drot_gl_adjoint_batch_plan plan) { delete plan; }
+
+size_t drot_gl_adjoint_batch_workspace_bytes(drot_gl_adjoint_batch_plan plan) {
+  return plan ? plan->total : 0;
+}
+
+int drot_gl_adjoint_batch_setup(drot_gl_adjoint_batch_plan plan,
+                                const drot_gl_adjoint_batch_instance* desc, const void* c,
+                                int c_dtype, float* xbar, float* vbar, float* cbar, float* pbar,
+                                float* qbar, void* workspace, size_t workspace_bytes,
+                                drot_stream_t stream) {
+  if (!plan || !desc || !c || !xbar || !vbar || !cbar || !pbar || !qbar || !workspace)
+    return DROT_ERR_INVALID_ARG;
+  if (c_dtype != DROT_C_F32 && c_dtype != DROT_C_BF16) return DROT_ERR_INVALID_ARG;
+  if (workspace_bytes < plan->total || ((uintptr_t)workspace & 255u)) return DROT_ERR_WORKSPACE;
+  char* ws = (char*)workspace;
+  const size_t esz = c_dtype == DROT_C_F32 ? sizeof(float) : 2;
+  std::vector<GlaParams> dev(plan->prm);
+  for (int k = 0; k < plan->n_inst; ++k) {
+    GlaParams& A = dev[k];
+    const drot_gl_adjoint_batch_instance& d = desc[k];
+    const GlaLayout L = gla_layout(A.nr, A.nc, A.G);
+    char* w = ws + plan->ws_off[k];
+    A.c = (const char*)c + (size_t)d.c_offset * esz;
+    A.c_bf16 = c_dtype == DROT_C_BF16;
+    A.xbar = xbar + d.x_offset;
+    A.cbar = cbar + d.c_offset;
+    A.vbar = vbar + (uintptr_t)plan->prm[k].vbar / sizeof(float);
+    A.pbar = pbar + d.row_offset;
+    A.qbar = qbar + d.col_offset;
+    A.rbar = (float*)(w + L.off_rbar);
+    A.cbarv = (float*)(w + L.off_cbar);
+    A.sbar = (float*)(w + L.off_sbar);
+    A.sig = (float*)(w + L.off_sig);
+    A.coef = (float*)(w + L.off_coef);
+    A.rowpart = (float*)(w + L.off_rowpart);
+    A.colpart = (float*)(w + L.off_colpart);
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(ws + plan->off_params, dev.data(), sizeof(GlaParams) * dev.size(),
+                      cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return DROT_ERR_CUDA;
+  return DROT_OK;
+}
+
+int drot_gl_adjoint_batch_step(drot_gl_adjoint_batch_plan plan, const float* x, const float* phi1,
+                               const float* phi2, void* workspace, size_t workspace_bytes,
+                               drot_stream_t stream) {
+  if (!plan || !x || !phi1 || !phi2 || !workspace) return DROT_ERR_INVALID_ARG;
+  if (workspace_bytes < plan->total || ((uintptr_t)workspace & 255u)) return DROT_ERR_WORKSPACE;
+  const GlaParams* PA = (const GlaParams*)((char*)workspace + plan->off_params);
+  cudaStream_t st = (cudaStream_t)stream;
+  const int n = plan->n_inst;
+  gl_adj_vec_batch<<<dim3((plan->max_lines + kGlaThreads - 1) / kGlaThreads, n), kGlaThreads, 0,
+                     st>>>(PA);
+  const int gblocks = (int)std::min<long long>((plan->max_tasks + 7) / 8, 4096);
+  gl_adj_groups_batch<<<dim3(gblocks, n), 256, 0, st>>>(PA, x, phi1, phi2);
+  gl_adj_elems_batch<<<dim3(plan->max_chunks, plan->max_rblocks, n), kGlaThreads, 0, st>>>(
+      PA, x, phi1, phi2);
+  gl_adj_rows_batch<<<dim3((plan->max_lines + 7) / 8, n), 256, 0, st>>>(PA);
   return cudaGetLastError() == cudaSuccess ? DROT_OK : DROT_ERR_CUDA;
 }
 

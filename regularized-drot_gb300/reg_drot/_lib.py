@@ -98,6 +98,16 @@ class DrotGlBatchInstance(ctypes.Structure):
     ]
 
 
+class DrotGlAdjointBatchInstance(ctypes.Structure):
+    _fields_ = [
+        ("n_rows", ctypes.c_int), ("n_cols", ctypes.c_int), ("ld", ctypes.c_int),
+        ("n_groups", ctypes.c_int),
+        ("x_offset", ctypes.c_longlong), ("c_offset", ctypes.c_longlong),
+        ("row_offset", ctypes.c_longlong), ("col_offset", ctypes.c_longlong),
+        ("step_size", ctypes.c_float), ("lambda_", ctypes.c_float),
+    ]
+
+
 class DrotBatchTuning(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in ("fine_cols", "finest_cols", "item_lines",
                                            "finest_item_lines", "level_quarters",
@@ -163,6 +173,15 @@ SIGNATURES = {
     "drot_qr_batch_launch_points": (_c_int, [_vp, _vp, _vp, _c_int, _c_float, _vp, _vp, _vp, _c_int,
                                              _vp, _c_size, _vp]),
     "drot_batch_set_tuning": (_c_int, [ctypes.POINTER(DrotBatchTuning)]),
+    "drot_batch_resume": (_c_int, [_vp, _vp, _c_int, _vp, _vp, _vp, _c_int, _vp, _c_size, _vp]),
+    "drot_gl_adjoint_batch_plan_create": (_c_int, [_c_int,
+                                                   ctypes.POINTER(DrotGlAdjointBatchInstance),
+                                                   ctypes.POINTER(_vp)]),
+    "drot_gl_adjoint_batch_plan_destroy": (None, [_vp]),
+    "drot_gl_adjoint_batch_workspace_bytes": (_c_size, [_vp]),
+    "drot_gl_adjoint_batch_setup": (_c_int, [_vp, ctypes.POINTER(DrotGlAdjointBatchInstance),
+                                             _vp, _c_int] + [_vp] * 6 + [_c_size, _vp]),
+    "drot_gl_adjoint_batch_step": (_c_int, [_vp, _vp, _vp, _vp, _vp, _c_size, _vp]),
     "drot_batch_plan_destroy": (None, [_vp]),
     "drot_batch_plan_workspace_bytes": (_c_size, [_vp]),
     "drot_batch_plan_tiles": (_c_int, [_vp]),

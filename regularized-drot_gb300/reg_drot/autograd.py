@@ -399,6 +399,54 @@ def _gl_unrolled_backward(c, p, q, G, s, lam, seg, checkpoints, T, t_lo, xbar):
     return cbar, pbar, qbar
 
 
+class _GlAdjointBatch:
+    """The batched GL adjoint of a GLBatch (drot_gl_adjoint_batch_*): one set
+    of launches per reverse iteration for every instance."""
+
+    def __init__(self, batch):
+        from ._lib import DrotGlAdjointBatchInstance
+        B = batch
+        self.n = B.n
+        self.desc = (DrotGlAdjointBatchInstance * B.n)()
+        steps = B.step_sizes()
+        prow = pcol = 0
+        self.vlen = 0
+        for k, (nr, nc) in enumerate(B.shapes):
+            d = self.desc[k]
+            d.n_rows, d.n_cols, d.ld, d.n_groups = nr, nc, B.lds[k], B.n_class[k]
+            d.x_offset = d.c_offset = B.offsets[k]
+            d.row_offset, d.col_offset = prow, pcol
+            d.step_size, d.lambda_ = steps[k], B.lambdas[k]
+            prow += nr
+            pcol += nc
+            self.vlen += 2 * (nr + nc) + 1
+        self.h = ctypes.c_void_p()
+        with torch.cuda.device(B.device):
+            check(lib().drot_gl_adjoint_batch_plan_create(B.n, self.desc, ctypes.byref(self.h)),
+                  "gl_adjoint_batch_plan_create")
+        self.nbytes = int(lib().drot_gl_adjoint_batch_workspace_bytes(self.h))
+        self.ws = torch.empty(self.nbytes + 256, dtype=torch.uint8, device=B.device)
+        self.ptr = self.ws.data_ptr() + (-self.ws.data_ptr()) % 256
+
+    def setup(self, c, xbar, vbar, cbar, pbar, qbar, stream):
+        check(lib().drot_gl_adjoint_batch_setup(
+            self.h, self.desc, c.data_ptr(), C_BF16 if c.dtype == torch.bfloat16 else C_F32,
+            xbar.data_ptr(), vbar.data_ptr(), cbar.data_ptr(), pbar.data_ptr(), qbar.data_ptr(),
+            self.ptr, self.nbytes, stream), "gl_adjoint_batch_setup")
+
+    def step(self, x, phi1, phi2, stream):
+        check(lib().drot_gl_adjoint_batch_step(self.h, x.data_ptr(), phi1.data_ptr(),
+                                               phi2.data_ptr(), self.ptr, self.nbytes, stream),
+              "gl_adjoint_batch_step")
+
+    def __del__(self):
+        try:
+            if self.h:
+                lib().drot_gl_adjoint_batch_plan_destroy(self.h)
+        except Exception:
+            pass
+
+
 class BatchGroupLassoDROTFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, c, p, q, batch, max_iters, last_k, segment):
@@ -408,43 +456,78 @@ class BatchGroupLassoDROTFn(torch.autograd.Function):
                           "adjoint is taken at the last iterate")
         ctx.save_for_backward(c, p, q)
         ctx.batch, ctx.last_k, ctx.seg = batch, int(last_k), int(segment)
-        ctx.state = batch.state(info)
-        ctx.x = x.detach().clone()
+        # the packed final state (alpha of each instance's own parity in slot 0)
+        v = batch.state_views()
+        par = torch.tensor([int(r["iters_run"]) & 1 for r in info], device=x.device)
+        ctx.snap = {"x": x.detach().clone(), "a": v["a"].clone(), "b": v["b"].clone(),
+                    "phi1": v["phi1"].clone(), "phi2": v["phi2"].clone(),
+                    "alpha": v["alpha"].gather(0, par.view(1, -1)).view(-1).clone()}
         ctx.info = info
+        ctx.state = batch.state(info)
         return x
 
     @staticmethod
     def backward(ctx, gx):
+        """Every instance's unrolled adjoint of last_k GL iterations taken
+        from its solution, batched: the iterations are recomputed for all
+        instances at once (drot_batch_resume, checkpoints every `segment`
+        iterations, the segment's states kept), then each reverse iteration
+        is one set of launches over all instances
+        (drot_gl_adjoint_batch_step)."""
         c, p, q = ctx.saved_tensors
         B = ctx.batch
-        G = gx.detach().float()
-        cbar = torch.zeros(c.shape, dtype=torch.float32, device=c.device)
-        pbars, qbars = [], []
-        prow = pcol = 0
-        for k, (nr, nc) in enumerate(B.shapes):
-            s, lam = B.step_sizes()[k], B.lambdas[k]
-            ck = B.view(c.detach(), k).contiguous()
-            pk, qk = p.detach()[prow:prow + nr], q.detach()[pcol:pcol + nc]
-            # the K steps taken from the solution: checkpoints every `seg`
-            # iterations of a run that starts at the final state
-            st = _GLState(ck, pk, qk, B.n_class[k], s, lam)
-            init = dict(ctx.state[k], x=B.view(ctx.x, k).contiguous())
-            st.restore(init)
-            checkpoints, T = [], 0
-            while T < ctx.last_k:
-                checkpoints.append((T // ctx.seg, st.snapshot()))
-                n = min(ctx.seg, ctx.last_k - T)
-                st.run(n, -1.0)
-                T += n
-            cb, pb, qb = _gl_unrolled_backward(ck, pk, qk, B.n_class[k], s, lam, ctx.seg,
-                                               checkpoints, T, 0,
-                                               B.view(G, k).contiguous())
-            B.view(cbar, k).copy_(cb)
-            pbars.append(pb)
-            qbars.append(qb)
-            prow += nr
-            pcol += nc
-        return cbar.to(c.dtype), torch.cat(pbars), torch.cat(qbars), None, None, None, None
+        dev = c.device
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        cd, pd, qd = c.detach(), p.detach(), q.detach()
+        xw = B.empty_x()
+        views = B.state_views()
+
+        def load(snap):
+            xw.copy_(snap["x"])
+            for k in ("a", "b", "phi1", "phi2"):
+                views[k].copy_(snap[k])
+            views["alpha"][0].copy_(snap["alpha"])
+
+        def save():
+            return {"x": xw.clone(), "a": views["a"].clone(), "b": views["b"].clone(),
+                    "phi1": views["phi1"].clone(), "phi2": views["phi2"].clone(),
+                    "alpha": views["alpha"][0].clone()}
+
+        # checkpoints at the start of every segment of the last_k iterations
+        K, seg = ctx.last_k, ctx.seg
+        load(ctx.snap)
+        checkpoints = []
+        T = 0
+        while T < K:
+            checkpoints.append((T, save()))
+            n = min(seg, K - T)
+            if T + n < K:
+                B.resume(cd, pd, qd, xw, n)
+            T += n
+        adj = getattr(B, "_gl_adjoint", None)
+        if adj is None:
+            adj = B._gl_adjoint = _GlAdjointBatch(B)
+        xbar = gx.detach().float().contiguous().clone()
+        vbar = torch.zeros(adj.vlen, device=dev)
+        cbar = torch.zeros(B.total, dtype=torch.float32, device=dev)
+        pbar = torch.zeros(B.total_rows, device=dev)
+        qbar = torch.zeros(B.total_cols, device=dev)
+        adj.setup(cd, xbar, vbar, cbar, pbar, qbar, stream)
+        sx = torch.empty(min(seg, K), B.total, device=dev)
+        s1 = torch.empty(min(seg, K), B.total_rows, device=dev)
+        s2 = torch.empty(min(seg, K), B.total_cols, device=dev)
+        for T0, snap in reversed(checkpoints):
+            n = min(seg, K - T0)
+            load(snap)
+            for i in range(n):
+                sx[i].copy_(xw)
+                s1[i].copy_(views["phi1"])
+                s2[i].copy_(views["phi2"])
+                if i + 1 < n:
+                    B.resume(cd, pd, qd, xw, 1)
+            for i in reversed(range(n)):
+                adj.step(sx[i], s1[i], s2[i], stream)
+        return cbar.to(c.dtype), pbar, qbar, None, None, None, None
 
 
 def batch_group_lasso_drot_fn(batch, c, p, q, max_iters, *, last_k=64, segment=32):

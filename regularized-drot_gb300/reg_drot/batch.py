@@ -427,6 +427,37 @@ class GLBatch(QRBatch):
             self._plans[cpt] = h
         return self._plans[cpt]
 
+    def state_views(self):
+        """Views (aliasing the workspace of the last launch) of the packed
+        state: a, phi1 (all rows), b, phi2 (all columns) and alpha [2, n]
+        by iteration parity (drot_batch_state_ex)."""
+        if self._ws_plan is None:
+            raise RuntimeError("no launch yet")
+        h, ptr, _ = self.workspace_for(self._ws_plan)
+        vp = [ctypes.c_void_p() for _ in range(5)]
+        check(lib().drot_batch_state_ex(h, ptr, *[ctypes.byref(v) for v in vp]), "batch_state_ex")
+        base = self._ws.data_ptr()
+
+        def view(pv, n):
+            o = pv.value - base
+            return self._ws[o:o + 4 * n].view(torch.float32)
+        return {"a": view(vp[0], self.total_rows), "b": view(vp[1], self.total_cols),
+                "phi1": view(vp[2], self.total_rows), "phi2": view(vp[3], self.total_cols),
+                "alpha": view(vp[4], 2 * self.n).view(2, self.n)}
+
+    def resume(self, c, p, q, x, n_iters, stream=None):
+        """Enqueue n_iters more iterations of every instance from the state in
+        the workspace (state_views(); alpha in parity slot 0) and the plans in
+        x, the stop test off (drot_batch_resume); alpha ends in slot 0."""
+        if self._ws_plan is None:
+            raise RuntimeError("no launch yet")
+        h, ptr, nbytes = self.workspace_for(self._ws_plan)
+        s = torch.cuda.current_stream(self.device) if stream is None else stream
+        check(lib().drot_batch_resume(h, c.data_ptr(),
+                                      C_BF16 if c.dtype == torch.bfloat16 else C_F32,
+                                      p.data_ptr(), q.data_ptr(), x.data_ptr(), int(n_iters),
+                                      ptr, nbytes, s.cuda_stream), "batch_resume")
+
     def launch_points(self, *args, **kwargs):
         raise RuntimeError("GLBatch solves cost matrices only")
 

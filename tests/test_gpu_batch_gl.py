@@ -187,3 +187,24 @@ def test_gl_batch_gradient_is_the_truncated_adjoint_at_the_solution(cuda, solver
         assert _rel(X.detach().numpy(), st["x"].numpy()) <= 5e-2
         prow += nr
         pcol += nc
+
+
+def test_gl_batch_gradient_does_not_depend_on_the_checkpoint_spacing(cuda, solver_lib):
+    """The recomputation from checkpoints is deterministic (the same batched
+    iterations from the same states), so any checkpoint spacing gives the
+    same gradient bit for bit."""
+    from reg_drot.autograd import batch_group_lasso_drot_fn
+    shapes = [(60, 40, 2), (300, 200, 3), (513, 300, 2)]
+    grads = []
+    for seg in (7, 16, 40):
+        B, insts, c, p, q = _batch(shapes, cuda, cpt=64)
+        cl = c.clone().requires_grad_(True)
+        pl = p.clone().requires_grad_(True)
+        ql = q.clone().requires_grad_(True)
+        x = batch_group_lasso_drot_fn(B, cl, pl, ql, 20000, last_k=40, segment=seg)
+        W = torch.linspace(-1.0, 1.0, x.numel(), device=cuda).view_as(x)
+        (x * W).sum().backward()
+        grads.append((cl.grad.clone(), pl.grad.clone(), ql.grad.clone()))
+    for g in grads[1:]:
+        for a, b in zip(grads[0], g):
+            assert torch.equal(a, b)
