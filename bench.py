@@ -978,6 +978,35 @@ def run_case(spec):
         return run_batch_timeline(parts[1] if len(parts) > 1 else "config4")
     if parts[0] == "diff":
         return run_diff_case(int(parts[1]), int(parts[2]))
+    if parts[0] == "diffpts":
+        # the first n_inst instances of the differentiable workload through the
+        # point-cloud launch (cost recomputed on the tensor cores), iters
+        # iterations, every instance active
+        import torch
+        from reg_drot.batch import QRBatch
+        dev = torch.device("cuda", 0)
+        shapes, xs, ys, _, eps = diff_workload()
+        n_inst, iters = int(parts[1]), int(parts[2])
+        shapes = shapes[:n_inst]
+        sl = instance_slices(shapes)
+        xd = torch.from_numpy(xs[:sl[-1][0].stop]).to(dev)
+        yd = torch.from_numpy(ys[:sl[-1][1].stop]).to(dev)
+        B = QRBatch(shapes, RHO, ALPHA, eps[:n_inst], device=dev, cols_per_tile=256)
+        p, q = B.pack_marginals([torch.full((m,), 1.0 / m) for m, _ in shapes],
+                                [torch.full((n,), 1.0 / n) for _, n in shapes])
+        x = B.empty_x()
+        B.launch_points(xd, yd, p, q, x, iters, scale=DIFF_SCALE)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        B.launch_points(xd, yd, p, q, x, iters, scale=DIFF_SCALE)
+        b.record()
+        b.synchronize()
+        t = a.elapsed_time(b) / 1e3
+        elems = sum(m * n for m, n in shapes)
+        print(json.dumps({"case": spec, "elements": elems, "solve_s": t,
+                          "us_per_iteration": 1e6 * t / max(1, iters),
+                          "achieved_GBps": 8.0 * elems * iters / t / 1e9}), flush=True)
+        return 0
     if parts[0] == "glbatch":
         import warnings
         import torch

@@ -333,8 +333,8 @@ typedef struct drot_batch_plan_s *drot_batch_plan;
  * 512 rows x cols_per_tile columns (<= 0: 128), plus the launch shape. */
 int drot_batch_plan_create(int n_inst, const drot_batch_instance *inst,
                            int cols_per_tile, drot_batch_plan *plan);
-/* The same with the tile height: band_rows 512 (cost-matrix launches) or
- * 128 (required by drot_qr_batch_launch_points). */
+/* The same with the tile height: band_rows 512 (the default; required by
+ * drot_qr_batch_launch_points) or 128. */
 int drot_batch_plan_create_ex(int n_inst, const drot_batch_instance *inst,
                               int cols_per_tile, int band_rows,
                               drot_batch_plan *plan);
@@ -408,9 +408,11 @@ int drot_qr_batch_launch(drot_batch_plan plan, const void *c, int c_dtype,
  * xpts[(R_k + i) * dim ...] and y_j = ypts[(S_k + j) * dim ...] (R_k, S_k:
  * the earlier instances' total rows / columns, i.e. the points of all
  * instances concatenated in order, row-major, 16-byte aligned); dim 8 or
- * 16; FP32 FMA arithmetic, k ascending.  8 bytes per element on every
- * iteration instead of 12 on those that read C.  The plan must be built
- * with band_rows = 128; c_offset of the descriptors is unused. */
+ * 16.  The values are those of drot_sqeuclidean_cost (the same split-TF32
+ * tcgen05 products, accumulated in TMEM, and the same epilogue), computed
+ * per tile on the tensor cores.  8 bytes of traffic per element on every
+ * iteration instead of 12 on those that read C.  The plan must have
+ * 512-row bands; c_offset of the descriptors is unused. */
 int drot_qr_batch_launch_points(drot_batch_plan plan, const float *xpts,
                                 const float *ypts, int dim, float cost_scale,
                                 const float *p, const float *q, float *x,

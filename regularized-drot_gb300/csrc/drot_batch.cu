@@ -166,14 +166,12 @@ __global__ void batch_init_kernel(const BatchParams P) {
 // the folded X - sC), else odd (reads X only).  FULL: the band is exactly
 // 128 * KVR rows (no row masks).  Element arithmetic as in the
 // single-instance kernel: t = (X + phi1) + phi2 (- sC), y = max(t, 0) / kappa.
-template <int KVR, bool EV, bool FULL, typename CT, int DIM>
+template <int KVR, bool EV, bool FULL, typename CT>
 __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const BatchInst& I,
                                                    const BatchTile& T, const float* f1s,
-                                                   const float* xs, const float* xns,
                                                    float (&acc)[4][4], float& ms_hi,
                                                    float& ms_lo, float& ob_hi, float& ob_lo,
                                                    int lane, int warp, int W) {
-  static_assert(DIM == 0 || KVR == 1, "point-cloud tiles are 128-row bands");
   constexpr int VEC = 4, SV = 128, NCOL = 4 / KVR;
   const CT* const cbase = reinterpret_cast<const CT*>(P.c);
   const int lo = T.lo, hi = T.hi, c1 = T.c1;
@@ -190,7 +188,7 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
         if (lane < 16) {
           const int cc = lane / (4 * KVR), r = lo + (lane % (4 * KVR)) * 32;
           if (jn + cc < c1 && r < hi) prefetch_l2(P.x + I.x_off + (long long)(jn + cc) * I.ld + r);
-        } else if constexpr (EV && DIM == 0) {
+        } else if constexpr (EV) {
           constexpr int EPL = 128 / (int)sizeof(CT);  // elements per line
           constexpr int LPC = (RPC + EPL - 1) / EPL;  // lines per column
           const int li = lane - 16, cc = li / LPC, r = lo + (li % LPC) * EPL;
@@ -208,7 +206,7 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
       const int r = lo + (v % KVR) * SV + lane * VEC;
       if ((NCOL == 1 || jc < c1) && (FULL || r < hi)) {
         load_vec<VEC>(P.x + I.x_off + (long long)jc * I.ld + r, xv[v]);
-        if constexpr (EV && DIM == 0)
+        if constexpr (EV)
           load_c_raw<VEC, CT>(cbase + I.c_off + (long long)jc * I.ld + r, cv[v]);
         else {
 #pragma unroll
@@ -222,50 +220,6 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
 #pragma unroll
     for (int cc = 0; cc < NCOL; ++cc)
       f2[cc] = (NCOL == 1 || j0 + cc < c1) ? __ldcg(P.phi2 + I.col_off + j0 + cc) : 0.0f;
-    if constexpr (EV && DIM > 0) {
-      // C of the step's 4 columns x the lane's 4 rows from the points: the
-      // band's x (k-major in shared memory) against y_j (broadcast loads),
-      // k ascending; cv = cscale * max(|x|^2 + |y|^2 - 2 <x, y>, 0).  Two
-      // columns at a time keeps the accumulators and y in registers without
-      // spilling.
-      const float4 xn4 = *reinterpret_cast<const float4*>(xns + lane * VEC);
-      const float xna[VEC] = {xn4.x, xn4.y, xn4.z, xn4.w};
-#pragma unroll
-      for (int v0 = 0; v0 < 4; v0 += 2) {
-        float dot[2][VEC];
-#pragma unroll
-        for (int v = 0; v < 2; ++v)
-#pragma unroll
-          for (int e = 0; e < VEC; ++e) dot[v][e] = 0.0f;
-#pragma unroll
-        for (int k0 = 0; k0 < DIM; k0 += 4) {
-          float4 yk[2];
-#pragma unroll
-          for (int v = 0; v < 2; ++v) {
-            const int jc = min(j0 + v0 + v, c1 - 1);
-            yk[v] = __ldg(reinterpret_cast<const float4*>(P.ypts + (long long)(I.col_off + jc) * DIM + k0));
-          }
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            const float4 xk = *reinterpret_cast<const float4*>(xs + (k0 + kk) * SV + lane * VEC);
-            const float xa[VEC] = {xk.x, xk.y, xk.z, xk.w};
-#pragma unroll
-            for (int v = 0; v < 2; ++v) {
-              const float yv = kk == 0 ? yk[v].x : (kk == 1 ? yk[v].y : (kk == 2 ? yk[v].z : yk[v].w));
-#pragma unroll
-              for (int e = 0; e < VEC; ++e) dot[v][e] = fmaf(xa[e], yv, dot[v][e]);
-            }
-          }
-        }
-#pragma unroll
-        for (int v = 0; v < 2; ++v) {
-          const float yn = __ldg(P.ynorm + I.col_off + min(j0 + v0 + v, c1 - 1));
-#pragma unroll
-          for (int e = 0; e < VEC; ++e)
-            cv[v0 + v][e] = P.cscale * fmaxf(fmaf(-2.0f, dot[v][e], xna[e] + yn), 0.0f);
-        }
-      }
-    }
     auto valid = [&](int v, int e) -> bool {
       if constexpr (FULL && NCOL == 1) return true;
       const bool colok = (NCOL == 1) || (j0 + v / KVR < c1);
@@ -572,16 +526,344 @@ __device__ __forceinline__ void reduce_lines(const float* base, int stride, int 
   }
 }
 
-// C_ij of a point-cloud launch, the same arithmetic as the fused update.
-template <int DIM>
-__device__ __forceinline__ float point_cost(const BatchParams& P, const BatchInst& I, int i, int j) {
-  const float* xr = P.xpts + (long long)(I.row_off + i) * DIM;
-  const float* yr = P.ypts + (long long)(I.col_off + j) * DIM;
-  float dot = 0.0f;
+// ---------------------------------------------------------------------------
+// Point-cloud launches: the cost recomputed on the tensor cores
+// ---------------------------------------------------------------------------
+//
+// On the iterations that read C (even QR iterations and the final unfold) a
+// point launch recomputes the tile's C_ij = cscale * max(|x_i|^2 + |y_j|^2 -
+// 2 <x_i, y_j>, 0) with the split-TF32 tcgen05 Gram product of the cost
+// kernel -- the same MMAs in the same order and the same epilogue, so the
+// values equal the stored cost's -- straight into TMEM, and the fused update
+// reads them from there: 8 bytes of DRAM traffic per element instead of 12.
+//
+// The tile is a 512-row band in four 128-row sub-bands; its columns go in
+// rounds of kPtCols = 16.  Per round one thread issues, for every sub-band,
+// the 3 x DIM/8 MMAs (M = 128 rows, N = 16 columns) into a 64-column TMEM
+// buffer (sub-band v at columns 16 v); the buffers alternate, so round n+1's
+// MMAs run while round n is updated.  Warp w reads TMEM lane quadrant
+// q = w % 4 -- rows 128 v + 32 q + lane -- for the round's columns
+// 8 (w / 4) .. + 7: each lane updates one row of each sub-band (its row
+// partials stay in registers) and the column sums are warp reductions,
+// combined over the quadrants in shared memory in a fixed order.
+constexpr int kPtCols = 64;    // columns per round (MMA N)
+constexpr int kPtTmemCols = 2 * 4 * kPtCols;  // two buffers x four sub-bands
+
+// Shared memory of the point path (after the common part of the kernel's).
+struct PointSmem {
+  unsigned char* xa;  // x band: 4 sub-bands x [hi | lo] x 128 rows x DIM (K-major)
+  unsigned char* yb;  // y of a round: 2 buffers x [hi | lo] x 16 rows x DIM
+  float* ycol;        // per round n % 3: |y_j|^2 [16], phi2_j [16] (a round's are
+                      // staged two rounds ahead, while the round before is read)
+  float* cpart;       // per buffer: column partials [4 quadrants][16]
+  float* xn;          // |x_i|^2 of the band's 512 rows
+};
+
+__host__ __device__ constexpr size_t point_smem_bytes(int dim) {
+  return 1024 /* alignment */ + (size_t)4 * 2 * 128 * dim * 4 + (size_t)2 * 2 * kPtCols * dim * 4 +
+         sizeof(float) * (3 * 2 * kPtCols + 2 * 4 * kPtCols + 512);
+}
+
+__device__ __forceinline__ PointSmem point_smem(void* base, int dim) {
+  unsigned char* p = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(base) + 1023) & ~static_cast<uintptr_t>(1023));
+  PointSmem S;
+  S.xa = p;
+  p += (size_t)4 * 2 * 128 * dim * 4;
+  S.yb = p;
+  p += (size_t)2 * 2 * kPtCols * dim * 4;
+  S.ycol = reinterpret_cast<float*>(p);
+  S.cpart = S.ycol + 3 * 2 * kPtCols;
+  S.xn = S.cpart + 2 * 4 * kPtCols;
+  return S;
+}
+
+// One tile of a point launch on an iteration that reads C.  UNFOLD: the
+// final unfold X = max(X + sC, 0) of a converged instance; otherwise the
+// even QR update (t = (X + phi1) + phi2 - sC, y = max(t, 0) / kappa, X =
+// y - sC stored folded), with the row partials left in red[w][row] (warps w
+// and w + 4 share a quadrant: rows of quadrant q in red[q] and red[q + 4]),
+// the column partials written to colpart and the mass / objective lane sums
+// in the float pairs.  mw: per buffer, the mbarrier phases waited so far.
+// False when an MMA did not complete within the time limit (every thread
+// returns the same).
+template <int DIM, bool UNFOLD>
+__device__ bool point_tile(const BatchParams& P, const BatchInst& I, const BatchTile& T,
+                           const float* f1s, const PointSmem& S, uint32_t tmem, uint64_t* mbar,
+                           unsigned (&mw)[2], float* red, float& ms_hi, float& ms_lo,
+                           float& ob_hi, float& ob_lo) {
+  constexpr int kc = DIM / 4;
+  constexpr uint32_t sub = 128u * DIM * 4;      // one hi or lo tile of a sub-band
+  constexpr uint32_t ysub = kPtCols * DIM * 4;  // one hi or lo tile of a round's y
+  constexpr uint32_t idesc = tf32_idesc(128, kPtCols);
+  constexpr int YT = 64;                        // threads staging a round's y (the last two warps)
+  constexpr int YV = (kPtCols * kc + YT - 1) / YT;  // float4 of y per staging thread
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int lo = T.lo, hi = T.hi, c0 = T.c0, c1 = T.c1;
+  // x of the band's rows, split, K-major per sub-band; their norms
+  for (int idx = tid; idx < 512 * kc; idx += nt) {
+    const int r = idx / kc, c4 = idx - r * kc;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (lo + r < hi)
+      v = __ldg(reinterpret_cast<const float4*>(P.xpts + (long long)(I.row_off + lo + r) * DIM) + c4);
+    unsigned char* h = S.xa + (r >> 7) * 2 * sub;
+    stage_split4(h, h + sub, r & 127, 4 * c4, kc, v);
+  }
+  for (int r = tid; r < 512; r += nt) S.xn[r] = lo + r < hi ? __ldg(P.xnorm + I.row_off + lo + r) : 0.0f;
+  const int rounds = (c1 - c0 + kPtCols - 1) / kPtCols;
+  // Round n's y: loaded into registers (y_load) by the staging threads,
+  // split into buffer n & 1 with norms and phi2 into slot n % 3 (y_store).
+  const int yt = tid - (nt - YT);  // staging thread index, < 0 for the others
+  float4 yreg[YV];
+  float ynr = 0.0f, yph = 0.0f;
+  auto y_load = [&](int n) {
+    if (yt < 0) return;
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) dot = fmaf(__ldg(xr + k), __ldg(yr + k), dot);
-  return P.cscale *
-         fmaxf(fmaf(-2.0f, dot, __ldg(P.xnorm + I.row_off + i) + __ldg(P.ynorm + I.col_off + j)), 0.0f);
+    for (int u = 0; u < YV; ++u) {
+      const int idx = yt + u * YT, jl = idx / kc, c4 = idx - jl * kc, j = c0 + n * kPtCols + jl;
+      yreg[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (idx < kPtCols * kc && j < c1)
+        yreg[u] = __ldg(reinterpret_cast<const float4*>(P.ypts + (long long)(I.col_off + j) * DIM) + c4);
+    }
+    if (yt < kPtCols) {
+      const int j = c0 + n * kPtCols + yt;
+      ynr = j < c1 ? __ldg(P.ynorm + I.col_off + j) : 0.0f;
+      yph = (!UNFOLD && j < c1) ? __ldcg(P.phi2 + I.col_off + j) : 0.0f;
+    }
+  };
+  auto y_store = [&](int n) {
+    if (yt < 0) return;
+    unsigned char* h = S.yb + (n & 1) * 2 * ysub;
+#pragma unroll
+    for (int u = 0; u < YV; ++u) {
+      const int idx = yt + u * YT, jl = idx / kc, c4 = idx - jl * kc;
+      if (idx < kPtCols * kc) stage_split4(h, h + ysub, jl, 4 * c4, kc, yreg[u]);
+    }
+    if (yt < kPtCols) {
+      float* yc = S.ycol + (n % 3) * 2 * kPtCols;
+      yc[yt] = ynr;
+      yc[kPtCols + yt] = yph;
+    }
+    fence_proxy_async_shared();
+  };
+  auto issue = [&](int n) {  // one thread: round n's MMAs, then the commit
+    const uint32_t yh = smem_u32(S.yb + (n & 1) * 2 * ysub);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const uint32_t xh = smem_u32(S.xa + v * 2 * sub);
+      gram_tf32x3(xh, xh + sub, yh, yh + ysub, DIM,
+                  tmem + (uint32_t)((n & 1) * 4 * kPtCols + v * kPtCols), idesc);
+    }
+    tc_commit(&mbar[n & 1]);
+  };
+  // lane quadrant and column group (16 of the round's 64 columns; 16 warps)
+  const int q = warp & 3, hcol = warp >> 2;
+  constexpr int WC = kPtCols / 4;  // columns of a warp per round
+  float f1[4], xnr[4], racc[4];
+  bool rowok[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    const int r = 128 * v + 32 * q + lane;
+    rowok[v] = lo + r < hi;
+    f1[v] = UNFOLD ? 0.0f : f1s[r];
+    racc[v] = 0.0f;
+  }
+  float* const xbase = P.x + I.x_off + lo + 32 * q + lane;
+  // L2 prefetch of the X lines of the warp's columns of round n (WC columns
+  // x 4 sub-bands of its quadrant: WC / 8 128-byte lines per lane)
+  auto prefetch_round = [&](int n) {
+#pragma unroll
+    for (int u = 0; u < WC / 8; ++u) {
+      const int line = lane + 32 * u, jn = c0 + n * kPtCols + WC * hcol + (line >> 2), vv = line & 3;
+      if (n < rounds && jn < c1 && rowok[vv]) prefetch_l2(xbase + (long long)jn * I.ld + 128 * vv);
+    }
+  };
+  y_load(0);
+  y_store(0);
+  if (rounds > 1) {
+    y_load(1);
+    y_store(1);
+  }
+  if (P.pf_dist > 0) {
+    prefetch_round(0);
+    prefetch_round(1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (tid == 0 && rounds > 0) issue(0);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) xnr[v] = S.xn[128 * v + 32 * q + lane];
+  const float s = I.s, kappa = I.kappa, krcp = I.kappa_rcp, cscale = P.cscale;
+  bool ok = true;
+  for (int n = 0; n < rounds; ++n) {
+    const int b = n & 1;
+    if (n + 2 < rounds) y_load(n + 2);  // in flight during the round
+    if (P.pf_dist > 0) prefetch_round(n + 2);
+    const bool got = mbar_wait(&mbar[b], mw[b] & 1u, P.timeout_ns);
+    ++mw[b];
+    // Round n-1's TMEM reads are done before this barrier, after which
+    // round n+1's MMAs may overwrite that buffer.
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    if (!__syncthreads_and(got ? 1 : 0)) {
+      // an MMA that did not complete: give it a second bounded chance to
+      // land (its TMEM and shared memory stay allocated until the end)
+      mbar_wait(&mbar[b], (mw[b] - 1u) & 1u, P.timeout_ns);
+      ok = false;
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (tid == 0 && n + 1 < rounds) issue(n + 1);
+    if (!UNFOLD && n > 0 && tid >= 32 && tid < 32 + kPtCols) {  // round n-1's column sums (warps 1, 2)
+      const int jl = tid - 32, j = c0 + (n - 1) * kPtCols + jl;
+      const float* cp = S.cpart + ((n - 1) & 1) * 4 * kPtCols;
+      if (j < c1)
+        P.colpart[I.cp_off + (long long)T.band * I.nc + j] =
+            ((cp[jl] + cp[kPtCols + jl]) + cp[2 * kPtCols + jl]) + cp[3 * kPtCols + jl];
+    }
+    // the warp's WC columns of the round, 4 at a time
+#pragma unroll 1
+    for (int hh = 0; hh < WC / 4; ++hh) {
+      const int jb = c0 + n * kPtCols + WC * hcol + 4 * hh;
+      const float* yc = S.ycol + (n % 3) * 2 * kPtCols + WC * hcol + 4 * hh;
+      float xv[4][4], cv[4][4];
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        const bool colok = jb + cc < c1;
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+          xv[v][cc] = (colok && rowok[v]) ? xbase[(long long)(jb + cc) * I.ld + 128 * v] : 0.0f;
+      }
+      {
+        uint32_t d[4][4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+          asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                       : "=r"(d[v][0]), "=r"(d[v][1]), "=r"(d[v][2]), "=r"(d[v][3])
+                       : "r"(tmem + ((uint32_t)(32 * q) << 16) +
+                             (uint32_t)(b * 4 * kPtCols + v * kPtCols + WC * hcol + 4 * hh))
+                       : "memory");
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+          const float yn = yc[cc];
+#pragma unroll
+          for (int v = 0; v < 4; ++v)
+            cv[v][cc] = cscale * fmaxf(fmaf(-2.0f, __uint_as_float(d[v][cc]), xnr[v] + yn), 0.0f);
+        }
+      }
+      if constexpr (UNFOLD) {
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+          if (jb + cc >= c1) continue;
+#pragma unroll
+          for (int v = 0; v < 4; ++v)
+            if (rowok[v])
+              xbase[(long long)(jb + cc) * I.ld + 128 * v] =
+                  fmaxf(fmaf(s, cv[v][cc], xv[v][cc]), 0.0f);
+        }
+        continue;
+      }
+      // t = (X + phi1) + phi2 - sC on packed column pairs
+      unsigned tmin = 0xffffffffu;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const f32x2 f1b = x2_pack(f1[v], f1[v]);
+#pragma unroll
+        for (int cc = 0; cc < 4; cc += 2) {
+          f32x2 tt = x2_add(x2_add(x2_pack(xv[v][cc], xv[v][cc + 1]), f1b),
+                            x2_pack(yc[kPtCols + cc], yc[kPtCols + cc + 1]));
+          tt = x2_fma(x2_pack(-s, -s), x2_pack(cv[v][cc], cv[v][cc + 1]), tt);
+          x2_unpack(tt, xv[v][cc], xv[v][cc + 1]);
+        }
+#pragma unroll
+        for (int cc = 0; cc < 4; ++cc) {
+          const unsigned key = (unsigned)__float_as_int(xv[v][cc]) - 1u;
+          tmin = min(tmin, (rowok[v] && jb + cc < c1) ? key : 0xffffffffu);
+        }
+      }
+      const bool slow = __any_sync(0xffffffffu, tmin < kDivTinyBitsM1);
+      float colp[4] = {0.0f, 0.0f, 0.0f, 0.0f}, objp = 0.0f;
+      if (!slow) {
+        const f32x2 nk = x2_pack(-kappa, -kappa), ky = x2_pack(krcp, krcp), ns2 = x2_pack(-s, -s);
+        f32x2 obj2 = x2_pack(0.0f, 0.0f);
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+#pragma unroll
+          for (int cc = 0; cc < 4; cc += 2) {
+            const bool ok0 = rowok[v] && jb + cc < c1, ok1 = rowok[v] && jb + cc + 1 < c1;
+            f32x2 y = x2_div_rn_by_fma(
+                x2_pack(fmaxf(xv[v][cc], 0.0f), fmaxf(xv[v][cc + 1], 0.0f)), nk, ky);
+            float y0, y1;
+            x2_unpack(y, y0, y1);
+            y0 = ok0 ? y0 : 0.0f;
+            y1 = ok1 ? y1 : 0.0f;
+            y = x2_pack(y0, y1);
+            const f32x2 c2 = x2_pack(ok0 ? cv[v][cc] : 0.0f, ok1 ? cv[v][cc + 1] : 0.0f);
+            x2_unpack(x2_fma(ns2, c2, y), xv[v][cc], xv[v][cc + 1]);
+            obj2 = x2_fma(y, c2, obj2);
+            racc[v] = (racc[v] + y0) + y1;
+            colp[cc] += y0;
+            colp[cc + 1] += y1;
+          }
+        float u0, u1;
+        x2_unpack(obj2, u0, u1);
+        objp = u0 + u1;
+      } else {
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) {
+            const bool okk = rowok[v] && jb + cc < c1;
+            float y = fmaxf(xv[v][cc], 0.0f) / kappa;
+            y = okk ? y : 0.0f;
+            const float c = okk ? cv[v][cc] : 0.0f;
+            xv[v][cc] = fmaf(-s, c, y);
+            objp = fmaf(y, c, objp);
+            racc[v] += y;
+            colp[cc] += y;
+          }
+      }
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        if (jb + cc >= c1) continue;
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+          if (rowok[v]) xbase[(long long)(jb + cc) * I.ld + 128 * v] = xv[v][cc];
+      }
+      float e1;
+      const float msum = ((colp[0] + colp[1]) + colp[2]) + colp[3];
+      two_sum(ms_hi, msum, ms_hi, e1);
+      ms_lo += e1;
+      two_sum(ob_hi, objp, ob_hi, e1);
+      ob_lo += e1;
+      float* cp = S.cpart + b * 4 * kPtCols + q * kPtCols + WC * hcol + 4 * hh;
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        const float cs = warp_sum(colp[cc]);
+        if (lane == 0) cp[cc] = cs;
+      }
+    }
+    if (n + 2 < rounds) y_store(n + 2);  // read by round n+2's MMAs, issued after the next barrier
+  }
+  // every warp past its last round (or the failed one): the last round's
+  // column sums, then the row partials
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (!UNFOLD && ok && rounds > 0 && tid < kPtCols) {
+    const int n = rounds - 1;
+    const int j = c0 + n * kPtCols + tid;
+    const float* cp = S.cpart + (n & 1) * 4 * kPtCols;
+    if (j < c1)
+      P.colpart[I.cp_off + (long long)T.band * I.nc + j] =
+          ((cp[tid] + cp[kPtCols + tid]) + cp[2 * kPtCols + tid]) + cp[3 * kPtCols + tid];
+  }
+  if (!UNFOLD) {  // the warp's rows of red hold its partials, the other rows zeros
+#pragma unroll
+    for (int r0 = 0; r0 < 512; r0 += 32)
+      red[(size_t)warp * 512 + r0 + lane] = ((r0 >> 5) & 3) == q ? racc[r0 >> 7] : 0.0f;
+  }
+  return ok;
 }
 
 // Norms |x_i|^2 (k ascending, FMA) of n points of dimension dim.
@@ -714,8 +996,12 @@ __device__ void build_active_lists(const BatchParams& P, int* scan) {
 // made by drot_gl_batch_plan_create -- bands are the instances' groups, the
 // stop test runs on every iteration with "<=", no fold, and n_iter counts
 // the iterations run.
+// Point launches (DIM > 0) run one 512-thread CTA per SM: a kernel that
+// allocates TMEM is given one resident CTA per SM by the runtime's occupancy
+// rule, so a cooperative launch of two per SM is refused.
 template <typename CT, int DIM, bool GL = false>
-__global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P) {
+__global__ void __launch_bounds__(DIM > 0 ? 512 : 256, DIM > 0 ? 1 : 2)
+    batch_solve_kernel(const BatchParams P) {
   constexpr int VEC = 4, KV = kBatchKV;
   const int S = GL ? P.band_cover : kBatchS;  // rows of the band staging
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -724,14 +1010,33 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
   float* f1s = red + (size_t)W * S;                 // [S]
   fpair* dscr = reinterpret_cast<fpair*>(f1s + S);  // [W + 1]
   fpair* oscr = dscr + W + 1;                       // [W]
-  // Point launches: the band's x, k-major [DIM][128], and their norms [128].
-  // float4 reads: 16-byte aligned (the pair scratch above ends on an 8-byte
-  // boundary).
-  float* xs = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(oscr + W) + 15) &
-                                       ~static_cast<uintptr_t>(15));
-  float* xns = xs + DIM * 128;
   __shared__ int s_flag, s_tile;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // Point launches: operand staging after the pair scratch, two mbarriers
+  // and kPtTmemCols TMEM columns (the round buffers of point_tile), held
+  // for the whole launch.
+  PointSmem ps{};
+  uint32_t tmem = 0;
+  unsigned mw[2] = {0u, 0u};
+  __shared__ __align__(8) uint64_t s_mbar[2];
+  __shared__ uint32_t s_tmem;
+  if constexpr (DIM > 0) {
+    ps = point_smem(oscr + W, DIM);
+    if (warp == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                   :: "r"(smem_u32(&s_tmem)), "r"((uint32_t)kPtTmemCols) : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+      mbar_init(&s_mbar[0], 1);
+      mbar_init(&s_mbar[1], 1);
+      fence_mbar_init();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tmem = s_tmem;
+  }
   const int G = gridDim.x;
   const CT* const cbase = reinterpret_cast<const CT*>(P.c);
   unsigned epoch = 0;
@@ -824,17 +1129,6 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
         const int r = lo + idx;
         f1s[idx] = r < hi ? __ldcg(P.phi1 + I.row_off + r) : 0.0f;
       }
-      if constexpr (DIM > 0) {
-        if (even) {
-          for (int idx = threadIdx.x; idx < 128 * DIM; idx += blockDim.x) {
-            const int rl = idx / DIM, k = idx - rl * DIM;
-            xs[k * 128 + rl] =
-                lo + rl < hi ? __ldg(P.xpts + (long long)(I.row_off + lo + rl) * DIM + k) : 0.0f;
-          }
-          for (int rl = threadIdx.x; rl < 128; rl += blockDim.x)
-            xns[rl] = lo + rl < hi ? __ldg(P.xnorm + I.row_off + lo + rl) : 0.0f;
-        }
-      }
       __syncthreads();
       float acc[4][4];
 #pragma unroll
@@ -846,18 +1140,27 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
         constexpr int KVR = decltype(kvr_tag)::value;
         constexpr bool EV = decltype(ev_tag)::value;
         if (hi - lo == 128 * KVR)
-          batch_tile_columns<KVR, EV, true, CT, DIM>(P, I, T, f1s, xs, xns, acc, ms_hi, ms_lo,
-                                                     ob_hi, ob_lo, lane, warp, W);
+          batch_tile_columns<KVR, EV, true, CT>(P, I, T, f1s, acc, ms_hi, ms_lo, ob_hi, ob_lo,
+                                                lane, warp, W);
         else
-          batch_tile_columns<KVR, EV, false, CT, DIM>(P, I, T, f1s, xs, xns, acc, ms_hi, ms_lo,
-                                                      ob_hi, ob_lo, lane, warp, W);
+          batch_tile_columns<KVR, EV, false, CT>(P, I, T, f1s, acc, ms_hi, ms_lo, ob_hi, ob_lo,
+                                                 lane, warp, W);
       };
       using K1 = std::integral_constant<int, 1>;
       using K2 = std::integral_constant<int, 2>;
       using K4 = std::integral_constant<int, 4>;
-      if constexpr (DIM > 0) {  // point launches plan 128-row bands only
-        if (even) run(K1(), std::true_type());
-        else run(K1(), std::false_type());
+      bool point_even = false;
+      if constexpr (DIM > 0) point_even = even;
+      if (point_even) {
+        // the cost from the points on the tensor cores (512-row bands)
+        if constexpr (DIM > 0) {
+          if (!point_tile<DIM, false>(P, I, T, f1s, ps, tmem, s_mbar, mw, red, ms_hi, ms_lo,
+                                      ob_hi, ob_lo)) {
+            aborted = true;
+            atomicExch(P.abort_flag, 1);
+            break;
+          }
+        }
       } else if (even) {
         if (T.kvr == 1) run(K1(), std::true_type());
         else if (T.kvr == 2) run(K2(), std::true_type());
@@ -870,11 +1173,13 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       // Tile partials: rows (fixed warp order), mass and objective (float pairs).
       const fpair wsum = warp_sum_fp(fpair{ms_hi, ms_lo});
       const fpair wobj = even ? warp_sum_fp(fpair{ob_hi, ob_lo}) : fp_make(0.0f);
+      if (!point_even) {
 #pragma unroll
-      for (int v = 0; v < 4; ++v)
-        if (v < T.kvr)
-          *reinterpret_cast<float4*>(red + (size_t)warp * S + v * 128 + lane * 4) =
-              make_float4(acc[v][0], acc[v][1], acc[v][2], acc[v][3]);
+        for (int v = 0; v < 4; ++v)
+          if (v < T.kvr)
+            *reinterpret_cast<float4*>(red + (size_t)warp * S + v * 128 + lane * 4) =
+                make_float4(acc[v][0], acc[v][1], acc[v][2], acc[v][3]);
+      }
       if (lane == 0) {
         dscr[warp] = wsum;
         oscr[warp] = wobj;
@@ -1036,6 +1341,15 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
       const BatchTile T = P.tiles[t];
       if (!__ldcg(P.conv + T.inst)) continue;
       const BatchInst I = P.inst[T.inst];
+      if constexpr (DIM > 0) {  // the same C as the fold's, from the points
+        float u0 = 0.0f, u1 = 0.0f, u2 = 0.0f, u3 = 0.0f;
+        __syncthreads();  // the previous tile's staging is no longer read
+        if (!point_tile<DIM, true>(P, I, T, nullptr, ps, tmem, s_mbar, mw, red, u0, u1, u2, u3)) {
+          aborted = true;
+          atomicExch(P.abort_flag, 1);
+          break;
+        }
+      } else {
       for (int j = T.c0 + warp; j < T.c1; j += W) {
         float* xcol = P.x + I.x_off + (long long)j * I.ld;
         const CT* ccol = cbase + I.c_off + (long long)j * I.ld;
@@ -1045,12 +1359,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
           if (r >= T.hi) continue;
           float xv[VEC], cv[VEC];
           load_vec<VEC>(xcol + r, xv);
-          if constexpr (DIM > 0) {
-#pragma unroll
-            for (int e = 0; e < VEC; ++e) cv[e] = r + e < T.hi ? point_cost<DIM>(P, I, r + e, j) : 0.0f;
-          } else {
-            load_c<VEC, CT>(ccol + r, cv);
-          }
+          load_c<VEC, CT>(ccol + r, cv);
 #pragma unroll
           for (int e = 0; e < VEC; ++e) xv[e] = fmaxf(fmaf(I.s, cv[e], xv[e]), 0.0f);
           if (r + VEC <= T.hi) store_vec<VEC>(xcol + r, xv);
@@ -1060,6 +1369,7 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
               if (r + e < T.hi) xcol[r + e] = xv[e];
           }
         }
+      }
       }
     }
   }
@@ -1076,6 +1386,13 @@ __global__ void __launch_bounds__(256, 2) batch_solve_kernel(const BatchParams P
     }
   }
   if (aborted && blockIdx.x == 0 && threadIdx.x == 0) atomicExch(P.abort_flag, 1);
+  if constexpr (DIM > 0) {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
+                   :: "r"(tmem), "r"((uint32_t)kPtTmemCols) : "memory");
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1124,7 +1441,10 @@ struct BatchPlanImpl {
   int gl = 0;                 // group-lasso plan
   int band_cover = kBatchS;   // GL: rows of the band staging (>= every group's cover)
   BatchTuning tune;           // tile-level shape and prefetch (drot_batch_set_tuning)
-  size_t smem = 0;
+  size_t smem = 0;     // dynamic shared memory of the cost-matrix launches
+  size_t smem_pt = 0;  // and of the point launches
+  int grid_pt = 0;     // CTAs of the point launches (one per SM)
+  int threads_pt = 512;  // their threads per CTA
   long long rows = 0, cols = 0, rowpart = 0, colpart = 0;
   std::vector<BatchInst> inst;
   std::vector<BatchTile> tiles;  // coarse tiles, then fine tiles, then finest tiles
@@ -1196,8 +1516,7 @@ constexpr int kBatchGlMaxCover = 4096;
 // band's x (k-major) and norms.
 static size_t batch_smem(int warps, int dim, int band_cover = kBatchS) {
   return sizeof(float) * ((size_t)warps * band_cover + band_cover) +
-         sizeof(fpair) * (2 * warps + 1) + 16 /* alignment of the point stage */ +
-         sizeof(float) * ((size_t)dim * 128 + 128);
+         sizeof(fpair) * (2 * warps + 1) + (dim > 0 ? point_smem_bytes(dim) : 0);
 }
 
 }  // namespace drot
@@ -1408,31 +1727,45 @@ static int batch_plan_create_impl(int n_inst, const drot_batch_instance* desc, i
       cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop)
     return DROT_ERR_CUDA;
   P.threads = 256;
+  P.threads_pt = 512;
   P.band_rows = band_rows;
-  P.smem = gl ? batch_smem(P.threads / 32, 0, P.band_cover)
-              : batch_smem(P.threads / 32, 16);  // sized for every kernel variant
-  const void* qr_kernels[] = {(const void*)batch_solve_kernel<float, 0>,
-                              (const void*)batch_solve_kernel<__nv_bfloat16, 0>,
-                              (const void*)batch_solve_kernel<float, 8>,
-                              (const void*)batch_solve_kernel<float, 16>};
-  const void* gl_kernels[] = {(const void*)batch_solve_kernel<float, 0, true>,
-                              (const void*)batch_solve_kernel<__nv_bfloat16, 0, true>};
-  std::vector<const void*> kernels;
-  if (gl) kernels.assign(gl_kernels, gl_kernels + 2);
-  else kernels.assign(qr_kernels, qr_kernels + 4);
-  int occ = 1 << 30;
-  for (const void* fn : kernels) {
-    if (P.smem > 48 * 1024 &&
-        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem) !=
-            cudaSuccess)
-      return DROT_ERR_CUDA;
-    int o = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, fn, P.threads, P.smem) != cudaSuccess)
-      return DROT_ERR_CUDA;
-    occ = std::min(occ, o);
-  }
+  P.smem = gl ? batch_smem(P.threads / 32, 0, P.band_cover) : batch_smem(P.threads / 32, 0);
+  P.smem_pt = gl ? 0 : batch_smem(P.threads_pt / 32, 16);  // point launches (d <= 16)
+  struct Variant {
+    const void* fn;
+    size_t smem;
+  };
+  const Variant qr_kernels[] = {{(const void*)batch_solve_kernel<float, 0>, P.smem},
+                                {(const void*)batch_solve_kernel<__nv_bfloat16, 0>, P.smem},
+                                {(const void*)batch_solve_kernel<float, 8>, P.smem_pt},
+                                {(const void*)batch_solve_kernel<float, 16>, P.smem_pt}};
+  const Variant gl_kernels[] = {{(const void*)batch_solve_kernel<float, 0, true>, P.smem},
+                                {(const void*)batch_solve_kernel<__nv_bfloat16, 0, true>, P.smem}};
+  auto occupancy = [&](const Variant* v, int n, int threads, int& occ) -> bool {
+    occ = 1 << 30;
+    for (int i = 0; i < n; ++i) {
+      if (v[i].smem > 48 * 1024 &&
+          cudaFuncSetAttribute(v[i].fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)v[i].smem) != cudaSuccess)
+        return false;
+      int o = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, v[i].fn, threads, v[i].smem) !=
+          cudaSuccess)
+        return false;
+      occ = std::min(occ, o);
+    }
+    return true;
+  };
+  int occ = 0, occ_pt = 0;
+  if (!occupancy(gl ? gl_kernels : qr_kernels, 2, P.threads, occ)) return DROT_ERR_CUDA;
   if (occ <= 0) return DROT_ERR_CUDA;
   P.grid = occ * sms;
+  if (!gl) {
+    // point launches hold kPtTmemCols TMEM columns per CTA for the whole launch
+    if (!occupancy(qr_kernels + 2, 2, P.threads_pt, occ_pt)) return DROT_ERR_CUDA;
+    occ_pt = std::min(occ_pt, 512 / kPtTmemCols);
+    P.grid_pt = occ_pt * sms;
+  }
 
   size_t off = 0;
   P.off_ctrl = off;  off = al(off + 512);
@@ -1530,7 +1863,12 @@ int drot_batch_upload(drot_batch_plan plan, void* workspace, size_t workspace_by
 // Shared by the cost-matrix and the point-cloud launches: parameter block,
 // control words, warm start, then the cooperative solve kernel `fn`.
 static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, void* workspace,
-                        size_t workspace_bytes, int max_iters, cudaStream_t st) {
+                        size_t workspace_bytes, int max_iters, cudaStream_t st,
+                        bool points = false) {
+  const int grid = points ? P.grid_pt : P.grid;
+  const int threads = points ? P.threads_pt : P.threads;
+  const size_t smem = points ? P.smem_pt : P.smem;
+  if (grid <= 0) return DROT_ERR_INVALID_ARG;
   if (workspace_bytes < P.total || ((uintptr_t)workspace & 255u)) return DROT_ERR_WORKSPACE;
   char* ws = (char*)workspace;
   B.inst = (const BatchInst*)(ws + P.off_inst);
@@ -1541,8 +1879,8 @@ static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, 
   B.n_tiles_x = P.n_tiles_x;
   B.n_items_x = P.n_items_x;
   // active tiles of a level below which the solve moves to the next finer one
-  B.fine_threshold = (int)((long long)P.grid * P.tune.level_quarters / 4);
-  B.tail_tiles = (int)((long long)P.grid * P.tune.tail_quarters / 4);
+  B.fine_threshold = (int)((long long)grid * P.tune.level_quarters / 4);
+  B.tail_tiles = (int)((long long)grid * P.tune.tail_quarters / 4);
   B.items = (const BatchItem*)(ws + P.off_items);
   B.n_items = P.n_items;
   B.res_slot = (float2*)(ws + P.off_res);
@@ -1577,12 +1915,12 @@ static int batch_launch(const BatchPlanImpl& P, const void* fn, BatchParams& B, 
   if (cudaMemsetAsync(ws + P.off_ctrl, 0, 512, st) != cudaSuccess) return DROT_ERR_CUDA;
   batch_init_kernel<<<dim3(64, P.n_inst), 256, 0, st>>>(B);
   if (cudaGetLastError() != cudaSuccess) return DROT_ERR_CUDA;
-  if (P.smem > 48 * 1024 &&
-      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem) !=
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess)
     return DROT_ERR_CUDA;
   void* args[] = {(void*)&B};
-  if (cudaLaunchCooperativeKernel(fn, dim3(P.grid), dim3(P.threads), args, P.smem, st) !=
+  if (cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), args, smem, st) !=
       cudaSuccess) {
     cudaGetLastError();
     return DROT_ERR_CUDA;
@@ -1657,7 +1995,7 @@ int drot_qr_batch_launch_points(drot_batch_plan plan, const float* xpts, const f
   if (!plan || !xpts || !ypts || !p || !q || !x || !workspace || max_iters < 0)
     return DROT_ERR_INVALID_ARG;
   if (dim != 8 && dim != 16) return DROT_ERR_UNSUPPORTED;
-  if (plan->p.band_rows != 128 || plan->p.gl) return DROT_ERR_INVALID_ARG;  // point tiles: 128-row QR bands
+  if (plan->p.band_rows != 512 || plan->p.gl) return DROT_ERR_INVALID_ARG;  // point tiles: 512-row QR bands
   if (((uintptr_t)x & 15u) || ((uintptr_t)xpts & 15u) || ((uintptr_t)ypts & 15u))
     return DROT_ERR_INVALID_ARG;
   const BatchPlanImpl& P = plan->p;
@@ -1685,7 +2023,7 @@ int drot_qr_batch_launch_points(drot_batch_plan plan, const float* xpts, const f
   if (cudaGetLastError() != cudaSuccess) return DROT_ERR_CUDA;
   const void* fn = dim == 8 ? (const void*)batch_solve_kernel<float, 8>
                             : (const void*)batch_solve_kernel<float, 16>;
-  return batch_launch(P, fn, B, workspace, workspace_bytes, max_iters, st);
+  return batch_launch(P, fn, B, workspace, workspace_bytes, max_iters, st, true);
 }
 
 int drot_batch_set_iteration_log(drot_batch_plan plan, unsigned long long* times,

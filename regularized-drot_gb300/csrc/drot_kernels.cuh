@@ -358,7 +358,7 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
 
 // Instruction descriptor of kind::tf32: D F32, A and B TF32, both K-major,
 // N >> 3 at bit 17, M >> 4 at bit 24.
-constexpr uint32_t tf32_idesc(int m, int n) {
+__host__ __device__ constexpr uint32_t tf32_idesc(int m, int n) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) |
          ((uint32_t)(m >> 4) << 24);
 }

@@ -236,9 +236,9 @@ def batch_quadratic_drot_fn(batch, c, p, q, max_iters, *, cg_tol=CG_TOL,
     """QRBatch.solve with a backward; c, p, q packed (QRBatch.pack_c /
     pack_marginals), returns the packed plans (QRBatch.unpack gives views).
     points=(x_cat, y_cat, scale): the forward recomputes the cost from the
-    clouds inside the solve (QRBatch.solve_points; the batch must have
-    band_rows=128) -- c must hold the same cost (e.g. packed_sqeuclidean_cost
-    of the clouds); the backward reads it once."""
+    clouds inside the solve (QRBatch.solve_points, on the tensor cores) -- c
+    must hold the same cost (packed_sqeuclidean_cost of the clouds: the
+    values the solve recomputes); the backward reads it once."""
     if not all(r > 0 for r in batch.r_weight):
         raise RuntimeError("batch_quadratic_drot_fn needs r_weight > 0 for every instance")
     return BatchQuadraticDROTFn.apply(c, p, q, batch, int(max_iters), float(cg_tol),

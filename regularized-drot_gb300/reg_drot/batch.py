@@ -133,7 +133,7 @@ class QRBatch:
         self.cols_per_tile = cols_per_tile
         if band_rows not in (128, 512):
             raise RuntimeError("band_rows must be 128 or 512")
-        self.band_rows = band_rows  # 128: plans for point-cloud launches (solve_points)
+        self.band_rows = band_rows  # 512 (default; point-cloud launches need it) or 128
         if tuning is not None and set(tuning) - set(_TUNING_FIELDS):
             raise RuntimeError(f"unknown tuning fields {sorted(set(tuning) - set(_TUNING_FIELDS))}")
         self.tuning = None if tuning is None else dict(tuning)  # tile levels (set_tuning)
@@ -247,8 +247,8 @@ class QRBatch:
         of its points (x_cat, y_cat: every instance's points concatenated in
         order, [rows, dim] / [cols, dim] float32, dim 8 or 16), recomputed in
         the fused update instead of read from memory."""
-        if self.band_rows != 128:
-            raise RuntimeError("point-cloud solves need a QRBatch built with band_rows=128")
+        if self.band_rows != 512:
+            raise RuntimeError("point-cloud solves need a QRBatch with 512-row bands (the default)")
         for t, name, n in ((x_cat, "x_cat", self.total_rows), (y_cat, "y_cat", self.total_cols)):
             if t.device != self.device or t.dtype != torch.float32 or t.dim() != 2 or \
                     t.size(0) != n or t.size(1) not in (8, 16) or not t.is_contiguous():

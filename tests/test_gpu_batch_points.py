@@ -2,13 +2,15 @@
 fused update (drot_qr_batch_launch_points; QRBatch.solve_points).
 
 The cost C_ij = scale * max(|x_i|^2 + |y_j|^2 - 2 <x_i, y_j>, 0) is never
-stored; each iteration that reads C recomputes it in FP32 (FMA, k
-ascending).  Checks: against the FP32 oracle on the FP64 cost rounded to
-FP32 (the two costs differ by FP32 rounding, about 1e-7 relative), against
-the same batch solved on the stored cost of the tensor-core kernel, and the
-autograd path with a point-cloud forward.  Bars as for the other batch
-tests: ||X - X_ref||_F <= 1e-5 ||X_ref||_F (max entry 1e-4), n_iter within
-one stop check.
+stored: on every iteration that reads C the launch recomputes the tile's
+values with the split-TF32 tcgen05 Gram product of the cost kernel (the
+same MMAs and epilogue), so they equal the stored cost of
+packed_sqeuclidean_cost bit for bit -- checked directly: one iteration from
+the warm start gives bitwise the same X on both paths.  Then: against the
+FP32 oracle on that cost, against the same batch solved on the stored cost,
+and the autograd path with a point-cloud forward.  Bars as for the other
+batch tests: ||X - X_ref||_F <= 1e-5 ||X_ref||_F (max entry 1e-4), n_iter
+within one stop check.
 """
 import numpy as np
 import pytest
@@ -42,16 +44,38 @@ def _close(xg, xo):
 
 
 @pytest.mark.parametrize("dim", [8, 16])
+@pytest.mark.parametrize("cpt", [32, 256])
+def test_points_first_iteration_equals_stored_cost_bitwise(cuda, solver_lib, dim, cpt):
+    """Iteration 0 from the warm start stores X = y - sC elementwise (no sums
+    involved), so equal X on both paths means equal C."""
+    from reg_drot.batch import QRBatch
+    from reg_drot.cost import packed_sqeuclidean_cost
+    xs, ys, ps, qs = _clouds(SHAPES, dim, 11)
+    xc = torch.tensor(np.concatenate(xs), device=cuda)
+    yc = torch.tensor(np.concatenate(ys), device=cuda)
+    B = QRBatch(SHAPES, 2.0, 1e-3, 0.0, device=cuda, cols_per_tile=cpt)
+    p, q = B.pack_marginals([torch.tensor(v) for v in ps], [torch.tensor(v) for v in qs])
+    c = packed_sqeuclidean_cost(B, xc, yc, SCALE)
+    x1, _ = B.solve(c, p, q, 1)
+    x1 = x1.clone()
+    x2, _ = B.solve_points(xc, yc, p, q, 1, SCALE)
+    for k in range(len(SHAPES)):
+        assert torch.equal(B.view(x1, k), B.view(x2, k)), k
+
+
+@pytest.mark.parametrize("dim", [8, 16])
 def test_points_solve_matches_oracle(cuda, solver_lib, dim):
     from reg_drot.batch import QRBatch
+    from reg_drot.cost import packed_sqeuclidean_cost
     xs, ys, ps, qs = _clouds(SHAPES, dim, dim)
-    B = QRBatch(SHAPES, 2.0, 1e-3, 1e-5, device=cuda, band_rows=128, cols_per_tile=256)
+    B = QRBatch(SHAPES, 2.0, 1e-3, 1e-5, device=cuda, cols_per_tile=256)
     p, q = B.pack_marginals([torch.tensor(v) for v in ps], [torch.tensor(v) for v in qs])
     xc = torch.tensor(np.concatenate(xs), device=cuda)
     yc = torch.tensor(np.concatenate(ys), device=cuda)
     x, info = B.solve_points(xc, yc, p, q, 50000, SCALE)
+    cst = packed_sqeuclidean_cost(B, xc, yc, SCALE)  # the values the launch recomputes
     for k in range(len(SHAPES)):
-        c = (A.sqeuclidean(xs[k], ys[k]) * SCALE).astype(np.float32)
+        c = B.view(cst, k).cpu().numpy()
         o = O.quadratic_drot(c, ps[k], qs[k], 2.0, 1e-3, 50000, 1e-5)
         assert info[k]["converged"] == 1
         assert abs(info[k]["n_iter"] - o["n_iter"]) <= 2, (k, info[k], o["n_iter"])
@@ -66,7 +90,7 @@ def test_points_solve_matches_stored_cost_solve(cuda, solver_lib):
     xs, ys, ps, qs = _clouds(SHAPES, 16, 3)
     xc = torch.tensor(np.concatenate(xs), device=cuda)
     yc = torch.tensor(np.concatenate(ys), device=cuda)
-    B = QRBatch(SHAPES, 2.0, 1e-3, 1e-5, device=cuda, band_rows=128, cols_per_tile=256)
+    B = QRBatch(SHAPES, 2.0, 1e-3, 1e-5, device=cuda, cols_per_tile=256)
     p, q = B.pack_marginals([torch.tensor(v) for v in ps], [torch.tensor(v) for v in qs])
     c = packed_sqeuclidean_cost(B, xc, yc, SCALE)
     x1, i1 = B.solve(c, p, q, 50000)
@@ -79,11 +103,10 @@ def test_points_solve_matches_stored_cost_solve(cuda, solver_lib):
             assert ok, (k, err)
         else:
             # A stop moved by one check: each solve against the oracle stopped
-            # at its own iteration, on the cost that solve used.
-            cp = (A.sqeuclidean(xs[k], ys[k]) * SCALE).astype(np.float32)
+            # at its own iteration (both on the same cost values).
             cs = B.view(c, k).cpu().numpy()
-            for r, xk, ck in ((i2[k], x2, cp), (i1[k], x1, cs)):
-                o = O.quadratic_drot_at(ck, ps[k], qs[k], 2.0, 1e-3, r["n_iter"])
+            for r, xk in ((i2[k], x2), (i1[k], x1)):
+                o = O.quadratic_drot_at(cs, ps[k], qs[k], 2.0, 1e-3, r["n_iter"])
                 ok, err = _close(B.view(xk, k).cpu().numpy(), o["x"])
                 assert ok, (k, err)
 
@@ -93,25 +116,27 @@ def test_points_fixed_iterations_and_determinism(cuda, solver_lib):
     xs, ys, ps, qs = _clouds(SHAPES, 8, 5)
     xc = torch.tensor(np.concatenate(xs), device=cuda)
     yc = torch.tensor(np.concatenate(ys), device=cuda)
-    B = QRBatch(SHAPES, 2.0, 1e-3, 0.0, device=cuda, band_rows=128, cols_per_tile=128)
+    B = QRBatch(SHAPES, 2.0, 1e-3, 0.0, device=cuda, cols_per_tile=128)
     p, q = B.pack_marginals([torch.tensor(v) for v in ps], [torch.tensor(v) for v in qs])
+    from reg_drot.cost import packed_sqeuclidean_cost
+    cst = packed_sqeuclidean_cost(B, xc, yc, SCALE)  # the values the launch recomputes
     for mi in (1, 2, 9):
         x, info = B.solve_points(xc, yc, p, q, mi, SCALE)
         x = x.clone()
         x2, _ = B.solve_points(xc, yc, p, q, mi, SCALE)
         assert torch.equal(x, x2)
         for k in range(len(SHAPES)):
-            c = (A.sqeuclidean(xs[k], ys[k]) * SCALE).astype(np.float32)
+            c = B.view(cst, k).cpu().numpy()
             o = O.quadratic_drot(c, ps[k], qs[k], 2.0, 1e-3, mi, 0.0)
             assert info[k]["n_iter"] == mi + 1
             ok, err = _close(B.view(x, k).cpu().numpy(), o["x"])
             assert ok, (mi, k, err)
 
 
-def test_points_need_128_row_plans(cuda, solver_lib):
+def test_points_need_512_row_plans(cuda, solver_lib):
     from reg_drot.batch import QRBatch
     xs, ys, ps, qs = _clouds(SHAPES[:2], 8, 1)
-    B = QRBatch(SHAPES[:2], 2.0, 1e-3, 1e-4, device=cuda)  # 512-row bands
+    B = QRBatch(SHAPES[:2], 2.0, 1e-3, 1e-4, device=cuda, band_rows=128)
     p, q = B.pack_marginals([torch.tensor(v) for v in ps], [torch.tensor(v) for v in qs])
     with pytest.raises(RuntimeError):
         B.solve_points(torch.tensor(np.concatenate(xs), device=cuda),
@@ -128,7 +153,7 @@ def test_points_forward_in_autograd(cuda, solver_lib):
     for use_points in (False, True):
         xc = torch.tensor(np.concatenate(xs), device=cuda, requires_grad=True)
         yc = torch.tensor(np.concatenate(ys), device=cuda, requires_grad=True)
-        B = QRBatch(shapes, 2.0, 1e-2, 1e-7, device=cuda, band_rows=128, cols_per_tile=256)
+        B = QRBatch(shapes, 2.0, 1e-2, 1e-7, device=cuda, cols_per_tile=256)
         p, q = B.pack_marginals([torch.tensor(v) for v in ps], [torch.tensor(v) for v in qs])
         c = packed_sqeuclidean_cost(B, xc, yc, SCALE)
         pts = (xc.detach(), yc.detach(), SCALE) if use_points else None
