@@ -538,14 +538,15 @@ __device__ __forceinline__ void reduce_lines(const float* base, int stride, int 
 // reads them from there: 8 bytes of DRAM traffic per element instead of 12.
 //
 // The tile is a 512-row band in four 128-row sub-bands; its columns go in
-// rounds of kPtCols = 16.  Per round one thread issues, for every sub-band,
-// the 3 x DIM/8 MMAs (M = 128 rows, N = 16 columns) into a 64-column TMEM
-// buffer (sub-band v at columns 16 v); the buffers alternate, so round n+1's
-// MMAs run while round n is updated.  Warp w reads TMEM lane quadrant
-// q = w % 4 -- rows 128 v + 32 q + lane -- for the round's columns
-// 8 (w / 4) .. + 7: each lane updates one row of each sub-band (its row
-// partials stay in registers) and the column sums are warp reductions,
-// combined over the quadrants in shared memory in a fixed order.
+// rounds of kPtCols = 64.  Per round, lane 0 of warp 4 v issues sub-band v's
+// 3 x DIM/8 MMAs (M = 128 rows, N = 64 columns) into its quarter of a
+// 256-column TMEM buffer and commits; the round's mbarrier completes on the
+// four commits.  The buffers alternate, so round n+1's MMAs run while round
+// n is updated.  Warp w (of 16) reads TMEM lane quadrant q = w % 4 -- rows
+// 128 v + 32 q + lane -- for the round's columns 16 (w / 4) .. + 15: each
+// lane updates one row of each sub-band (its row partials stay in
+// registers) and the column sums are warp reductions, combined over the
+// quadrants in shared memory in a fixed order.
 constexpr int kPtCols = 64;    // columns per round (MMA N)
 constexpr int kPtTmemCols = 2 * 4 * kPtCols;  // two buffers x four sub-bands
 
@@ -646,14 +647,16 @@ __device__ bool point_tile(const BatchParams& P, const BatchInst& I, const Batch
     }
     fence_proxy_async_shared();
   };
-  auto issue = [&](int n) {  // one thread: round n's MMAs, then the commit
+  // Round n's MMAs: sub-band v's chain issued by lane 0 of warp 4 v (four
+  // issuing threads share the work), each followed by its commit (the
+  // round's mbarrier completes on the four arrivals).
+  const bool issuer = lane == 0 && (warp & 3) == 0 && warp < 16;
+  auto issue = [&](int n) {
+    const int v = warp >> 2;
     const uint32_t yh = smem_u32(S.yb + (n & 1) * 2 * ysub);
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const uint32_t xh = smem_u32(S.xa + v * 2 * sub);
-      gram_tf32x3(xh, xh + sub, yh, yh + ysub, DIM,
-                  tmem + (uint32_t)((n & 1) * 4 * kPtCols + v * kPtCols), idesc);
-    }
+    const uint32_t xh = smem_u32(S.xa + v * 2 * sub);
+    gram_tf32x3(xh, xh + sub, yh, yh + ysub, DIM,
+                tmem + (uint32_t)((n & 1) * 4 * kPtCols + v * kPtCols), idesc);
     tc_commit(&mbar[n & 1]);
   };
   // lane quadrant and column group (16 of the round's 64 columns; 16 warps)
@@ -691,7 +694,7 @@ __device__ bool point_tile(const BatchParams& P, const BatchInst& I, const Batch
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (tid == 0 && rounds > 0) issue(0);
+  if (issuer && rounds > 0) issue(0);
 #pragma unroll
   for (int v = 0; v < 4; ++v) xnr[v] = S.xn[128 * v + 32 * q + lane];
   const float s = I.s, kappa = I.kappa, krcp = I.kappa_rcp, cscale = P.cscale;
@@ -713,7 +716,7 @@ __device__ bool point_tile(const BatchParams& P, const BatchInst& I, const Batch
       break;
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (tid == 0 && n + 1 < rounds) issue(n + 1);
+    if (issuer && n + 1 < rounds) issue(n + 1);
     if (!UNFOLD && n > 0 && tid >= 32 && tid < 32 + kPtCols) {  // round n-1's column sums (warps 1, 2)
       const int jl = tid - 32, j = c0 + (n - 1) * kPtCols + jl;
       const float* cp = S.cpart + ((n - 1) & 1) * 4 * kPtCols;
@@ -1028,8 +1031,8 @@ __global__ void __launch_bounds__(DIM > 0 ? 512 : 256, DIM > 0 ? 1 : 2)
       asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (threadIdx.x == 0) {
-      mbar_init(&s_mbar[0], 1);
-      mbar_init(&s_mbar[1], 1);
+      mbar_init(&s_mbar[0], 4);  // one commit per sub-band (point_tile)
+      mbar_init(&s_mbar[1], 4);
       fence_mbar_init();
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
