@@ -30,6 +30,7 @@ that of the exact solution on a locally fixed support, so it assumes the
 forward solve converged (a warning is raised otherwise) and r_weight > 0.
 """
 import ctypes
+import math
 import warnings
 
 import numpy as np
@@ -530,12 +531,19 @@ class BatchGroupLassoDROTFn(torch.autograd.Function):
         return cbar.to(c.dtype), pbar, qbar, None, None, None, None
 
 
-def batch_group_lasso_drot_fn(batch, c, p, q, max_iters, *, last_k=64, segment=32):
+def batch_group_lasso_drot_fn(batch, c, p, q, max_iters, *, last_k=64, segment=None):
     """GLBatch.solve with a backward: for every instance, the unrolled
     adjoint of last_k GL iterations taken from its solution (the state the
     batched solve stopped at, held fixed) -- the truncated adjoint at the
     fixed point, where last_k more iterations leave the plan within the stop
-    tolerance.  c, p, q packed (GLBatch.pack_c / pack_marginals)."""
+    tolerance.  c, p, q packed (GLBatch.pack_c / pack_marginals).
+    segment: checkpoint spacing of the recomputation; the backward holds
+    about last_k / segment checkpoints and segment stored iterates of the
+    packed plans, so the default ceil(sqrt(last_k)) keeps both near their
+    minimum (8 + 8 plan copies for last_k = 64).  The gradient does not
+    depend on it."""
+    if segment is None:
+        segment = max(1, int(math.ceil(math.sqrt(int(last_k)))))
     if int(last_k) <= 0:
         raise RuntimeError("last_k must be positive")
     return BatchGroupLassoDROTFn.apply(c, p, q, batch, int(max_iters), int(last_k),
