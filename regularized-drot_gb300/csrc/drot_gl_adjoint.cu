@@ -356,6 +356,7 @@ struct drot_gl_adjoint_batch_plan_s {
   int n_inst = 0;
   std::vector<GlaParams> prm;  // host copies; pointers filled by setup
   std::vector<size_t> ws_off;  // per instance: scratch offset in the workspace
+  std::vector<long long> v_off;  // per instance: offset of its vector adjoint in vbar
   size_t off_params = 0, total = 0;
   int max_lines = 0, max_chunks = 0, max_rblocks = 0;
   long long max_tasks = 0;
@@ -429,13 +430,15 @@ int drot_gl_adjoint_batch_plan_create(int n_inst, const drot_gl_adjoint_batch_in
   P->n_inst = n_inst;
   P->prm.resize(n_inst);
   P->ws_off.resize(n_inst);
+  P->v_off.resize(n_inst);
   size_t off = al(sizeof(GlaParams) * (size_t)n_inst);
   long long vo = 0;
   for (int k = 0; k < n_inst; ++k) {
     const drot_gl_adjoint_batch_instance& d = desc[k];
     if (d.n_rows <= 0 || d.n_cols <= 0 || d.ld < d.n_rows || d.n_groups <= 0 ||
         d.n_groups > kMaxGroups || d.n_groups > d.n_rows || d.x_offset < 0 || d.c_offset < 0 ||
-        d.row_offset < 0 || d.col_offset < 0 || !(d.step_size > 0.0f) || !(d.lambda >= 0.0f)) {
+        d.row_offset < 0 || d.col_offset < 0 || d.row_offset > INT32_MAX - d.n_rows ||
+        d.col_offset > INT32_MAX - d.n_cols || !(d.step_size > 0.0f) || !(d.lambda >= 0.0f)) {
       delete P;
       return DROT_ERR_INVALID_ARG;
     }
@@ -457,9 +460,7 @@ int drot_gl_adjoint_batch_plan_create(int n_inst, const drot_gl_adjoint_batch_in
     A.xo = d.x_offset;
     A.ro = (int)d.row_offset;
     A.co = (int)d.col_offset;
-    // pointers are offsets until setup: C / Xbar / Cbar at c_offset / x_offset,
-    // p / q at the line offsets, vbar at the running offset vo
-    A.vbar = (float*)(uintptr_t)(vo * sizeof(float));
+    P->v_off[k] = vo;  // the buffers' pointers are filled by setup
     vo += 2LL * (d.n_rows + d.n_cols) + 1;
     P->ws_off[k] = off;
     off = al(off + L.total);
@@ -501,7 +502,7 @@ int drot_gl_adjoint_batch_setup(drot_gl_adjoint_batch_plan plan,
     A.c_bf16 = c_dtype == DROT_C_BF16;
     A.xbar = xbar + d.x_offset;
     A.cbar = cbar + d.c_offset;
-    A.vbar = vbar + (uintptr_t)plan->prm[k].vbar / sizeof(float);
+    A.vbar = vbar + plan->v_off[k];
     A.pbar = pbar + d.row_offset;
     A.qbar = qbar + d.col_offset;
     A.rbar = (float*)(w + L.off_rbar);

@@ -474,7 +474,10 @@ class BatchGroupLassoDROTFn(torch.autograd.Function):
         instances at once (drot_batch_resume, checkpoints every `segment`
         iterations, the segment's states kept), then each reverse iteration
         is one set of launches over all instances
-        (drot_gl_adjoint_batch_step)."""
+        (drot_gl_adjoint_batch_step).  The recomputation runs in the
+        batch's own workspace: afterwards GLBatch.results() describes those
+        launches; the forward's per-instance outcomes stay in
+        grad_fn.info."""
         c, p, q = ctx.saved_tensors
         B = ctx.batch
         dev = c.device

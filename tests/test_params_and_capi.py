@@ -197,3 +197,49 @@ def test_cost_and_adjoint_reject_bad_arguments_on_the_host(solver_lib):
                                            None) == 1
     adj[0].ld, adj[0].lambda_ = 10, 0.0
     assert solver_lib.drot_qr_adjoint_workspace_bytes(1, adj) == 0  # lambda must be > 0
+
+
+def test_batch_tuning_is_checked_on_the_host(solver_lib):
+    from reg_drot._lib import DrotBatchTuning
+    names = [n for n, _ in DrotBatchTuning._fields_]
+    keep = DrotBatchTuning(*([-1] * len(names)))
+    assert solver_lib.drot_batch_set_tuning(ctypes.byref(keep)) == 0
+    for name, value in [("prefetch_distance", 9), ("fine_cols", 0), ("item_lines", 0),
+                        ("finest_item_lines", 0), ("level_quarters", 5000),
+                        ("tail_quarters", 5000), ("fine_cols", 5000)]:
+        t = DrotBatchTuning(*([-1] * len(names)))
+        setattr(t, name, value)
+        assert solver_lib.drot_batch_set_tuning(ctypes.byref(t)) == 1, (name, value)
+    assert solver_lib.drot_batch_set_tuning(None) == 0  # the defaults again
+    assert solver_lib.drot_batch_resume(None, None, 0, None, None, None, 1, None, 0, None) == 1
+
+
+def test_gl_adjoint_batch_plan_is_checked_on_the_host(solver_lib):
+    from reg_drot._lib import DrotGlAdjointBatchInstance
+    good = dict(n_rows=300, n_cols=200, ld=300, n_groups=3, x_offset=0, c_offset=0,
+                row_offset=0, col_offset=0, step_size=0.004, lambda_=1e-3)
+    bad = [dict(ld=299), dict(n_groups=0), dict(n_groups=301), dict(x_offset=-4),
+           dict(row_offset=-1), dict(col_offset=2 ** 31 - 10), dict(step_size=0.0),
+           dict(lambda_=-1.0), dict(n_cols=0)]
+    h = ctypes.c_void_p()
+    for change in bad:
+        arr = (DrotGlAdjointBatchInstance * 2)()
+        for d in arr:
+            for k, v in good.items():
+                setattr(d, k, v)
+        for k, v in change.items():
+            setattr(arr[1], k, v)
+        assert solver_lib.drot_gl_adjoint_batch_plan_create(2, arr, ctypes.byref(h)) == 1, change
+        assert not h.value
+    arr = (DrotGlAdjointBatchInstance * 2)()
+    for d in arr:
+        for k, v in good.items():
+            setattr(d, k, v)
+    arr[1].row_offset, arr[1].col_offset = 300, 200
+    assert solver_lib.drot_gl_adjoint_batch_plan_create(2, arr, ctypes.byref(h)) == 0
+    assert solver_lib.drot_gl_adjoint_batch_workspace_bytes(h) > 0
+    assert solver_lib.drot_gl_adjoint_batch_setup(h, arr, None, 0, None, None, None, None,
+                                                  None, None, 0, None) == 1
+    assert solver_lib.drot_gl_adjoint_batch_step(h, None, None, None, None, 0, None) == 1
+    solver_lib.drot_gl_adjoint_batch_plan_destroy(h)
+    assert solver_lib.drot_gl_adjoint_batch_workspace_bytes(None) == 0
