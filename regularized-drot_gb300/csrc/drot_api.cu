@@ -433,6 +433,27 @@ static size_t scratch_bytes(int mode, int nr, int nc, int G, const int* ubounds 
   return best;
 }
 
+// Column-aligned copies.  Columns of n_rows % 4 != 0 rows are not 16-byte
+// aligned, so the 128-bit vector path cannot read them in place; given the
+// room, the solve runs on copies of C and X whose leading dimension is
+// n_rows rounded up to 4 (the pad rows zero and masked), then copies X back:
+// about 24 bytes per element once against 10 per iteration.  Every solve
+// that has the room takes it, short ones too, so a solve split into
+// segments (checkpointed autograd) keeps the arithmetic of one whole solve.
+// The region follows the scratch.
+constexpr int kRepackMinIters = 1;
+static size_t repack_bytes(int nr, int nc) {
+  const size_t ldp = ((size_t)nr + 3) & ~(size_t)3;
+  return 2 * align_up(ldp * (size_t)nc * sizeof(float));
+}
+// Workspace of drot_*_solve: the scratch, then the aligned copies when the
+// columns are unaligned.
+static size_t solve_ws_bytes(int mode, int nr, int nc, int G, const int* ubounds = nullptr) {
+  const size_t sc = scratch_bytes(mode, nr, nc, G, ubounds);
+  if (sc == 0) return 0;
+  return nr % 4 != 0 ? align_up(sc) + repack_bytes(nr, nc) : sc;
+}
+
 static long long barrier_timeout_ns() {
   const char* e = getenv("DROT_BARRIER_TIMEOUT_MS");
   if (e && *e) {
@@ -493,18 +514,32 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
   if (A.nr <= 0 || A.nc <= 0 || A.max_iters < 0) return DROT_ERR_INVALID_ARG;
   if (((uintptr_t)A.ws & (kAlign - 1)) != 0) return DROT_ERR_WORKSPACE;
   if (A.ctype != DROT_C_F32 && A.ctype != DROT_C_BF16) return DROT_ERR_INVALID_ARG;
-  const long long ld = A.nr;
   const bool c_aligned = A.ctype == DROT_C_F32 ? aligned16(A.c) : (((uintptr_t)A.c & 7u) == 0);
-  const bool aligned4 = ld % 4 == 0 && aligned16(A.x) && c_aligned;
+  const bool aligned4 = A.nr % 4 == 0 && aligned16(A.x) && c_aligned;
+  char* ws = (char*)A.ws;
+  // Unaligned columns: the aligned copies when the workspace holds them.
+  bool repack = false;
+  char* cpad = nullptr;
+  float* xpad = nullptr;
+  const long long ldp = ((long long)A.nr + 3) & ~3LL;
+  if (!aligned4 && A.max_iters >= kRepackMinIters) {
+    const size_t base = align_up(scratch_bytes(A.mode, A.nr, A.nc, A.G, A.bounds));
+    if (base > 0 && A.ws_bytes >= base + repack_bytes(A.nr, A.nc)) {
+      repack = true;
+      cpad = ws + base;
+      xpad = (float*)(cpad + align_up((size_t)ldp * A.nc * sizeof(float)));
+    }
+  }
+  const long long ld = repack ? ldp : A.nr;
   Plan pl;
-  int rc = choose_plan(A.mode, A.nr, A.nc, A.G, aligned4, pl, A.ctype, A.bounds);
+  int rc = choose_plan(A.mode, A.nr, A.nc, A.G, aligned4 || repack, pl, A.ctype, A.bounds);
   if (rc != DROT_OK) return rc;
   if (A.ws_bytes < pl.total) return DROT_ERR_WORKSPACE;
 
-  char* ws = (char*)A.ws;
   SolveParams prm;
   memset(&prm, 0, sizeof(prm));
-  prm.c = A.c; prm.p = A.p; prm.q = A.q; prm.x = A.x;
+  prm.c = repack ? (const void*)cpad : A.c; prm.p = A.p; prm.q = A.q;
+  prm.x = repack ? xpad : A.x;
   prm.a = A.a; prm.b = A.b; prm.phi1 = A.phi1; prm.phi2 = A.phi2; prm.alpha = A.alpha;
   prm.ld = ld; prm.nr = A.nr; prm.nc = A.nc;
   prm.s = A.s; prm.kappa = A.kappa; prm.lambda = A.lambda;
@@ -540,6 +575,20 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
   prm.stall_cta = stall_cta_hook();
 
   if (cudaMemsetAsync(ws, 0, 512, A.stream) != cudaSuccess) return DROT_ERR_CUDA;
+  if (repack) {
+    const size_t esz = A.ctype == DROT_C_F32 ? sizeof(float) : 2;
+    const size_t padr = (size_t)(ldp - A.nr);
+    if ((padr && (cudaMemset2DAsync(cpad + A.nr * esz, ldp * esz, 0, padr * esz, A.nc,
+                                    A.stream) != cudaSuccess ||
+                  cudaMemset2DAsync(xpad + A.nr, ldp * sizeof(float), 0, padr * sizeof(float),
+                                    A.nc, A.stream) != cudaSuccess)) ||
+        cudaMemcpy2DAsync(cpad, ldp * esz, A.c, A.nr * esz, A.nr * esz, A.nc,
+                          cudaMemcpyDeviceToDevice, A.stream) != cudaSuccess ||
+        cudaMemcpy2DAsync(xpad, ldp * sizeof(float), A.x, A.nr * sizeof(float),
+                          A.nr * sizeof(float), A.nc, cudaMemcpyDeviceToDevice,
+                          A.stream) != cudaSuccess)
+      return DROT_ERR_CUDA;
+  }
   SolveFn fn = kernel_for(A.mode, pl.vec, pl.kv, pl.tma, pl.ctype);
   if (pl.smem > 48 * 1024 &&
       cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -551,6 +600,10 @@ static int run_solve(const SolveArgs& A, drot_result* result) {
     cudaGetLastError();
     return DROT_ERR_CUDA;
   }
+  if (repack && cudaMemcpy2DAsync(A.x, A.nr * sizeof(float), xpad, ldp * sizeof(float),
+                                  A.nr * sizeof(float), A.nc, cudaMemcpyDeviceToDevice,
+                                  A.stream) != cudaSuccess)
+    return DROT_ERR_CUDA;
   if (result) return read_stats(ws, result, A.stream);
   return DROT_OK;
 }
@@ -712,11 +765,11 @@ int drot_init_state(int n_rows, int n_cols, float step_size, int warm, const flo
 }
 
 size_t drot_qr_workspace_bytes(int n_rows, int n_cols) {
-  return scratch_bytes(MODE_QR, n_rows, n_cols, 0);
+  return solve_ws_bytes(MODE_QR, n_rows, n_cols, 0);
 }
 
 size_t drot_gl_workspace_bytes(int n_rows, int n_cols, int n_groups) {
-  return scratch_bytes(MODE_GL, n_rows, n_cols, n_groups);
+  return solve_ws_bytes(MODE_GL, n_rows, n_cols, n_groups);
 }
 
 int drot_qr_solve_ex(const void* c, int c_dtype, const float* p, const float* q, int n_rows,
@@ -771,9 +824,9 @@ static bool valid_bounds(int nr, int G, const int* b) {
 size_t drot_np_workspace_bytes(int mode, int n_rows, int n_cols, int n_groups,
                                const int* bounds) {
   if (n_rows <= 0 || n_cols <= 0) return 0;
-  if (mode == MODE_QR) return scratch_bytes(MODE_QR, n_rows, n_cols, 0);
+  if (mode == MODE_QR) return solve_ws_bytes(MODE_QR, n_rows, n_cols, 0);
   if (mode != MODE_GL || !valid_bounds(n_rows, n_groups, bounds)) return 0;
-  return scratch_bytes(MODE_GL, n_rows, n_cols, n_groups, bounds);
+  return solve_ws_bytes(MODE_GL, n_rows, n_cols, n_groups, bounds);
 }
 
 int drot_np_solve(int mode, const void* c, int c_dtype, const float* p, const float* q,
@@ -802,16 +855,17 @@ int drot_read_result(const void* workspace, drot_result* result, drot_stream_t s
   return read_stats(workspace, result, (cudaStream_t)stream);
 }
 
+// Operator-style workspace: the dual state, then the solve's workspace.
 size_t drot_quadratic_drot_workspace_bytes(int n_rows, int n_cols) {
-  const size_t sc = scratch_bytes(MODE_QR, n_rows, n_cols, 0);
-  if (sc == 0) return 0;
-  return state_layout(sc, n_rows, n_cols).total;
+  const size_t sw = solve_ws_bytes(MODE_QR, n_rows, n_cols, 0);
+  if (sw == 0) return 0;
+  return state_layout(0, n_rows, n_cols).total + sw;
 }
 
 size_t drot_group_lasso_drot_workspace_bytes(int n_rows, int n_cols, int n_class) {
-  const size_t sc = scratch_bytes(MODE_GL, n_rows, n_cols, n_class);
-  if (sc == 0) return 0;
-  return state_layout(sc, n_rows, n_cols).total;
+  const size_t sw = solve_ws_bytes(MODE_GL, n_rows, n_cols, n_class);
+  if (sw == 0) return 0;
+  return state_layout(0, n_rows, n_cols).total + sw;
 }
 
 int drot_quadratic_drot_ex(const void* c, int c_dtype, const float* p, const float* q,
@@ -821,8 +875,8 @@ int drot_quadratic_drot_ex(const void* c, int c_dtype, const float* p, const flo
   if (n_rows <= 0 || n_cols <= 0 || !workspace) return DROT_ERR_INVALID_ARG;
   const size_t sc = scratch_bytes(MODE_QR, n_rows, n_cols, 0);
   if (sc == 0) return DROT_ERR_UNSUPPORTED;
-  const StateLayout L = state_layout(sc, n_rows, n_cols);
-  if (workspace_bytes < L.total) return DROT_ERR_WORKSPACE;
+  const StateLayout L = state_layout(0, n_rows, n_cols);
+  if (workspace_bytes < L.total + sc) return DROT_ERR_WORKSPACE;
   char* ws = (char*)workspace;
   // pytorch/src/qr_drot_cuda_kernel.cu:100-102
   const float s = rho / ((float)n_rows + (float)n_cols);
@@ -836,7 +890,8 @@ int drot_quadratic_drot_ex(const void* c, int c_dtype, const float* p, const flo
                       (cudaStream_t)stream);
   if (rc != DROT_OK) return rc;
   return drot_qr_solve_ex(c, c_dtype, p, q, n_rows, n_cols, s, kappa, max_iters, eps, x, a, b,
-                          phi1, phi2, alpha, workspace, sc, result, stream);
+                          phi1, phi2, alpha, ws + L.total, workspace_bytes - L.total, result,
+                          stream);
 }
 
 int drot_quadratic_drot(const float* c, const float* p, const float* q, int n_rows, int n_cols,
@@ -854,8 +909,8 @@ int drot_group_lasso_drot_ex(const void* c, int c_dtype, const float* p, const f
   if (n_rows <= 0 || n_cols <= 0 || n_class <= 0 || !workspace) return DROT_ERR_INVALID_ARG;
   const size_t sc = scratch_bytes(MODE_GL, n_rows, n_cols, n_class);
   if (sc == 0) return DROT_ERR_UNSUPPORTED;
-  const StateLayout L = state_layout(sc, n_rows, n_cols);
-  if (workspace_bytes < L.total) return DROT_ERR_WORKSPACE;
+  const StateLayout L = state_layout(0, n_rows, n_cols);
+  if (workspace_bytes < L.total + sc) return DROT_ERR_WORKSPACE;
   char* ws = (char*)workspace;
   // pytorch/src/glr_drot_cuda_kernel.cu:255-257
   const float s = rho / ((float)n_rows + (float)n_cols);
@@ -867,7 +922,8 @@ int drot_group_lasso_drot_ex(const void* c, int c_dtype, const float* p, const f
                       (cudaStream_t)stream);
   if (rc != DROT_OK) return rc;
   return drot_gl_solve_ex(c, c_dtype, p, q, n_rows, n_cols, n_class, s, lambda, max_iters, eps,
-                          x, a, b, phi1, phi2, alpha, workspace, sc, result, stream);
+                          x, a, b, phi1, phi2, alpha, ws + L.total, workspace_bytes - L.total,
+                          result, stream);
 }
 
 int drot_group_lasso_drot(const float* c, const float* p, const float* q, int n_rows,
@@ -890,13 +946,13 @@ static float* wrapper_impl(int mode, const float* hc, const float* hp, const flo
     return nullptr;
   }
   const size_t mat = sizeof(float) * (size_t)nr * nc;
-  const size_t sc = mode == MODE_QR ? scratch_bytes(MODE_QR, nr, nc, 0)
-                                    : scratch_bytes(MODE_GL, nr, nc, G);
-  if (sc == 0) {
+  const size_t sw = mode == MODE_QR ? solve_ws_bytes(MODE_QR, nr, nc, 0)
+                                    : solve_ws_bytes(MODE_GL, nr, nc, G);
+  if (sw == 0) {
     g_last_status = DROT_ERR_UNSUPPORTED;
     return nullptr;
   }
-  const StateLayout L = state_layout(sc, nr, nc);
+  const StateLayout L = state_layout(0, nr, nc);  // the state, then the solve's workspace
   cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -912,7 +968,7 @@ static float* wrapper_impl(int mode, const float* hc, const float* hp, const flo
   if (cudaMalloc(&c, mat) != cudaSuccess || cudaMalloc(&x, mat) != cudaSuccess ||
       cudaMalloc(&p, sizeof(float) * nr) != cudaSuccess ||
       cudaMalloc(&q, sizeof(float) * nc) != cudaSuccess ||
-      cudaMalloc(&ws, L.total) != cudaSuccess) {
+      cudaMalloc(&ws, L.total + sw) != cudaSuccess) {
     rc = DROT_ERR_CUDA;
   }
   if (rc == DROT_OK &&
@@ -933,12 +989,12 @@ static float* wrapper_impl(int mode, const float* hc, const float* hp, const flo
       t = t * r_weight;
       const float kappa = 1.0f + t;
       rc = drot_qr_solve(c, p, q, nr, nc, s, kappa, max_iters, eps, x, a, b, phi1, phi2, alpha,
-                         ws, sc, &res, 0);
+                         ws + L.total, sw, &res, 0);
     } else {
       // core/drot_glr.hpp:385: lambda = r_weight / sqrt(n_rows / NGROUPS)
       const float lambda = (float)((double)r_weight / sqrt((double)(nr / G)));
       rc = drot_gl_solve(c, p, q, nr, nc, G, s, lambda, max_iters, eps, x, a, b, phi1, phi2,
-                         alpha, ws, sc, &res, 0);
+                         alpha, ws + L.total, sw, &res, 0);
     }
   }
   cudaEventRecord(e2, 0);
@@ -1032,8 +1088,11 @@ extern "C" int drot_quadratic_drot_noalloc(const float* c, const float* p, const
   if (!c || !p || !q || !x || n_rows <= 0 || n_cols <= 0 || max_iters < 0)
     return DROT_ERR_INVALID_ARG;
   // Size check first: nothing is launched for a problem that does not fit.
-  const size_t need = drot_quadratic_drot_workspace_bytes(n_rows, n_cols);
-  if (need == 0) return DROT_ERR_UNSUPPORTED;
+  // The minimum (without the aligned copies of unaligned columns, which the
+  // solve takes when the rest of the array holds them).
+  const size_t sc = scratch_bytes(MODE_QR, n_rows, n_cols, 0);
+  if (sc == 0) return DROT_ERR_UNSUPPORTED;
+  const size_t need = state_layout(0, n_rows, n_cols).total + sc;
   if (need > (size_t)DROT_NOALLOC_WORKSPACE_BYTES) return DROT_ERR_WORKSPACE;
   void* ws = nullptr;
   const int rc = noalloc_workspace(&ws);
