@@ -1035,6 +1035,37 @@ def run_case(spec):
                           "us_per_iteration": 1e6 * t / max(1, iters),
                           "achieved_GBps": 8.0 * elems * iters / t / 1e9}), flush=True)
         return 0
+    if parts[0] == "diffgl":
+        # the GL half's first n_inst instances in one GLBatch (2 classes, the
+        # C++ wrapper's threshold), iters iterations with every instance
+        # active (eps 0); the second of two launches timed
+        import torch
+        from reg_drot.batch import GLBatch
+        from reg_drot.cost import packed_sqeuclidean_cost
+        dev = torch.device("cuda", 0)
+        shapes, xs, ys, _, _ = diff_workload()
+        n_inst, iters = int(parts[1]), int(parts[2])
+        shapes = shapes[:n_inst]
+        sl = instance_slices(shapes)
+        B = GLBatch(shapes, 2, RHO, ALPHA, 0.0, device=dev, cols_per_tile=256,
+                    convention="wrapper")
+        p, q = B.pack_marginals([torch.full((m,), 1.0 / m) for m, _ in shapes],
+                                [torch.full((n,), 1.0 / n) for _, n in shapes])
+        c = packed_sqeuclidean_cost(B, torch.from_numpy(xs[:sl[-1][0].stop]).to(dev),
+                                    torch.from_numpy(ys[:sl[-1][1].stop]).to(dev), DIFF_SCALE)
+        x = B.empty_x()
+        B.launch(c, p, q, x, iters)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        B.launch(c, p, q, x, iters)
+        b.record()
+        b.synchronize()
+        t = a.elapsed_time(b) / 1e3
+        elems = sum(m * n for m, n in shapes)
+        print(json.dumps({"case": spec, "elements": elems, "solve_s": t,
+                          "us_per_iteration": 1e6 * t / max(1, iters),
+                          "achieved_GBps": 12.0 * elems * iters / t / 1e9}), flush=True)
+        return 0
     if parts[0] == "glbatch":
         import warnings
         import torch

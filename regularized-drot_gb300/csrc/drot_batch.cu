@@ -358,11 +358,13 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
 // 128-bit vectors per lane, all loads issued first): y = max((X + phi1) +
 // phi2 - sC, 0) (kernel_glr.hpp:163-305), stored back, and the float sum of
 // y^2 -- the group norm, a float sum as the reference's atomics make it.
-// The shrink factor max(1 - lambda / (||y|| + 1e-9), 0) follows
-// (kernel_glr.hpp:307-326).  Pass B re-reads the column's y -- just
-// touched, so from L2 -- stores X = y * scale and adds the column, row
-// (per-warp shared row partials wred[row - base]) and mass sums; the
-// column's objective term <C, X> = scale <C, y> comes from pass A.
+// phi1 is staged as -inf on the rows of the 16-byte vectors that lie
+// outside [lo, hi), so y = 0 there with no masks.  The shrink factor
+// max(1 - lambda / (||y|| + 1e-9), 0) follows (kernel_glr.hpp:307-326).
+// Pass B re-reads the column's y -- just touched, so from L2 -- stores X = y
+// * scale and adds the column, row (per-warp shared row partials
+// wred[row - base]) and mass sums; the column's objective term <C, X> =
+// scale <C, y> comes from pass A.  The element math runs on packed pairs.
 // DRAM traffic stays 12 bytes per element, as in the single-pass update.
 // Stores the vector of rows r..r+3 that lie inside [lo, hi); a vector that
 // straddles a group boundary is stored element by element (the rows of the
@@ -387,12 +389,14 @@ __device__ __forceinline__ void batch_gl_tile_columns(const BatchParams& P, cons
   const CT* const cbase = reinterpret_cast<const CT*>(P.c);
   const int lo = T.lo, hi = T.hi, base = lo & ~3;
   const int nsub = (hi - base + 511) / 512;
-  const float s = I.s;
+  const f32x2 ms2 = x2_pack(-I.s, -I.s);
   for (int j = T.c0 + warp; j < T.c1; j += W) {
     const float f2 = __ldcg(P.phi2 + I.col_off + j);
+    const f32x2 f2b = x2_pack(f2, f2);
     float* xcol = P.x + I.x_off + (long long)j * I.ld;
     const CT* ccol = cbase + I.c_off + (long long)j * I.ld;
-    float nsl = 0.0f, cy = 0.0f;  // the column's |y|^2 and <C, y> (lane parts)
+    // the column's |y|^2 and <C, y> (lane parts, two per lane)
+    f32x2 ns2 = x2_pack(0.0f, 0.0f), cy2 = ns2;
     for (int sb = 0; sb < nsub; ++sb) {
       float xv[4][VEC], cv[4][VEC];
 #pragma unroll
@@ -409,26 +413,32 @@ __device__ __forceinline__ void batch_gl_tile_columns(const BatchParams& P, cons
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         const int r = base + sb * 512 + v * 128 + lane * VEC;
-        if (r >= hi) continue;
-        const int li = r - base;
+        const float4 f1 = *reinterpret_cast<const float4*>(f1s + (r - base));
+        const f32x2 f1p[2] = {x2_pack(f1.x, f1.y), x2_pack(f1.z, f1.w)};
 #pragma unroll
-        for (int e = 0; e < VEC; ++e) {
-          const bool ok = r + e >= lo && r + e < hi;
-          const float t = fmaf(-s, cv[v][e], (xv[v][e] + f1s[li + e]) + f2);
-          const float y = ok ? fmaxf(t, 0.0f) : 0.0f;
-          xv[v][e] = y;
-          nsl = fmaf(y, y, nsl);
-          cy = fmaf(y, ok ? cv[v][e] : 0.0f, cy);
+        for (int h = 0; h < VEC; h += 2) {
+          const f32x2 c2 = x2_pack(cv[v][h], cv[v][h + 1]);
+          float t0, t1;
+          x2_unpack(x2_fma(ms2, c2, x2_add(x2_add(x2_pack(xv[v][h], xv[v][h + 1]), f1p[h / 2]),
+                                           f2b)), t0, t1);
+          xv[v][h] = fmaxf(t0, 0.0f);
+          xv[v][h + 1] = fmaxf(t1, 0.0f);
+          const f32x2 y2 = x2_pack(xv[v][h], xv[v][h + 1]);
+          ns2 = x2_fma(y2, y2, ns2);
+          cy2 = x2_fma(y2, c2, cy2);
         }
-        gl_store(xcol, r, lo, hi, xv[v]);
+        if (r < hi) gl_store(xcol, r, lo, hi, xv[v]);
       }
     }
-    nsl = warp_sum(nsl);
-    const float scale = gl_shrink(nsl, I.lambda);
+    float a0, a1;
+    x2_unpack(ns2, a0, a1);
+    const float scale = gl_shrink(warp_sum(a0 + a1), I.lambda);
+    const f32x2 sc2 = x2_pack(scale, scale);
+    x2_unpack(cy2, a0, a1);
     // Pass B re-reads only y: the objective's <C, X> of the column is
     // scale <C, y>, summed in pass A.
-    float colp = 0.0f;
-    const float objp = scale * cy;
+    const float objp = scale * (a0 + a1);
+    f32x2 col2 = x2_pack(0.0f, 0.0f);
     for (int sb = 0; sb < nsub; ++sb) {
       float xv[4][VEC];
 #pragma unroll
@@ -440,30 +450,33 @@ __device__ __forceinline__ void batch_gl_tile_columns(const BatchParams& P, cons
       for (int v = 0; v < 4; ++v) {
         const int r = base + sb * 512 + v * 128 + lane * VEC;
         if (r >= hi) continue;
-        const int li = r - base;
-        float4 acc = *reinterpret_cast<float4*>(wred + li);
-        float* ap = reinterpret_cast<float*>(&acc);
+        // rows of the vector outside [lo, hi) hold another group's X
+        if (r < lo || r + 4 > hi) {
 #pragma unroll
-        for (int e = 0; e < VEC; ++e) {
-          const bool ok = r + e >= lo && r + e < hi;
-          const float xn = xv[v][e] * scale;
-          if (ok) {
-            xv[v][e] = xn;
-            ap[e] += xn;
-            colp += xn;
-          }
+          for (int e = 0; e < VEC; ++e)
+            if (r + e < lo || r + e >= hi) xv[v][e] = 0.0f;
         }
-        *reinterpret_cast<float4*>(wred + li) = acc;
+        float4 acc = *reinterpret_cast<float4*>(wred + (r - base));
+        const f32x2 x01 = x2_mul(x2_pack(xv[v][0], xv[v][1]), sc2);
+        const f32x2 x23 = x2_mul(x2_pack(xv[v][2], xv[v][3]), sc2);
+        x2_unpack(x2_add(x2_pack(acc.x, acc.y), x01), acc.x, acc.y);
+        x2_unpack(x2_add(x2_pack(acc.z, acc.w), x23), acc.z, acc.w);
+        col2 = x2_add(col2, x2_add(x01, x23));
+        *reinterpret_cast<float4*>(wred + (r - base)) = acc;
+        x2_unpack(x01, xv[v][0], xv[v][1]);
+        x2_unpack(x23, xv[v][2], xv[v][3]);
         gl_store(xcol, r, lo, hi, xv[v]);
       }
     }
+    x2_unpack(col2, a0, a1);
+    const float colp = a0 + a1;
     float e1;
     two_sum(ms_hi, colp, ms_hi, e1);
     ms_lo += e1;
     two_sum(ob_hi, objp, ob_hi, e1);
     ob_lo += e1;
-    colp = warp_sum(colp);
-    if (lane == 0) P.colpart[I.cp_off + (long long)T.band * I.nc + j] = colp;
+    const float cs = warp_sum(colp);
+    if (lane == 0) P.colpart[I.cp_off + (long long)T.band * I.nc + j] = cs;
   }
 }
 
@@ -1089,12 +1102,13 @@ __global__ void __launch_bounds__(DIM > 0 ? 512 : 256, DIM > 0 ? 1 : 2)
       const BatchInst I = P.inst[T.inst];
       const int lo = T.lo, hi = T.hi;
       if constexpr (GL) {
-        // phi1 of the group's rows (from the 16-byte boundary below lo) and
+        // phi1 of the group's rows from the 16-byte boundary below lo (-inf
+        // on the rows outside [lo, hi), through the last 512-row step) and
         // zeroed per-warp row partials, then the two-pass column walk.
-        const int base = lo & ~3, cover = hi - base;
-        for (int idx = threadIdx.x; idx < cover; idx += blockDim.x) {
+        const int base = lo & ~3, cover = hi - base, span = (cover + 511) / 512 * 512;
+        for (int idx = threadIdx.x; idx < span; idx += blockDim.x) {
           const int r = base + idx;
-          f1s[idx] = r >= lo ? __ldcg(P.phi1 + I.row_off + r) : 0.0f;
+          f1s[idx] = (r >= lo && r < hi) ? __ldcg(P.phi1 + I.row_off + r) : -INFINITY;
         }
         for (int idx = threadIdx.x; idx < W * S; idx += blockDim.x) red[idx] = 0.0f;
         __syncthreads();
