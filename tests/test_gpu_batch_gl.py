@@ -139,6 +139,37 @@ def test_gl_batch_graph_replay_and_determinism(cuda, solver_lib):
         assert info == i_ref
 
 
+def test_gl_batch_largest_staged_classes_match_oracle(cuda, solver_lib):
+    """Classes at the staging limit of 4096 rows from the 16-byte boundary
+    below their first row: one 4096-row class, and classes of 4093 rows of
+    which the second starts at row 4093 (staged from row 4092).  The plan's
+    shared staging then admits one CTA per SM.  Fixed iteration counts
+    against the FP32 oracle, then a converged solve against the FP64 one."""
+    shapes = [(4096, 80, 1), (8186, 40, 2), (300, 200, 3)]
+    for mi in (2, 7):
+        B, insts, c, p, q = _batch(shapes, cuda, eps=0.0, cpt=64)
+        x, info = B.solve(c, p, q, mi)
+        for k, ((nr, nc, G), (ci, pi, qi)) in enumerate(zip(shapes, insts)):
+            s = O.step_size(2.0, nr, nc)
+            o = O.gl_solve(ci.numpy(), pi.numpy(), qi.numpy(), O.group_bounds(nr, G), s,
+                           B.lambdas[k], mi, 0.0)
+            assert info[k]["n_iter"] == mi == o["n_iter"]
+            floor = float(np.linalg.norm(pi.numpy()) * np.linalg.norm(qi.numpy()))
+            xg = B.view(x, k).cpu().numpy().astype(np.float64)
+            assert np.linalg.norm(xg - o["x"]) <= 1e-5 * max(np.linalg.norm(o["x"]), floor), k
+    B, insts, c, p, q = _batch(shapes, cuda, cpt=64)
+    x, info = B.solve(c, p, q, 20000)
+    for k, ((nr, nc, G), (ci, pi, qi)) in enumerate(zip(shapes, insts)):
+        s = O.step_size(2.0, nr, nc)
+        bnd = O.group_bounds(nr, G)
+        o32 = O.gl_solve(ci.numpy(), pi.numpy(), qi.numpy(), bnd, s, B.lambdas[k], 20000, 1e-4)
+        o64 = O.gl_solve(ci.numpy(), pi.numpy(), qi.numpy(), bnd, s, B.lambdas[k], 20000, 1e-4,
+                         dtype=np.float64)
+        assert info[k]["converged"] == 1, (k, info[k])
+        ref = _rel(o32["x"], o64["x"])
+        assert _rel(B.view(x, k).cpu().numpy(), o64["x"]) <= max(1e-5, 2.0 * ref), k
+
+
 def test_gl_batch_rejects_classes_taller_than_its_staging(cuda, solver_lib):
     from reg_drot.batch import GLBatch
     B = GLBatch([(9000, 64)], 2, 2.0, 1e-3, 1e-4, device=cuda, cols_per_tile=64)
