@@ -964,17 +964,47 @@ drot_solve_kernel(const SolveParams P) {
           if (slow) body(std::true_type());
           else body(std::false_type());
         } else {
+          // y = max((X + phi1) + phi2 - sC, 0); 4-wide vectors on packed
+          // pairs (each lane rounded as the scalar code), the group norm's
+          // lane part then in two partial sums.
           float nsl = 0.0f;
+          if constexpr (VEC == 4) {
+            const f32x2 ms2 = x2_pack(-s, -s), f2b = x2_pack(f2, f2);
+            f32x2 n2 = x2_pack(0.0f, 0.0f);
 #pragma unroll
-          for (int v = 0; v < KV; ++v)
+            for (int v = 0; v < KV; ++v)
 #pragma unroll
-            for (int e = 0; e < VEC; ++e) {
-              const float t = fmaf(-s, c_at<CT>(cv[v], e), (xv[v][e] + f1[v][e]) + f2);
-              float y = fmaxf(t, 0.0f);
-              if constexpr (!FULL) y = einf(v, e) ? y : 0.0f;
-              xv[v][e] = y;
-              nsl = fmaf(y, y, nsl);
-            }
+              for (int h = 0; h < 4; h += 2) {
+                const f32x2 c2 = x2_pack(c_at<CT>(cv[v], h), c_at<CT>(cv[v], h + 1));
+                float t0, t1;
+                x2_unpack(x2_fma(ms2, c2, x2_add(x2_add(x2_pack(xv[v][h], xv[v][h + 1]),
+                                                        x2_pack(f1[v][h], f1[v][h + 1])), f2b)),
+                          t0, t1);
+                float y0 = fmaxf(t0, 0.0f), y1 = fmaxf(t1, 0.0f);
+                if constexpr (!FULL) {
+                  y0 = einf(v, h) ? y0 : 0.0f;
+                  y1 = einf(v, h + 1) ? y1 : 0.0f;
+                }
+                xv[v][h] = y0;
+                xv[v][h + 1] = y1;
+                const f32x2 y2 = x2_pack(y0, y1);
+                n2 = x2_fma(y2, y2, n2);
+              }
+            float u0, u1;
+            x2_unpack(n2, u0, u1);
+            nsl = u0 + u1;
+          } else {
+#pragma unroll
+            for (int v = 0; v < KV; ++v)
+#pragma unroll
+              for (int e = 0; e < VEC; ++e) {
+                const float t = fmaf(-s, c_at<CT>(cv[v], e), (xv[v][e] + f1[v][e]) + f2);
+                float y = fmaxf(t, 0.0f);
+                if constexpr (!FULL) y = einf(v, e) ? y : 0.0f;
+                xv[v][e] = y;
+                nsl = fmaf(y, y, nsl);
+              }
+          }
           // Group norm: a float sum, as the reference's atomics make it.
           nsl = warp_sum(nsl);
           if (Wt > 1) {
@@ -985,16 +1015,36 @@ drot_solve_kernel(const SolveParams P) {
             for (int kk = 0; kk < Wt; ++kk) nsl += slot[kk];
           }
           const float scale = gl_shrink(nsl, P.lambda);
+          if constexpr (VEC == 4) {
+            const f32x2 sc2 = x2_pack(scale, scale);
+            f32x2 col2 = x2_pack(0.0f, 0.0f), obj2 = col2;
 #pragma unroll
-          for (int v = 0; v < KV; ++v)
+            for (int v = 0; v < KV; ++v)
 #pragma unroll
-            for (int e = 0; e < VEC; ++e) {
-              const float y = xv[v][e] * scale;
-              xv[v][e] = y;
-              acc[v][e] += y;
-              colp += y;
-              objp = fmaf(y, c_at<CT>(cv[v], e), objp);
-            }
+              for (int h = 0; h < 4; h += 2) {
+                const f32x2 y2 = x2_mul(x2_pack(xv[v][h], xv[v][h + 1]), sc2);
+                x2_unpack(y2, xv[v][h], xv[v][h + 1]);
+                x2_unpack(x2_add(x2_pack(acc[v][h], acc[v][h + 1]), y2), acc[v][h], acc[v][h + 1]);
+                col2 = x2_add(col2, y2);
+                obj2 = x2_fma(y2, x2_pack(c_at<CT>(cv[v], h), c_at<CT>(cv[v], h + 1)), obj2);
+              }
+            float u0, u1;
+            x2_unpack(col2, u0, u1);
+            colp = u0 + u1;
+            x2_unpack(obj2, u0, u1);
+            objp = u0 + u1;
+          } else {
+#pragma unroll
+            for (int v = 0; v < KV; ++v)
+#pragma unroll
+              for (int e = 0; e < VEC; ++e) {
+                const float y = xv[v][e] * scale;
+                xv[v][e] = y;
+                acc[v][e] += y;
+                colp += y;
+                objp = fmaf(y, c_at<CT>(cv[v], e), objp);
+              }
+          }
         }
 
 #pragma unroll
