@@ -39,7 +39,7 @@ forward + backward of the differentiable OT loss over one batch:
 `--impl reference` times that CPU implementation alone.  The reference's own
 CPU solver is numpy, whose sources do not reach the GPU host; the oracle port
 stands in for it (on the reference's CPU-runnable 1000^2 case the numpy
-solver takes 42.6 ms per iteration and the port 0.80 ms on the same 8 cores:
+solver takes 47.0 ms per iteration and the port 0.54 ms on the same 8 cores:
 oracle/time_reference_numpy.py).
 
 Multi-GPU: the instances are independent and a step does not shard; N ranks
@@ -967,10 +967,14 @@ def run_batch_timeline(workload="config4"):
 
 
 def run_case(spec):
-    """One solve of the headline workload at size n for a fixed iteration count
-    (for profiler captures): --case n:iters[:gl][:bf16]; --case diff:n_inst:iters
-    for the differentiable workload's kernels; --case batchlog for the
-    batched solver's per-iteration timeline."""
+    """Single cases for profiler captures and one-off measurements:
+    n:iters[:gl][:bf16] (one dense solve at a fixed iteration count),
+    diff:n_inst:iters (the differentiable workload's kernels),
+    batchlog[:diff|:gl] (the batched solver's per-iteration timeline),
+    conv:n:alpha[:bf16] (one dense solve to its stop), diffpts:n_inst:iters
+    (the point-cloud launch), diffgl:n_inst:iters (the GL batch, every
+    instance active) and glbatch:n_inst (the GL half of the differentiable
+    workload with its gradient)."""
     import torch
     import reg_drot
     parts = spec.split(":")
@@ -983,8 +987,6 @@ def run_case(spec):
         # conv:n:alpha[:bf16] (C ~ U[0,1), Dirichlet marginals, as configured
         # for the 3000^2 / 10000^2 workloads); the residual is recomputed
         # from X in FP64
-        import torch
-        import reg_drot
         dev = torch.device("cuda", 0)
         n, alpha = int(parts[1]), float(parts[2])
         c, p, q, eps = make_problem(n)
@@ -1010,7 +1012,6 @@ def run_case(spec):
         # the first n_inst instances of the differentiable workload through the
         # point-cloud launch (cost recomputed on the tensor cores), iters
         # iterations, every instance active
-        import torch
         from reg_drot.batch import QRBatch
         dev = torch.device("cuda", 0)
         shapes, xs, ys, _, eps = diff_workload()
@@ -1039,7 +1040,6 @@ def run_case(spec):
         # the GL half's first n_inst instances in one GLBatch (2 classes, the
         # C++ wrapper's threshold), iters iterations with every instance
         # active (eps 0); the second of two launches timed
-        import torch
         from reg_drot.batch import GLBatch
         from reg_drot.cost import packed_sqeuclidean_cost
         dev = torch.device("cuda", 0)
@@ -1068,7 +1068,6 @@ def run_case(spec):
         return 0
     if parts[0] == "glbatch":
         import warnings
-        import torch
         warnings.simplefilter("ignore")
         dev = torch.device("cuda", 0)
         shapes, xs, ys, w, eps = diff_workload()
