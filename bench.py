@@ -666,7 +666,7 @@ def diff_gl_point(dev, shapes, xs, ys, w, eps, gl_inst=8, gl_iters=20000):
             "lambda_convention": "wrapper"}
 
 
-def diff_gl_batched(dev, shapes, xs, ys, w, eps, gl_inst, gl_iters=20000, steps=1):
+def diff_gl_batched(dev, shapes, xs, ys, w, eps, gl_inst, gl_iters=20000, steps=1, cpt=256):
     """The group-lasso half of the differentiable workload through the
     batched solver: the first gl_inst instances in one GLBatch (2 classes,
     the C++ wrapper's threshold), each stopped at its relative 1e-4, packed
@@ -679,7 +679,7 @@ def diff_gl_batched(dev, shapes, xs, ys, w, eps, gl_inst, gl_iters=20000, steps=
     from reg_drot.cost import packed_sqeuclidean_cost
     sh = shapes[:gl_inst]
     sl = instance_slices(sh)
-    B = GLBatch(sh, 2, RHO, ALPHA, eps[:gl_inst], device=dev, cols_per_tile=256,
+    B = GLBatch(sh, 2, RHO, ALPHA, eps[:gl_inst], device=dev, cols_per_tile=cpt,
                 convention="wrapper")
     p, q = B.pack_marginals([torch.full((m,), 1.0 / m) for m, _ in sh],
                             [torch.full((n,), 1.0 / n) for _, n in sh])
@@ -972,9 +972,9 @@ def run_case(spec):
     diff:n_inst:iters (the differentiable workload's kernels),
     batchlog[:diff|:gl] (the batched solver's per-iteration timeline),
     conv:n:alpha[:bf16] (one dense solve to its stop), diffpts:n_inst:iters
-    (the point-cloud launch), diffgl:n_inst:iters (the GL batch, every
-    instance active) and glbatch:n_inst (the GL half of the differentiable
-    workload with its gradient)."""
+    (the point-cloud launch), diffgl:n_inst:iters[:cols_per_tile] (the GL
+    batch, every instance active) and glbatch:n_inst[:cols_per_tile] (the GL
+    half of the differentiable workload with its gradient)."""
     import torch
     import reg_drot
     parts = spec.split(":")
@@ -1045,9 +1045,10 @@ def run_case(spec):
         dev = torch.device("cuda", 0)
         shapes, xs, ys, _, _ = diff_workload()
         n_inst, iters = int(parts[1]), int(parts[2])
+        cpt = int(parts[3]) if len(parts) > 3 else 256
         shapes = shapes[:n_inst]
         sl = instance_slices(shapes)
-        B = GLBatch(shapes, 2, RHO, ALPHA, 0.0, device=dev, cols_per_tile=256,
+        B = GLBatch(shapes, 2, RHO, ALPHA, 0.0, device=dev, cols_per_tile=cpt,
                     convention="wrapper")
         p, q = B.pack_marginals([torch.full((m,), 1.0 / m) for m, _ in shapes],
                                 [torch.full((n,), 1.0 / n) for _, n in shapes])
@@ -1072,7 +1073,8 @@ def run_case(spec):
         dev = torch.device("cuda", 0)
         shapes, xs, ys, w, eps = diff_workload()
         n = int(parts[1])
-        out = {"case": spec, "batched": diff_gl_batched(dev, shapes, xs, ys, w, eps, n)}
+        cpt = int(parts[2]) if len(parts) > 2 else 256
+        out = {"case": spec, "batched": diff_gl_batched(dev, shapes, xs, ys, w, eps, n, cpt=cpt)}
         if n <= 8:
             out["one_at_a_time"] = diff_gl_point(dev, shapes, xs, ys, w, eps, gl_inst=n)
         print(json.dumps(out), flush=True)
