@@ -243,3 +243,26 @@ def test_gl_adjoint_batch_plan_is_checked_on_the_host(solver_lib):
     assert solver_lib.drot_gl_adjoint_batch_step(h, None, None, None, None, 0, None) == 1
     solver_lib.drot_gl_adjoint_batch_plan_destroy(h)
     assert solver_lib.drot_gl_adjoint_batch_workspace_bytes(None) == 0
+
+
+def test_gl_batch_plan_is_checked_on_the_host(solver_lib):
+    """drot_gl_batch_plan_create refuses, before any device work, a class
+    count outside 1..n_rows, a negative threshold, a non-positive rho
+    (status 1), and a class whose rows from the 16-byte boundary below its
+    first row exceed the 4096 rows the launch stages (status 4: 8194 rows
+    in two classes of 4097)."""
+    from reg_drot._lib import DrotGlBatchInstance
+    good = dict(n_rows=300, n_cols=200, ld=300, n_groups=3, c_offset=0, x_offset=0,
+                p_offset=0, q_offset=0, rho=2.0, lambda_=1e-3, eps=1e-4)
+    h = ctypes.c_void_p()
+    for change, status in [(dict(n_groups=0), 1), (dict(n_groups=301), 1),
+                           (dict(rho=0.0), 1), (dict(lambda_=-1.0), 1),
+                           (dict(n_rows=8194, ld=8196, n_groups=2), 4)]:
+        arr = (DrotGlBatchInstance * 2)()
+        for d in arr:
+            for k, v in good.items():
+                setattr(d, k, v)
+        for k, v in change.items():
+            setattr(arr[1], k, v)
+        assert solver_lib.drot_gl_batch_plan_create(2, arr, 128, ctypes.byref(h)) == status, change
+        assert not h.value
