@@ -545,10 +545,12 @@ def batch_group_lasso_drot_fn(batch, c, p, q, max_iters, *, last_k=64, segment=N
     packed plans, so the default ceil(sqrt(last_k)) keeps both near their
     minimum (8 + 8 plan copies for last_k = 64).  The gradient does not
     depend on it."""
-    if segment is None:
-        segment = max(1, int(math.ceil(math.sqrt(int(last_k)))))
     if int(last_k) <= 0:
         raise RuntimeError("last_k must be positive")
+    if segment is None:
+        segment = max(1, int(math.ceil(math.sqrt(int(last_k)))))
+    if int(segment) <= 0:
+        raise RuntimeError("segment must be positive")
     return BatchGroupLassoDROTFn.apply(c, p, q, batch, int(max_iters), int(last_k),
                                        int(segment))
 
@@ -566,6 +568,8 @@ def group_lasso_drot_fn(c, p, q, n_class, rho, r_weight, max_iters, eps, *, segm
     n_class), the C++ wrapper)."""
     if last_k is not None and int(last_k) <= 0:
         raise RuntimeError("last_k must be positive")
+    if int(segment) <= 0:
+        raise RuntimeError("segment must be positive")
     return GroupLassoDROTFn.apply(c, p, q, int(n_class), float(rho), float(r_weight),
                                   int(max_iters), float(eps), int(segment), str(convention),
                                   None if last_k is None else int(last_k))

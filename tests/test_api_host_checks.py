@@ -42,6 +42,18 @@ def test_autograd_rejects_zero_regularisation():
                           1e-4)
 
 
+def test_gl_autograd_rejects_bad_unroll_settings():
+    """last_k and the checkpoint spacing must be positive (a zero spacing
+    would recompute nothing); checked before the solve starts."""
+    from reg_drot.autograd import batch_group_lasso_drot_fn, group_lasso_drot_fn
+    c, p, q = torch.zeros(3, 2), torch.ones(2) / 2, torch.ones(3) / 3
+    for kw in (dict(last_k=0), dict(segment=0), dict(segment=-3)):
+        with pytest.raises(RuntimeError, match="positive"):
+            group_lasso_drot_fn(c, p, q, 1, 2.0, 1e-3, 10, 1e-4, **kw)
+        with pytest.raises(RuntimeError, match="positive"):
+            batch_group_lasso_drot_fn(None, c.view(-1), p, q, 10, **kw)
+
+
 def test_npdrot_rejects_unsupported_arguments():
     from reg_drot import npdrot
     C = np.asfortranarray(np.random.default_rng(0).random((4, 3)))
