@@ -117,7 +117,7 @@ struct Plan {
 };
 
 struct DeviceInfo {
-  int dev = 0, sms = 0, smem_optin = 0;
+  int dev = 0, sms = 0, smem_optin = 0, l2 = 0;
   bool ok = false;
 };
 
@@ -127,6 +127,7 @@ static DeviceInfo device_info() {
   if (cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, d.dev) != cudaSuccess)
     return d;
   cudaDeviceGetAttribute(&d.smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, d.dev);
+  cudaDeviceGetAttribute(&d.l2, cudaDevAttrL2CacheSize, d.dev);
   int coop = 0;
   cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, d.dev);
   d.ok = coop != 0 && d.sms > 0;
@@ -210,8 +211,25 @@ static int make_plan_uncached(int mode, int nr, int nc, int G, int vec, bool tma
     if (pl.kv == 0) {
       // Groups taller than one warp covers: teams of 4-vector warps (the
       // 8-vector kernel spills at the register cap; measured at 3000^2 with
-      // two 1500-row groups: 26.7 us per iteration against 31.8).
-      if (!kv_pinned) kvcap = std::min(kvcap, 4);
+      // two 1500-row groups: 26.7 us per iteration against 31.8) -- unless
+      // X + C lie beyond L2 and 8-vector teams fill at least 3 more warp
+      // slots of the CTA (the kernel holds one CTA per SM, and the update is
+      // latency-bound): 6000^2, 3000-row groups, 15 warps against 12: 86.3
+      // against 95.4 us per iteration; 10000^2, 5000-row groups, 15 against
+      // 10: 213 against 286 us.  With equal warps (5000^2, 8192 x 3000) the
+      // 4-vector teams measured as fast or faster.
+      if (!kv_pinned) {
+        kvcap = 4;
+        auto team_warps = [&](int kv) {
+          const int wt = (hmax + kv * SV - 1) / (kv * SV);
+          const int cap = wt >= 3 ? 16 : 8;
+          return wt >= cap ? wt : (cap / wt) * wt;
+        };
+        const bool beyond_l2 = (double)nr * (double)nc * 8.0 > (double)dev.l2;
+        if (!tma && vec == 4 && ctype == DROT_C_F32 && beyond_l2 &&
+            team_warps(8) <= 16 && team_warps(8) >= team_warps(4) + 3)
+          kvcap = 8;
+      }
       pl.kv = kvcap;
       pl.wt = (hmax + kvcap * SV - 1) / (kvcap * SV);
       if (pl.wt > 16) return DROT_ERR_UNSUPPORTED;

@@ -189,6 +189,22 @@ def test_fixed_iteration_counts_match_oracle(cuda, path, kind, iters):
         _assert_close_x(x.cpu().numpy(), o["x"])
 
 
+def test_tall_classes_beyond_l2_match_oracle(cuda):
+    """GL with 3000-row classes on a 6000 x 6000 problem (X + C = 288 MB,
+    beyond L2): the default launch takes teams of 8-vector warps here (15
+    warps per CTA against 12 with 4-vector teams).  Fixed iteration counts
+    against the FP32 oracle."""
+    import reg_drot
+    nr = nc = 6000
+    c, p, q = _problem(nr, nc, seed=60, marg="dirichlet")
+    for iters in (1, 6):
+        x, info, _ = reg_drot.solve_gl(c.to(cuda), p.to(cuda), q.to(cuda), 2, 2.0, 1e-3, iters,
+                                       0.0)
+        o = O.group_lasso_drot(c.numpy(), p.numpy(), q.numpy(), 2, 2.0, 1e-3, iters, 0.0)
+        assert info["n_iter"] == iters == o["n_iter"]
+        _assert_close_x(x.cpu().numpy(), o["x"])
+
+
 def test_first_iteration_is_bitwise_identical_to_oracle(cuda, path):
     """One iteration from the warm start involves no cross-element sums in X,
     so the solver and the FP32 oracle agree bit for bit."""
