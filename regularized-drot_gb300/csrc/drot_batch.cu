@@ -1140,84 +1140,84 @@ __global__ void __launch_bounds__(DIM > 0 ? 512 : 256, DIM > 0 ? 1 : 2)
             P.tile_obj[t] = make_float2(a2.hi, a2.lo);
           }
         }
-        continue;
-      }
-      for (int idx = threadIdx.x; idx < S; idx += blockDim.x) {
-        const int r = lo + idx;
-        f1s[idx] = r < hi ? __ldcg(P.phi1 + I.row_off + r) : 0.0f;
-      }
-      __syncthreads();
-      float acc[4][4];
-#pragma unroll
-      for (int v = 0; v < 4; ++v)
-#pragma unroll
-        for (int e = 0; e < 4; ++e) acc[v][e] = 0.0f;
-      float ms_hi = 0.0f, ms_lo = 0.0f, ob_hi = 0.0f, ob_lo = 0.0f;
-      auto run = [&](auto kvr_tag, auto ev_tag) {
-        constexpr int KVR = decltype(kvr_tag)::value;
-        constexpr bool EV = decltype(ev_tag)::value;
-        if (hi - lo == 128 * KVR)
-          batch_tile_columns<KVR, EV, true, CT>(P, I, T, f1s, acc, ms_hi, ms_lo, ob_hi, ob_lo,
-                                                lane, warp, W);
-        else
-          batch_tile_columns<KVR, EV, false, CT>(P, I, T, f1s, acc, ms_hi, ms_lo, ob_hi, ob_lo,
-                                                 lane, warp, W);
-      };
-      using K1 = std::integral_constant<int, 1>;
-      using K2 = std::integral_constant<int, 2>;
-      using K4 = std::integral_constant<int, 4>;
-      bool point_even = false;
-      if constexpr (DIM > 0) point_even = even;
-      if (point_even) {
-        // the cost from the points on the tensor cores (512-row bands)
-        if constexpr (DIM > 0) {
-          if (!point_tile<DIM, false>(P, I, T, f1s, ps, tmem, s_mbar, mw, red, ms_hi, ms_lo,
-                                      ob_hi, ob_lo)) {
-            aborted = true;
-            atomicExch(P.abort_flag, 1);
-            break;
-          }
-        }
-      } else if (even) {
-        if (T.kvr == 1) run(K1(), std::true_type());
-        else if (T.kvr == 2) run(K2(), std::true_type());
-        else run(K4(), std::true_type());
       } else {
-        if (T.kvr == 1) run(K1(), std::false_type());
-        else if (T.kvr == 2) run(K2(), std::false_type());
-        else run(K4(), std::false_type());
-      }
-      // Tile partials: rows (fixed warp order), mass and objective (float pairs).
-      const fpair wsum = warp_sum_fp(fpair{ms_hi, ms_lo});
-      const fpair wobj = even ? warp_sum_fp(fpair{ob_hi, ob_lo}) : fp_make(0.0f);
-      if (!point_even) {
+        for (int idx = threadIdx.x; idx < S; idx += blockDim.x) {
+          const int r = lo + idx;
+          f1s[idx] = r < hi ? __ldcg(P.phi1 + I.row_off + r) : 0.0f;
+        }
+        __syncthreads();
+        float acc[4][4];
 #pragma unroll
         for (int v = 0; v < 4; ++v)
-          if (v < T.kvr)
-            *reinterpret_cast<float4*>(red + (size_t)warp * S + v * 128 + lane * 4) =
-                make_float4(acc[v][0], acc[v][1], acc[v][2], acc[v][3]);
-      }
-      if (lane == 0) {
-        dscr[warp] = wsum;
-        oscr[warp] = wobj;
-      }
-      __syncthreads();
-      for (int idx = threadIdx.x; idx < S; idx += blockDim.x) {
-        const int r = lo + idx;
-        if (r < hi) {
-          float tsum = 0.0f;
-          for (int w = 0; w < W; ++w) tsum += red[(size_t)w * S + idx];
-          P.rowpart[I.rp_off + (long long)T.chunk * I.nr + r] = tsum;
+#pragma unroll
+          for (int e = 0; e < 4; ++e) acc[v][e] = 0.0f;
+        float ms_hi = 0.0f, ms_lo = 0.0f, ob_hi = 0.0f, ob_lo = 0.0f;
+        auto run = [&](auto kvr_tag, auto ev_tag) {
+          constexpr int KVR = decltype(kvr_tag)::value;
+          constexpr bool EV = decltype(ev_tag)::value;
+          if (hi - lo == 128 * KVR)
+            batch_tile_columns<KVR, EV, true, CT>(P, I, T, f1s, acc, ms_hi, ms_lo, ob_hi, ob_lo,
+                                                  lane, warp, W);
+          else
+            batch_tile_columns<KVR, EV, false, CT>(P, I, T, f1s, acc, ms_hi, ms_lo, ob_hi, ob_lo,
+                                                   lane, warp, W);
+        };
+        using K1 = std::integral_constant<int, 1>;
+        using K2 = std::integral_constant<int, 2>;
+        using K4 = std::integral_constant<int, 4>;
+        bool point_even = false;
+        if constexpr (DIM > 0) point_even = even;
+        if (point_even) {
+          // the cost from the points on the tensor cores (512-row bands)
+          if constexpr (DIM > 0) {
+            if (!point_tile<DIM, false>(P, I, T, f1s, ps, tmem, s_mbar, mw, red, ms_hi, ms_lo,
+                                        ob_hi, ob_lo)) {
+              aborted = true;
+              atomicExch(P.abort_flag, 1);
+              break;
+            }
+          }
+        } else if (even) {
+          if (T.kvr == 1) run(K1(), std::true_type());
+          else if (T.kvr == 2) run(K2(), std::true_type());
+          else run(K4(), std::true_type());
+        } else {
+          if (T.kvr == 1) run(K1(), std::false_type());
+          else if (T.kvr == 2) run(K2(), std::false_type());
+          else run(K4(), std::false_type());
         }
-      }
-      if (warp == 0) {
-        fpair a1 = lane < W ? dscr[lane] : fp_make(0.0f);
-        fpair a2 = lane < W ? oscr[lane] : fp_make(0.0f);
-        a1 = warp_sum_fp(a1);
-        if (even) a2 = warp_sum_fp(a2);
+        // Tile partials: rows (fixed warp order), mass and objective (float pairs).
+        const fpair wsum = warp_sum_fp(fpair{ms_hi, ms_lo});
+        const fpair wobj = even ? warp_sum_fp(fpair{ob_hi, ob_lo}) : fp_make(0.0f);
+        if (!point_even) {
+#pragma unroll
+          for (int v = 0; v < 4; ++v)
+            if (v < T.kvr)
+              *reinterpret_cast<float4*>(red + (size_t)warp * S + v * 128 + lane * 4) =
+                  make_float4(acc[v][0], acc[v][1], acc[v][2], acc[v][3]);
+        }
         if (lane == 0) {
-          P.tile_sum[t] = make_float2(a1.hi, a1.lo);
-          if (even) P.tile_obj[t] = make_float2(a2.hi, a2.lo);
+          dscr[warp] = wsum;
+          oscr[warp] = wobj;
+        }
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < S; idx += blockDim.x) {
+          const int r = lo + idx;
+          if (r < hi) {
+            float tsum = 0.0f;
+            for (int w = 0; w < W; ++w) tsum += red[(size_t)w * S + idx];
+            P.rowpart[I.rp_off + (long long)T.chunk * I.nr + r] = tsum;
+          }
+        }
+        if (warp == 0) {
+          fpair a1 = lane < W ? dscr[lane] : fp_make(0.0f);
+          fpair a2 = lane < W ? oscr[lane] : fp_make(0.0f);
+          a1 = warp_sum_fp(a1);
+          if (even) a2 = warp_sum_fp(a2);
+          if (lane == 0) {
+            P.tile_sum[t] = make_float2(a1.hi, a1.lo);
+            if (even) P.tile_obj[t] = make_float2(a2.hi, a2.lo);
+          }
         }
       }
     }
