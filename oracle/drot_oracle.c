@@ -3,7 +3,8 @@
  *
  * A plain-C CPU restatement of the reference DROT hot path
  * (WangZesen/Regularized-DROT, core/drot_qr.hpp, core/drot_glr.hpp,
- * core/kernel_qr.hpp, core/kernel_glr.hpp, pytorch/src/*_drot_cuda_kernel.cu).
+ * core/kernel_qr.hpp, core/kernel_glr.hpp, pytorch/src/qr_drot_cuda_kernel.cu,
+ * pytorch/src/glr_drot_cuda_kernel.cu).
  * It is the checker for the CUDA solver: tests, the smoke check and the CPU
  * baseline leg of the benchmark call it; the solver library never does.
  *
