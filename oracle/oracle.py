@@ -13,7 +13,6 @@ Arrays are numpy, column-major X/C given as a [n_cols, n_rows] C-order array
 (the reference's PyTorch layout).
 """
 import ctypes
-import os
 
 import numpy as np
 

@@ -19,8 +19,6 @@ FP32 sums in a fixed order).
 x_cat, y_cat)`` builds every instance of a QRBatch straight into its packed
 C buffer (x_cat, y_cat: the instances' points concatenated in order).
 """
-import ctypes
-
 import torch
 
 from ._lib import DrotCostInstance, check, lib

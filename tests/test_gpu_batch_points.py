@@ -19,7 +19,6 @@ pytestmark = pytest.mark.gpu
 
 torch = pytest.importorskip("torch")
 
-from oracle import adjoint as A  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
 SHAPES = [(64, 96), (300, 257), (513, 200), (130, 1100), (1000, 700), (2, 3), (257, 129)]
