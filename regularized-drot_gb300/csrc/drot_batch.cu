@@ -17,6 +17,7 @@
 // those of the single-instance solver (core/drot_qr.hpp:159-234).
 #include <cuda_runtime.h>
 
+#include <limits.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -359,7 +360,8 @@ __device__ __forceinline__ void batch_tile_columns(const BatchParams& P, const B
 // phi2 - sC, 0) (kernel_glr.hpp:163-305), stored back, and the float sum of
 // y^2 -- the group norm, a float sum as the reference's atomics make it.
 // phi1 is staged as -inf on the rows of the 16-byte vectors that lie
-// outside [lo, hi), so y = 0 there with no masks.  The shrink factor
+// outside [lo, hi), so y = 0 there with no per-element masks (only the C
+// of the caller's padding rows is zeroed, for <C, y>).  The shrink factor
 // max(1 - lambda / (||y|| + 1e-9), 0) follows (kernel_glr.hpp:307-326).
 // Pass B re-reads the column's y -- just touched, so from L2 -- stores X = y
 // * scale and adds the column, row (per-warp shared row partials
@@ -389,6 +391,7 @@ __device__ __forceinline__ void batch_gl_tile_columns(const BatchParams& P, cons
   const CT* const cbase = reinterpret_cast<const CT*>(P.c);
   const int lo = T.lo, hi = T.hi, base = lo & ~3;
   const int nsub = (hi - base + 511) / 512;
+  const int pad = (hi == I.nr && (hi & 3)) ? hi : INT_MAX;  // first padding row, if any
   const f32x2 ms2 = x2_pack(-I.s, -I.s);
   for (int j = T.c0 + warp; j < T.c1; j += W) {
     const float f2 = __ldcg(P.phi2 + I.col_off + j);
@@ -413,6 +416,15 @@ __device__ __forceinline__ void batch_gl_tile_columns(const BatchParams& P, cons
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         const int r = base + sb * 512 + v * 128 + lane * VEC;
+        // The caller's padding rows below ld (the last class's vector that
+        // holds row n_rows - 1) may hold any value: their C is zeroed, as y
+        // = 0 there and <C, y> must not see a NaN (a neighbouring class's
+        // rows hold finite costs).
+        if (r + 4 > pad) {
+#pragma unroll
+          for (int e = 0; e < VEC; ++e)
+            if (r + e >= hi) cv[v][e] = 0.0f;
+        }
         const float4 f1 = *reinterpret_cast<const float4*>(f1s + (r - base));
         const f32x2 f1p[2] = {x2_pack(f1.x, f1.y), x2_pack(f1.z, f1.w)};
 #pragma unroll

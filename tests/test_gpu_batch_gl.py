@@ -124,6 +124,26 @@ def test_gl_batch_wrapper_convention_and_bf16_cost(cuda, solver_lib):
         assert _rel(B.view(x, k).cpu().numpy(), o64["x"]) <= max(1e-5, 2.0 * ref), k
 
 
+def test_gl_batch_ignores_padding_rows(cuda, solver_lib):
+    """Rows between n_rows and ld belong to the caller: NaN there changes
+    neither the plans nor any reported figure (the objective included)."""
+    B, insts, c, p, q = _batch(SHAPES, cuda, cpt=64)
+    x1, i1 = B.solve(c, p, q, 20000)
+    x1 = x1.clone()
+    c2 = c.clone()
+    padded = 0
+    for k, (nr, nc, _) in enumerate(SHAPES):
+        ld, off = B.lds[k], B.offsets[k]
+        if ld > nr:
+            c2[off:off + ld * nc].view(nc, ld)[:, nr:] = float("nan")
+            padded += 1
+    assert padded >= 2
+    x2, i2 = B.solve(c2, p, q, 20000)
+    for k in range(len(SHAPES)):
+        assert torch.equal(B.view(x1, k), B.view(x2, k)), k
+        assert i1[k] == i2[k], k
+
+
 def test_gl_batch_graph_replay_and_determinism(cuda, solver_lib):
     B, insts, c, p, q = _batch(SHAPES[:5], cuda, cpt=64)
     x_ref, i_ref = B.solve(c, p, q, 20000)
