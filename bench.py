@@ -295,7 +295,6 @@ def run_reference(args):
     return 0
 
 
-
 def hbm_point(dev, flush):
     """QR at 10000^2 (X + C = 800 MB, beyond L2) for a fixed iteration count."""
     import torch
